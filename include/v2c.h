@@ -1,0 +1,279 @@
+/*
+ * v2c.h -- C ABI of the GB300 marker-in-cell (MIC) step of VELO2CYCLEs.
+ *
+ * The reference program (src/i2evps.c) calls four routines per time step
+ * with no arguments; they read and write fixed-size global arrays declared in
+ * src/headevps.c and src/input_RSF.c:
+ *
+ *   marker2nodes()                  src/interpolation.c:55-926
+ *   interpolate_center2basic_old()  src/interpolation.c:1575-1598
+ *   nodes2markers()                 src/interpolation.c:929-1048
+ *   moveandrotatemarkers()          src/moveandrotatemarkers.c:1-178
+ *
+ * plus the node loops compute_before_solve / compute_after_solve
+ * (src/plastic.c:2-129) inside the Stokes Picard loop.
+ *
+ * This header replaces that global-array seam with explicit handles:
+ * a context owns the device copies of the grid, the rock table, the marker
+ * arrays and the node arrays.  Arrays cross the boundary as plain host
+ * pointers in the reference's own layout (FP64, node index m3 = m1*ynumy+m2,
+ * y fastest; markers indexed by the reference marker number).  Every entry
+ * point returns an int status (V2C_OK = 0).  A context is single-stream and
+ * not thread-safe; contexts are independent.
+ */
+#ifndef V2C_H
+#define V2C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+enum {
+  V2C_OK = 0,
+  V2C_ERR_ARG = 1,          /* bad argument (null pointer, size mismatch)        */
+  V2C_ERR_CAPACITY = 2,     /* more markers/nodes than the context was made for  */
+  V2C_ERR_CUDA = 3,         /* a CUDA runtime call failed                        */
+  V2C_ERR_UNSUPPORTED = 4,  /* configuration outside what the kernels implement  */
+  V2C_ERR_NAN = 5,          /* NaN / non-positive viscosity detected (errcheck)  */
+  V2C_ERR_NOCONV = 6,       /* per-marker Newton did not converge for some marker */
+  V2C_ERR_STATE = 7         /* call order violated (e.g. no markers uploaded)     */
+};
+
+#define V2C_MAXTMR 200 /* rock types, src/headevps.c:15 */
+
+/* ------------------------------------------------------------------ params
+ * Scalars and flags the reference keeps as globals.  Defaults in brackets are
+ * the shipped configuration (src/mode_RSF.t3c, src/input_RSF.c:13-63). */
+typedef struct v2c_params {
+  long xnumx, ynumy;        /* grid lines            headevps.c:36            */
+  double xsize, ysize;      /* model size, m         headevps.c:40            */
+  double xstpx, ystpy;      /* mean grid steps       headevps.c:46            */
+  double timesum;           /* time from start, s    headevps.c:446           */
+  double timestep;          /* current dt, s         headevps.c:440           */
+  int interpolationmod;     /* [2] 1: 13-node stencil, 2: 1-2|d| kernel     */
+  int antidiffinter;        /* [1]                                           */
+  int markmod;              /* [1] 1 Euler, 0/2 RK4 (2 also averages spin)    */
+  int stoksmod;             /* [1] 1 rotation formula, 2 Jaumann              */
+  int outgrid;              /* [2]                                           */
+  int densimod;             /* [0]                                           */
+  int RSFmode;              /* [1]                                           */
+  int power_law_RSF;        /* [0]                                           */
+  int rkmod;                /* [0]                                           */
+  int stickymod;            /* [1]                                           */
+  int inertyn;              /* [0] radiation damping on                       */
+  int pmode;                /* [0] normal stress = nstress                    */
+  int tempmod;              /* [1] tkrecalc after the scatter                 */
+  int compressiblemode;     /* [0]                                           */
+  int reloadfromDP;         /* [0]                                           */
+  double nubeg, nuend;      /* [1e1, 1.667e27] viscosity limits              */
+  double nstress;           /* [10e6] effective normal stress, Pa            */
+  double Dphis;             /* [0] state diffusion (ghost copy when > 0)     */
+  double zdeep, tdeep;      /* markers coming from depth: T reset            */
+  double eps2;              /* eps[2]: T given to newly incoming markers     */
+  /* rate-and-state parameters, input_RSF.c:30-56 */
+  double a_vw, b_vw, L_vw, V0_vw;
+  double a_vs, b_vs, L_vs, V0_vs;
+  double a_hr, b_hr, L_hr, V0_hr;
+  double start_updip, end_updip, start_downdip, end_downdip, half_range;
+  /* frictional band: |y - (fault_y + fault_slope*x)| <= fault_hw.  The
+   * reference hard-codes fault_y=10e3, fault_hw=100, fault_slope=0
+   * (calc_RSF.c:226-230); a non-zero slope gives a dipping megathrust. */
+  double fault_y, fault_hw, fault_slope;
+  /* per-marker visco-elasto-plastic + RSF Newton (no counterpart in the
+   * reference; see v2c_rsf_newton) */
+  double faultwidth;        /* [400] m, plastic.c:22                          */
+  double newton_rtol;       /* [1e-10] relative residual                      */
+  int newton_maxit;         /* [60]                                           */
+  int newton_guess;         /* V2C_GUESS_*                                    */
+} v2c_params;
+
+/* initial-guess modes of the per-marker Newton */
+enum { V2C_GUESS_PLAIN = 0, V2C_GUESS_LEARNED = 1, V2C_GUESS_OFF = 2 };
+
+/* -------------------------------------------------------------- rock table
+ * Per-type coefficients, each a double[V2C_MAXTMR] row, headevps.c:256-272. */
+enum {
+  V2C_RT_GG = 0, /* markgg shear modulus            */
+  V2C_RT_NU,     /* marknu                          */
+  V2C_RT_DH,     /* markdh activation energy        */
+  V2C_RT_DV,     /* markdv activation volume        */
+  V2C_RT_SS,     /* markss                          */
+  V2C_RT_MM,     /* markmm power-law exponent       */
+  V2C_RT_RO,     /* markro                          */
+  V2C_RT_BB,     /* markbb                          */
+  V2C_RT_AA,     /* markaa                          */
+  V2C_RT_CP,     /* markcp                          */
+  V2C_RT_KT,     /* markkt                          */
+  V2C_RT_HT,     /* markht                          */
+  V2C_RT_KF,     /* markkf                          */
+  V2C_RT_KP,     /* markkp                          */
+  V2C_RT_N0,     /* markn0 viscosity lower limit    */
+  V2C_RT_N1,     /* markn1 viscosity upper limit    */
+  V2C_RT_IM,     /* markim immobility flag (0/1)    */
+  V2C_RT_N
+};
+
+/* ------------------------------------------------------------ marker fields
+ * Same names as the reference arrays (headevps.c:209-248, input_RSF.c:11).
+ * The rock type markt is a separate signed char array. */
+enum {
+  V2C_MF_X = 0, V2C_MF_Y, V2C_MF_K, V2C_MF_D, V2C_MF_E, V2C_MF_P, V2C_MF_W,
+  V2C_MF_EXX, V2C_MF_EXY, V2C_MF_XX, V2C_MF_XY, V2C_MF_V, V2C_MF_VX, V2C_MF_VY,
+  V2C_MF_C, V2C_MF_C0, V2C_MF_FRIC_STATIC, V2C_MF_PHI, V2C_MF_A, V2C_MF_B,
+  V2C_MF_L, V2C_MF_L0, V2C_MF_V0,
+  V2C_MF_SLIPV,  /* per-marker slip rate of the marker Newton (extension) */
+  V2C_MF_N
+};
+
+/* -------------------------------------------------------------- node fields
+ * Same names as the reference node arrays (headevps.c:99-190,
+ * input_RSF.c:3-6).  Each is a double[nodenum]. */
+enum {
+  /* state carried between steps / solver outputs read by the MIC step */
+  V2C_NF_PHIS_IT = 0, V2C_NF_PHIE, V2C_NF_SXY, V2C_NF_SXYEE, V2C_NF_EXY,
+  V2C_NF_EXYEE, V2C_NF_PES, V2C_NF_PEE, V2C_NF_SXX, V2C_NF_SXXEE, V2C_NF_PR,
+  V2C_NF_SPPEE, V2C_NF_EXX, V2C_NF_EXXEE, V2C_NF_VX, V2C_NF_MVXE, V2C_NF_VY,
+  V2C_NF_MVYE, V2C_NF_ESP,
+  /* marker2nodes outputs */
+  V2C_NF_PHIN, V2C_NF_SXYEN, V2C_NF_EXYEN, V2C_NF_PEN, V2C_NF_PHIS,
+  V2C_NF_SXYE, V2C_NF_EXYE, V2C_NF_PE, V2C_NF_MUS_S, V2C_NF_AS, V2C_NF_BS,
+  V2C_NF_LS, V2C_NF_V0S, V2C_NF_COHESION, V2C_NF_NU_M2C, V2C_NF_GG,
+  V2C_NF_SXXEN, V2C_NF_SPPEN, V2C_NF_EXXEN, V2C_NF_SXXE, V2C_NF_SPPE,
+  V2C_NF_EXXE, V2C_NF_ND_M2C, V2C_NF_GD, V2C_NF_BM, V2C_NF_DRO, V2C_NF_DRP,
+  V2C_NF_MVXN, V2C_NF_MVX, V2C_NF_MRX, V2C_NF_MVYN, V2C_NF_MVY, V2C_NF_MRY,
+  V2C_NF_RO, V2C_NF_ET, V2C_NF_HT, V2C_NF_KT, V2C_NF_CP, V2C_NF_TK,
+  V2C_NF_STICKY01, V2C_NF_NU, V2C_NF_ND,
+  /* interpolate_center2basic_old outputs */
+  V2C_NF_EXXES, V2C_NF_SXXES, V2C_NF_SPPES,
+  /* node RSF update (plastic.c) */
+  V2C_NF_SXXS, V2C_NF_RK_SLIPRS_FINAL, V2C_NF_RK_PHIDTS_FINAL,
+  V2C_NF_RK_SLIPRS_SOLVED, V2C_NF_RK_PHIDTS_SOLVED, V2C_NF_SYIELDS,
+  V2C_NF_NUVP_IT, V2C_NF_SLIPRS, V2C_NF_EXXPL, V2C_NF_RK_DELTAS,
+  /* nodes2markers back-scatter sums and outputs */
+  V2C_NF_PHISUM, V2C_NF_WTPHISUM, V2C_NF_SXYSUM, V2C_NF_EXYSUM, V2C_NF_ESUM,
+  V2C_NF_PSUM, V2C_NF_SXXSUM, V2C_NF_EXXSUM, V2C_NF_WTSXXSUM, V2C_NF_VXSUM,
+  V2C_NF_VYSUM, V2C_NF_WTVXSUM, V2C_NF_WTVYSUM, V2C_NF_MRX0, V2C_NF_MRY0,
+  V2C_NF_N
+};
+
+/* ------------------------------------------------------------ status block */
+typedef struct v2c_status {
+  long n_markers;           /* markers held by the context                    */
+  long n_out_of_grid;       /* markers outside the grid after the last move   */
+  long n_far_moves;         /* markers that moved more than one cell          */
+  long n_nan;               /* NaN / non-positive values caught (errcheck)     */
+  long newton_iters;        /* total Newton iterations in the last solve      */
+  long newton_fallbacks;    /* learned guesses rejected for the plain guess   */
+  long newton_nonconv;      /* markers that did not reach the tolerance       */
+  double newton_max_res;    /* largest relative residual after the last solve */
+  long max_cell_count;      /* most markers in one cell after the last sort   */
+  int last_error;           /* last non-zero status returned                   */
+} v2c_status;
+
+typedef struct v2c_ctx v2c_ctx;
+
+/* ================================================================ life cycle
+ * Replaces the static allocation of headevps.c:8-21 (MAXXLN/MAXYLN/MAXMRK):
+ * capacities are fixed per context.  stream may be NULL (the per-thread
+ * default stream is then not used; the context creates its own). */
+int v2c_create(const v2c_params *p, long max_markers, void *cuda_stream,
+               v2c_ctx **out);
+int v2c_destroy(v2c_ctx *ctx);
+/* Re-read the scalar parameters (timesum, timestep, flags) before a call,
+ * as the reference re-reads its globals on every call. */
+int v2c_set_params(v2c_ctx *ctx, const v2c_params *p);
+
+/* Grid lines gx[xnumx], gy[ynumy] (headevps.c:95); xsize == gx[xnumx-1]. */
+int v2c_set_grid(v2c_ctx *ctx, const double *gx, const double *gy);
+/* Rock table rows rt[V2C_RT_N][V2C_MAXTMR] (row-major). */
+int v2c_set_rock_table(v2c_ctx *ctx, const double *rt);
+/* Boundary-condition equations in the reference layout
+ * (headevps.c:205-209): bondm[nodenum*4], bondn[bondnum][3],
+ * bondv[bondnum][4].  Used by the boundary corrections that end
+ * marker2nodes (momentum_continuity_addmatrix_checkerror.c:1002-1184,
+ * temperature_iterate.c:828-891). */
+int v2c_set_bonds(v2c_ctx *ctx, const long *bondm, const long *bondn,
+                  const double *bondv, long bondnum);
+
+/* =========================================================== marker arrays
+ * fields[V2C_MF_N] are host pointers (any may be NULL = not transferred;
+ * X, Y and markt are required on upload).  Markers keep the reference
+ * numbering at the boundary; the device holds them sorted by cell. */
+int v2c_upload_markers(v2c_ctx *ctx, const double *const *fields,
+                       const signed char *markt, long n);
+int v2c_download_markers(v2c_ctx *ctx, double *const *fields,
+                         signed char *markt, long n);
+/* Cell index of every marker (reference numbering) as found on the device:
+ * ix*(ynumy-1)+iy with ix = nxsearch(x), iy = nysearch(y). */
+int v2c_download_cells(v2c_ctx *ctx, int32_t *cell, long n);
+
+/* ============================================================= node arrays */
+int v2c_upload_node_field(v2c_ctx *ctx, int field, const double *src);
+int v2c_download_node_field(v2c_ctx *ctx, int field, double *dst);
+
+/* ======================================================= the MIC step calls
+ * Reference equivalents in brackets.  All are asynchronous on the context
+ * stream except where a status must be read back (noted). */
+int v2c_marker2nodes(v2c_ctx *ctx);                 /* [interpolation.c:55]   */
+int v2c_center2basic_old(v2c_ctx *ctx);             /* [interpolation.c:1575] */
+int v2c_compute_before_solve(v2c_ctx *ctx, double dt, int rk); /* [plastic.c:2] */
+/* returns the RMS of (syield - sigin) in *deltas, [plastic.c:61] (syncs) */
+int v2c_compute_after_solve(v2c_ctx *ctx, double dt, int rk, double *deltas);
+int v2c_nodes2markers(v2c_ctx *ctx);                /* [interpolation.c:929]  */
+int v2c_moveandrotatemarkers(v2c_ctx *ctx);         /* [moveandrotatemarkers.c:1] */
+/* nodes2markers followed by moveandrotatemarkers in one marker pass. */
+int v2c_nodes2markers_move(v2c_ctx *ctx);
+
+int v2c_synchronize(v2c_ctx *ctx);
+int v2c_get_status(v2c_ctx *ctx, v2c_status *st);
+
+/* ================================================ per-marker VEP+RSF Newton
+ * No counterpart in the reference (it resolves stress and slip rate only
+ * through the global Picard loop, momentum_continuity_iterate.c:49-124).
+ * Solves, per state i, for the slip rate V>0 that makes the Maxwell
+ * visco-elasto-plastic stress equal the regularised RSF yield stress
+ *   F(V) = 2 eta_vp Z edot + (1-Z) tau_old - tau_y(V) = 0,
+ *   tau_y(V) = sn a asinh(V/(2V0) exp((mu0 + b phi(V))/a)) + 4.3303e6 V,
+ *   phi(V)   = ageing-law update over dt           (calc_RSF.c:96-103),
+ *   eta_vp   = eta tau_y /(2 eta V/W + tau_y)     (calc_RSF.c:142),
+ *   Z        = G dt /(G dt + eta_vp).
+ * States are device pointers of V2C_RS_N float64 columns of length n
+ * (column-major, see V2C_RS_*).  Outputs: V, phi(V), tau_y(V), and the
+ * Newton iteration count.  guess = V2C_GUESS_PLAIN starts from V_old,
+ * V2C_GUESS_LEARNED from the network loaded with v2c_mlp_load and falls back
+ * to the plain guess when the learned start does not converge. */
+enum {
+  V2C_RS_VOLD = 0, V2C_RS_PHIOLD, V2C_RS_A, V2C_RS_B, V2C_RS_L, V2C_RS_V0,
+  V2C_RS_MU0, V2C_RS_SN, V2C_RS_DT, V2C_RS_TAUOLD, V2C_RS_EDOT, V2C_RS_ETA,
+  V2C_RS_G, V2C_RS_N
+};
+enum { V2C_RO_V = 0, V2C_RO_PHI, V2C_RO_TAU, V2C_RO_RES, V2C_RO_N };
+
+int v2c_rsf_newton(v2c_ctx *ctx, const double *states_dev, long n, int guess,
+                   double *out_dev, int32_t *iters_dev);
+
+/* Multilayer perceptron 8 -> 64 -> 64 -> 2 that proposes the Newton start.
+ * Weights are one packed float32 vector (see V2C_MLP_NPARAM), layout
+ * W1[64][8] b1[64] W2[64][64] b2[64] W3[2][64] b3[2] plus the feature
+ * normalisation mean[8] std[8] and the output scale mean[2] std[2]. */
+#define V2C_MLP_IN 8
+#define V2C_MLP_H 64
+#define V2C_MLP_OUT 2
+#define V2C_MLP_NPARAM (64 * 8 + 64 + 64 * 64 + 64 + 2 * 64 + 2 + 8 + 8 + 2 + 2)
+int v2c_mlp_load(v2c_ctx *ctx, const float *params_host);
+int v2c_mlp_save(v2c_ctx *ctx, float *params_host);
+/* Train on n states (device, as for v2c_rsf_newton) whose Newton solutions
+ * are targets_dev[2][n] = (log V, phi).  Hand-written BF16 tensor-core
+ * forward/backward + Adam; returns the final mean loss. */
+int v2c_mlp_train(v2c_ctx *ctx, const double *states_dev,
+                  const double *targets_dev, long n, int epochs, int batch,
+                  float lr, uint64_t seed, float *final_loss);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* V2C_H */

@@ -1,0 +1,274 @@
+"""ctypes / subprocess front-ends of the two CPU checkers (test infrastructure)."""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+from velo2cycles_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+
+
+def restatement_path() -> str:
+    return os.path.join(OUT, "liboracle.so")
+
+
+def reference_path() -> str:
+    return os.path.join(OUT, "v2c_ref")
+
+
+def build(force: bool = False) -> None:
+    """Compile both checkers with oracle/build_ref.sh (seconds)."""
+    if force or not os.path.exists(restatement_path()) or not os.path.exists(reference_path()):
+        subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True)
+
+
+def reference_available() -> bool:
+    return os.path.exists(reference_path())
+
+
+# ------------------------------------------------------------ restatement
+
+class _State(ctypes.Structure):
+    _fields_ = [
+        ("p", abi.Params),
+        ("gx", ctypes.POINTER(ctypes.c_double)),
+        ("gy", ctypes.POINTER(ctypes.c_double)),
+        ("rt", ctypes.POINTER(ctypes.c_double)),
+        ("N", ctypes.POINTER(ctypes.c_double) * abi.NF_N),
+        ("M", ctypes.POINTER(ctypes.c_double) * abi.MF_N),
+        ("t", ctypes.POINTER(ctypes.c_byte)),
+        ("n", ctypes.c_long),
+        ("bondm", ctypes.POINTER(ctypes.c_long)),
+        ("bondn", ctypes.POINTER(ctypes.c_long)),
+        ("bondv", ctypes.POINTER(ctypes.c_double)),
+        ("bondnum", ctypes.c_long),
+        ("nthreads", ctypes.c_int),
+        ("phantom", ctypes.c_int),
+    ]
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+_LIB = None
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(restatement_path()):
+            build()
+        lib = ctypes.CDLL(restatement_path())
+        P = ctypes.POINTER
+        lib.v2c_oracle_nxsearch.restype = ctypes.c_long
+        lib.v2c_oracle_nxsearch.argtypes = [P(ctypes.c_double), ctypes.c_long, ctypes.c_double]
+        for fn in ("v2c_oracle_marker2nodes", "v2c_oracle_center2basic_old",
+                   "v2c_oracle_nodes2markers", "v2c_oracle_move"):
+            getattr(lib, fn).restype = ctypes.c_int
+            getattr(lib, fn).argtypes = [P(_State)]
+        lib.v2c_oracle_compute_before_solve.restype = ctypes.c_int
+        lib.v2c_oracle_compute_before_solve.argtypes = [P(_State), ctypes.c_double, ctypes.c_int]
+        lib.v2c_oracle_compute_after_solve.restype = ctypes.c_double
+        lib.v2c_oracle_compute_after_solve.argtypes = [P(_State), ctypes.c_double, ctypes.c_int]
+        lib.v2c_oracle_rsf_newton.restype = ctypes.c_long
+        lib.v2c_oracle_rsf_newton.argtypes = [P(ctypes.c_double), ctypes.c_long, ctypes.c_double,
+                                              ctypes.c_double, ctypes.c_int, P(ctypes.c_double),
+                                              P(ctypes.c_double), P(ctypes.c_int)]
+        lib.v2c_oracle_rsf_features.restype = None
+        lib.v2c_oracle_rsf_features.argtypes = [P(ctypes.c_double), ctypes.c_long, ctypes.c_long,
+                                                P(ctypes.c_double)]
+        lib.v2c_oracle_rsf_residual.restype = ctypes.c_double
+        lib.v2c_oracle_rsf_residual.argtypes = [P(ctypes.c_double), ctypes.c_double, ctypes.c_double,
+                                                P(ctypes.c_double), P(ctypes.c_double),
+                                                P(ctypes.c_double), P(ctypes.c_double)]
+        lib.v2c_oracle_mlp_loss_grad.restype = ctypes.c_double
+        lib.v2c_oracle_mlp_loss_grad.argtypes = [P(ctypes.c_float), P(ctypes.c_double),
+                                                 P(ctypes.c_double), ctypes.c_long, P(ctypes.c_double)]
+        lib.v2c_oracle_mlp_forward.restype = None
+        lib.v2c_oracle_mlp_forward.argtypes = [P(ctypes.c_float), P(ctypes.c_double), ctypes.c_long,
+                                               P(ctypes.c_double)]
+        _LIB = lib
+    return _LIB
+
+
+class Restatement:
+    """Runs the C restatement on a copy of a synth.Case (arrays updated in place)."""
+
+    def __init__(self, case, nthreads: int = 1, phantom: bool = False):
+        self.case = case
+        self.lib = _lib()
+        c = case
+        self._keep = []
+        self.nodes = {f: np.ascontiguousarray(c.nodes[f], dtype=np.float64) for f in range(abi.NF_N)}
+        self.marks = {f: np.ascontiguousarray(c.marks[f], dtype=np.float64) for f in range(abi.MF_N)}
+        self.markt = np.ascontiguousarray(c.markt, dtype=np.int8)
+        self.gx = np.ascontiguousarray(c.gx, dtype=np.float64)
+        self.gy = np.ascontiguousarray(c.gy, dtype=np.float64)
+        self.rt = np.ascontiguousarray(c.rt, dtype=np.float64)
+        self.bondm = np.ascontiguousarray(c.bondm, dtype=np.int64)
+        self.bondn = np.ascontiguousarray(c.bondn, dtype=np.int64)
+        self.bondv = np.ascontiguousarray(c.bondv, dtype=np.float64)
+        st = _State()
+        st.p = abi.Params.from_dict(c.params)
+        st.gx, st.gy, st.rt = _dp(self.gx), _dp(self.gy), _dp(self.rt)
+        for f in range(abi.NF_N):
+            st.N[f] = _dp(self.nodes[f])
+        for f in range(abi.MF_N):
+            st.M[f] = _dp(self.marks[f])
+        st.t = self.markt.ctypes.data_as(ctypes.POINTER(ctypes.c_byte))
+        st.n = c.n
+        st.bondm = self.bondm.ctypes.data_as(ctypes.POINTER(ctypes.c_long))
+        st.bondn = self.bondn.ctypes.data_as(ctypes.POINTER(ctypes.c_long))
+        st.bondv = _dp(self.bondv)
+        st.bondnum = c.bondnum
+        st.nthreads = nthreads
+        st.phantom = int(phantom)
+        self.st = st
+
+    def set_params(self, **kw):
+        d = self.st.p.to_dict()
+        d.update(kw)
+        self.st.p = abi.Params.from_dict(d)
+
+    def marker2nodes(self):
+        return self.lib.v2c_oracle_marker2nodes(ctypes.byref(self.st))
+
+    def center2basic_old(self):
+        return self.lib.v2c_oracle_center2basic_old(ctypes.byref(self.st))
+
+    def compute_before_solve(self, dt, rk=0):
+        return self.lib.v2c_oracle_compute_before_solve(ctypes.byref(self.st), dt, rk)
+
+    def compute_after_solve(self, dt, rk=0):
+        return self.lib.v2c_oracle_compute_after_solve(ctypes.byref(self.st), dt, rk)
+
+    def nodes2markers(self):
+        return self.lib.v2c_oracle_nodes2markers(ctypes.byref(self.st))
+
+    def move(self):
+        return self.lib.v2c_oracle_move(ctypes.byref(self.st))
+
+    def step(self):
+        """One MIC step with the solver outputs held fixed."""
+        dt = self.st.p.timestep
+        rc = self.marker2nodes()
+        rc |= self.center2basic_old()
+        rc |= self.compute_before_solve(dt, 0)
+        self.compute_after_solve(dt, 0)
+        rc |= self.nodes2markers()
+        rc |= self.move()
+        return rc
+
+
+def nxsearch(g: np.ndarray, x: float) -> int:
+    g = np.ascontiguousarray(g, dtype=np.float64)
+    return int(_lib().v2c_oracle_nxsearch(_dp(g), g.size, float(x)))
+
+
+def rsf_newton(states: np.ndarray, W=400.0, rtol=1e-10, maxit=200, guess_logV=None):
+    """states: float64[V2C_RS_N, n] -> (out[V2C_RO_N, n], iters[n], nonconv)"""
+    states = np.ascontiguousarray(states, dtype=np.float64)
+    n = states.shape[1]
+    out = np.zeros((abi.RO_N, n))
+    it = np.zeros(n, dtype=np.int32)
+    g = None if guess_logV is None else np.ascontiguousarray(guess_logV, dtype=np.float64)
+    nc = _lib().v2c_oracle_rsf_newton(_dp(states), n, W, rtol, maxit,
+                                      _dp(g) if g is not None else None, _dp(out),
+                                      it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return out, it, nc
+
+
+def rsf_features(states: np.ndarray) -> np.ndarray:
+    states = np.ascontiguousarray(states, dtype=np.float64)
+    n = states.shape[1]
+    X = np.zeros((n, 8))
+    lib = _lib()
+    buf = np.zeros(8)
+    for i in range(n):
+        lib.v2c_oracle_rsf_features(_dp(states), n, i, _dp(buf))
+        X[i] = buf
+    return X
+
+
+def mlp_loss_grad(params: np.ndarray, X: np.ndarray, Y: np.ndarray, want_grad=True):
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    Y = np.ascontiguousarray(Y, dtype=np.float64)
+    ng = abi.MLP_NPARAM - 20
+    g = np.zeros(ng) if want_grad else None
+    loss = _lib().v2c_oracle_mlp_loss_grad(params.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                           _dp(X), _dp(Y), X.shape[0], _dp(g) if want_grad else None)
+    return loss, g
+
+
+def mlp_forward(params: np.ndarray, X: np.ndarray) -> np.ndarray:
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    Y = np.zeros((X.shape[0], 2))
+    _lib().v2c_oracle_mlp_forward(params.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                  _dp(X), X.shape[0], _dp(Y))
+    return Y
+
+
+# -------------------------------------------------------------- reference
+
+STAGE_M2N, STAGE_C2B, STAGE_BEFORE, STAGE_AFTER, STAGE_N2M, STAGE_MOVE = range(6)
+ALL_STAGES = 0b111111
+
+
+def write_case(path: str, case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0) -> None:
+    c = case
+    nn = c.nodenum
+    with open(path, "wb") as f:
+        f.write(b"V2CCASE1")
+        np.array([c.params["xnumx"], c.params["ynumy"], c.n, c.bondnum, nthreads, stages,
+                  nsteps, warmup], dtype=np.int64).tofile(f)
+        f.write(bytes(abi.Params.from_dict(c.params)))
+        np.ascontiguousarray(c.gx, dtype=np.float64).tofile(f)
+        np.ascontiguousarray(c.gy, dtype=np.float64).tofile(f)
+        np.ascontiguousarray(c.rt, dtype=np.float64).tofile(f)
+        for k in range(abi.NF_N):
+            np.ascontiguousarray(c.nodes[k], dtype=np.float64).reshape(nn).tofile(f)
+        for k in range(abi.MF_N):
+            np.ascontiguousarray(c.marks[k], dtype=np.float64).tofile(f)
+        np.ascontiguousarray(c.markt, dtype=np.int8).tofile(f)
+        np.ascontiguousarray(c.bondm, dtype=np.int64).tofile(f)
+        np.ascontiguousarray(c.bondn, dtype=np.int64).tofile(f)
+        np.ascontiguousarray(c.bondv, dtype=np.float64).tofile(f)
+
+
+def read_result(path: str, nodenum: int):
+    with open(path, "rb") as f:
+        assert f.read(8) == b"V2CRES01"
+        n = int(np.fromfile(f, dtype=np.int64, count=1)[0])
+        nodes = {k: np.fromfile(f, dtype=np.float64, count=nodenum) for k in range(abi.NF_N)}
+        marks = {k: np.fromfile(f, dtype=np.float64, count=n) for k in range(abi.MF_N)}
+        markt = np.fromfile(f, dtype=np.int8, count=n)
+        secs = np.fromfile(f, dtype=np.float64, count=8)
+        deltas = float(np.fromfile(f, dtype=np.float64, count=1)[0])
+    return dict(nodes=nodes, marks=marks, markt=markt, seconds=secs, deltas=deltas, n=n)
+
+
+def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeout=3600):
+    """Run the reference routines on `case`; returns the arrays after the
+    stages plus per-stage seconds summed over the timed steps."""
+    if not reference_available():
+        build()
+    if not reference_available():
+        raise RuntimeError("reference oracle not built (reference sources unavailable)")
+    with tempfile.TemporaryDirectory() as d:
+        cp, rp = os.path.join(d, "case.bin"), os.path.join(d, "res.bin")
+        write_case(cp, case, stages, nthreads, nsteps, warmup)
+        env = dict(os.environ, OMP_NUM_THREADS=str(max(1, nthreads)))
+        r = subprocess.run([reference_path(), cp, rp], env=env, capture_output=True,
+                           timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError(f"v2c_ref failed ({r.returncode}): {r.stderr.decode()[-2000:]}")
+        return read_result(rp, case.nodenum)

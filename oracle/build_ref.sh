@@ -1,0 +1,53 @@
+#!/bin/sh
+# Build recipe for the two CPU checkers (test infrastructure only):
+#
+#  1. oracle/_ref/liboracle.so -- the C restatement oracle/v2c_oracle.c.
+#  2. oracle/_ref/v2c_ref      -- the reference's own hot-path routines,
+#     compiled from its sources with oracle/ref_harness.c.
+#
+# For (2) the reference sources are copied from $V2C_REFERENCE/src (default
+# /root/reference/src) into oracle/_ref/src, raising only the array-size
+# macros of headevps.c so larger grids and marker sets fit.  That staging
+# directory is git-ignored; it exists so the same recipe can rebuild the
+# binary on a machine without the reference tree.  When neither the tree nor
+# a staged copy is present only (1) is built.
+#
+# Both are compiled with -ffp-contract=off so FP64 arithmetic is evaluated
+# exactly as written on every host architecture.
+set -e
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+REF="${V2C_REFERENCE:-/root/reference}"
+CC="${CC:-gcc}"
+mkdir -p "$OUT"
+
+$CC -std=gnu99 -O2 -ffp-contract=off -fPIC -shared -Wall \
+    -o "$OUT/liboracle.so" "$HERE/v2c_oracle.c" -lm
+
+FILES="headevps.c input_RSF.c calc_RSF.c gausevps.c interpolation.c \
+density_ductilevisc_calc.c moveandrotatemarkers.c \
+momentum_continuity_addmatrix_checkerror.c temperature_iterate.c plastic.c \
+recalc_marker_properties.c"
+
+if [ -d "$REF/src" ]; then
+  mkdir -p "$OUT/src"
+  for f in $FILES; do cp "$REF/src/$f" "$OUT/src/$f"; done
+  # grid up to 1100 x 420 lines, 2.1 M markers; the Stokes matrix arrays are
+  # only used by the small boundary-correction solves on this path.
+  sed -i \
+    -e 's/^#define MAXMAT .*/#define MAXMAT  8000000/' \
+    -e 's/^#define MAXVAL .*/#define MAXVAL  8000000/' \
+    -e 's/^#define MAXXLN .*/#define MAXXLN  1100/' \
+    -e 's/^#define MAXYLN .*/#define MAXYLN  420/' \
+    -e 's/^#define MAXMRK .*/#define MAXMRK  2100000/' \
+    "$OUT/src/headevps.c"
+fi
+
+if [ -f "$OUT/src/headevps.c" ]; then
+  MODEL=""
+  case "$(uname -m)" in x86_64) MODEL="-mcmodel=medium" ;; esac
+  $CC -std=gnu99 -O3 -fopenmp -fcommon -w -ffp-contract=off $MODEL \
+      -I"$OUT/src" -o "$OUT/v2c_ref" "$HERE/ref_harness.c" -lm
+else
+  echo "build_ref.sh: reference sources not found; built the restatement only" >&2
+fi
