@@ -1,0 +1,361 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 marker-in-cell step (markers per second).
+
+A step is one pass of the per-timestep MIC pipeline over all markers:
+  marker2nodes (cell-sorted scatter with per-marker rheology, node tail,
+  boundary corrections) -> interpolate_center2basic_old ->
+  compute_before_solve / compute_after_solve (node RSF update) ->
+  nodes2markers + moveandrotatemarkers (gather, back-scatter, RK4 advection,
+  stress rotation) -> counting sort of the moved markers.
+The Stokes (Pardiso) and temperature solves are outside the path; their
+outputs are the seeded synthetic node fields already on the device.
+
+Workload: the 4001 x 1001 grid with 20 markers per cell (80 M markers,
+synth.make_case("c4")).  Inputs are larger than L2 (the marker arrays alone
+are ~5.6 GB), so no flush is needed between steps.
+
+`value` is device-timed with CUDA events on the context's stream, inputs
+resident in HBM.  `e2e` is the same step through the C ABI with the node
+fields crossing the host boundary every step, as in the reference time loop
+around its host Stokes solve: the solver outputs are uploaded from pinned
+host memory before nodes2markers and the Stokes inputs are read back after
+marker2nodes.  `--impl reference` times the reference's own C routines
+(compiled from its sources, oracle/_ref) on all host cores on a bounded
+window of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "markers/s per MIC step, learned-guess vs plain Newton, same GPU & residual"
+UNIT = "markers/s"
+
+# algorithmic bytes per marker (FP32/int32 canonical form, each persistent
+# field counted once per read and once per write; node fields spread over
+# the markers per node).  Derivation in the design doc.
+ALG_BYTES = {
+    "m2n": 57 + 4,            # marker reads + phi write
+    "n2m_move": 17 + 48,      # marker reads + writes
+}
+NODE_FIELDS = {"m2n": 18 + 39, "n2m_move": 10 + 24}
+STEP_MARKER_BYTES = 57 + 48
+STEP_NODE_FIELDS = 94
+
+# node fields that cross the host boundary in the e2e loop
+E2E_UP = ["VX", "VY", "PR", "SXX", "SXY", "EXX", "EXY", "ESP"]
+E2E_DOWN = ["NU_M2C", "GG", "ND_M2C", "GD", "RO", "MRX", "MRY", "MVX", "MVY", "SPPE",
+            "SXXE", "SXYE", "EXXE", "EXYE", "PHIS", "TK"]
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ helpers
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get(kernel)
+    return None
+
+
+def cpu_baseline(steps: int = 3, warmup: int = 1, threads: int | None = None) -> dict:
+    """Reference routines (oracle/_ref, compiled from the reference sources)
+    on a window of the same workload, all host cores."""
+    import oracle
+    from oracle import bindings as B
+    from velo2cycles_gb300 import synth
+
+    oracle.build()
+    threads = threads or os.cpu_count() or 1
+    case = synth.make_case("c4", seed=1, window=(1200, 0, 401, 101))
+    if B.reference_available():
+        res = B.run_reference(case, nthreads=threads, nsteps=steps, warmup=warmup)
+        secs = float(res["seconds"][:6].sum()) / steps
+        kind = "reference"
+    else:
+        r = oracle.Restatement(case.copy())
+        for _ in range(warmup):
+            r.step()
+        t = time.perf_counter()
+        for _ in range(steps):
+            r.step()
+        secs = (time.perf_counter() - t) / steps
+        threads, kind = 1, "port"
+    return {"value": case.n / secs, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"c4 window of 401x101 grid lines at the c4 spacing, {case.n} markers, "
+                      f"{warmup} warm-up + {steps} timed steps, full MIC step",
+            "seconds_per_step": secs}
+
+
+# ------------------------------------------------------- reference arm
+def run_reference_arm(args, rank: int) -> None:
+    if rank != 0:
+        return
+    base = cpu_baseline(steps=args.steps, warmup=args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": base["seconds_per_step"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "c4 marker-in-cell step (bounded window, see cpu_baseline.sample)"},
+        "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------- GPU arm
+def run_gpu(args, rank: int, world: int) -> None:
+    import torch
+
+    from velo2cycles_gb300 import abi, build, mic, synth
+
+    build.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    t0 = time.time()
+    case = synth.make_case(args.config, seed=1 + rank)
+    log(f"[bench] {args.config}: {case.n} markers, {case.nodenum} nodes, generated in "
+        f"{time.time() - t0:.1f}s")
+    stream = torch.cuda.Stream()
+    m = mic.MarkerInCell(case.params, case.n, stream=stream.cuda_stream)
+    m.set_grid(case.gx, case.gy)
+    m.set_rock_table(case.rt)
+    m.set_bonds(case.bondm, case.bondn, case.bondv)
+    m.upload_markers(case.marks, case.markt)
+    m.upload_nodes(case.nodes)
+    m.synchronize()
+    n = case.n
+    dt = case.params["timestep"]
+    log(f"[bench] uploaded in {time.time() - t0:.1f}s")
+
+    def step():
+        m.marker2nodes()
+        m.interpolate_center2basic_old()
+        m.compute_before_solve(dt, 0)
+        m.compute_after_solve(dt, 0)
+        m.nodes2markers_move()
+
+    for _ in range(args.warmup):
+        step()
+    m.synchronize()
+
+    # device-timed steps; the library brackets each kernel group with CUDA
+    # events on its own stream (v2c_set_profiling)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    st0 = m.status()
+    m.set_profiling(True)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(args.steps):
+        step()
+    end.record(stream)
+    torch.cuda.synchronize()
+    st1 = m.status()
+    prof = m.profile()
+    m.set_profiling(False)
+    ms_total = start.elapsed_time(end)
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    stage_ms = {k: (v[0] / args.steps) for k, v in prof.items() if v[1] > 0}
+    ms = ms_total / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms * 1e-3)
+
+    # end to end through the C ABI with host node buffers
+    nn = case.nodenum
+    up = {getattr(abi, "NF_" + f): torch.from_numpy(case.nodes[getattr(abi, "NF_" + f)]).pin_memory().numpy()
+          for f in E2E_UP}
+    down = {getattr(abi, "NF_" + f): torch.empty(nn, dtype=torch.float64, pin_memory=True).numpy()
+            for f in E2E_DOWN}
+    import ctypes
+
+    from velo2cycles_gb300._lib import call
+
+    dp = ctypes.POINTER(ctypes.c_double)
+
+    def e2e_step():
+        m.marker2nodes()
+        for f, a in down.items():
+            call("v2c_download_node_field", m.h, f, a.ctypes.data_as(dp))
+        m.interpolate_center2basic_old()
+        m.compute_before_solve(dt, 0)
+        m.compute_after_solve(dt, 0)
+        for f, a in up.items():
+            call("v2c_upload_node_field", m.h, f, a.ctypes.data_as(dp))
+        m.nodes2markers_move()
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    m.synchronize()
+    s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s2.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e2.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = s2.elapsed_time(e2) / args.steps
+    if dist:
+        t = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+
+    if rank != 0:
+        m.close()
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # roofline of the dominant kernel
+    peaks = measured_peaks()
+    mpn = n / nn
+    dom = max(("m2n", "n2m_move"), key=lambda k: stage_ms.get(k, 0.0))
+    alg = n * (ALG_BYTES[dom] + NODE_FIELDS[dom] * 4 / mpn)
+    achieved = alg / (stage_ms[dom] * 1e-3) / 1e9
+    tr = ncu_traffic(dom)
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+            "traffic": (tr * n) if tr is not None else None,
+            "peak_source": peaks["source"],
+            "alg_bytes_per_marker": ALG_BYTES[dom] + NODE_FIELDS[dom] * 4 / mpn}
+    step_alg = STEP_MARKER_BYTES + STEP_NODE_FIELDS * 4 / mpn
+    base = cpu_baseline() if not args.no_cpu_baseline else None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 fields, f64 node normalisation", "data": "synthetic",
+        "config": {"workload": f"{args.config}: {case.params['xnumx']}x{case.params['ynumy']} grid, "
+                               f"{n} markers ({mpn:.1f}/node), dt={dt:g}s, RK4, interpolationmod=2, "
+                               "antidiffinter=1",
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas only"},
+        "stage_ms": stage_ms,
+        "step_alg_bytes_per_marker": step_alg,
+        "step_roofline_frac": (value / world) * step_alg / (peaks["hbm_gbs"] * 1e9),
+        "roofline": roof,
+        "cpu_baseline": ({k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
+                         if base else None),
+        "e2e": {"value": world * n / (ms_e2e * 1e-3), "unit": UNIT,
+                "h2d_bytes_per_step": 8 * nn * len(E2E_UP),
+                "d2h_bytes_per_step": 8 * nn * len(E2E_DOWN)},
+        "gpu_launches": int(st1["kernel_launches"] - st0["kernel_launches"]),
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    m.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c4")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference_arm(args, rank)
+    else:
+        run_gpu(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

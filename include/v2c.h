@@ -171,6 +171,7 @@ typedef struct v2c_status {
   long newton_nonconv;      /* markers that did not reach the tolerance       */
   double newton_max_res;    /* largest relative residual after the last solve */
   long max_cell_count;      /* most markers in one cell after the last sort   */
+  long kernel_launches;     /* device kernels launched by this context        */
   int last_error;           /* last non-zero status returned                   */
 } v2c_status;
 
@@ -230,6 +231,24 @@ int v2c_nodes2markers_move(v2c_ctx *ctx);
 
 int v2c_synchronize(v2c_ctx *ctx);
 int v2c_get_status(v2c_ctx *ctx, v2c_status *st);
+
+/* Per-kernel timing (instrumentation, no counterpart in the reference): when
+ * enabled, every launch group below is bracketed by CUDA events on the
+ * context stream; v2c_get_profile synchronises and returns the summed
+ * milliseconds and the number of timed launches of one group. */
+enum {
+  V2C_PROF_M2N = 0,     /* marker2nodes sweep                          */
+  V2C_PROF_M2N_TAIL,    /* sticky flags, state ghosts, boundary rows   */
+  V2C_PROF_C2B,         /* interpolate_center2basic_old                */
+  V2C_PROF_BEFORE,      /* compute_before_solve                        */
+  V2C_PROF_AFTER,       /* compute_after_solve                         */
+  V2C_PROF_N2M_MOVE,    /* nodes2markers + move sweep                  */
+  V2C_PROF_SORT,        /* counting sort by cell                       */
+  V2C_PROF_NEWTON,      /* per-marker Newton (with the network guess)  */
+  V2C_PROF_N
+};
+int v2c_set_profiling(v2c_ctx *ctx, int on);
+int v2c_get_profile(v2c_ctx *ctx, int group, double *ms, long *launches);
 
 /* ================================================ per-marker VEP+RSF Newton
  * No counterpart in the reference (it resolves stress and slip rate only

@@ -1,0 +1,129 @@
+"""Parity of the CUDA MIC step with the oracle restatement (GPU).
+
+Same seeded state on both sides; the GPU stores marker fields in FP32 and
+positions as cell + FP32 offset, the oracle runs FP64 on the original
+inputs.  Tolerances (relative to each field's magnitude):
+  * cell indices: bit-exact against nxsearch/nysearch on the FP64 positions;
+  * node fields: 1e-6, viscosity-derived fields 1e-5 (see parity.VISCOUS);
+  * marker fields: 1e-6; positions after the move: 3e-7 cell widths
+    (the FP32 offset resolves 2^-24 = 6e-8 of a cell).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from velo2cycles_gb300 import abi, mic, synth
+
+from .parity import (C2B_OUT, M2N_OUT, MOVE_MARK, N2M_MARK, N2M_OUT, RSF_OUT, VISCOUS,
+                     node_errors, marker_errors, nxsearch_np)
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+TOL_VISC = 1e-5
+
+
+def _tol(name):
+    f = {v: k for k, v in abi.node_field_names().items()}.get(name)
+    return TOL_VISC if f in VISCOUS else TOL
+
+
+def _check_nodes(errs):
+    bad = {k: v for k, v in errs.items() if not v <= _tol(k)}
+    assert not bad, f"node fields over tolerance: {bad}"
+
+
+@pytest.fixture(scope="module", params=["tiny", "small"])
+def case(request, built_lib, oracle_built):
+    return synth.make_case(request.param, seed=7)
+
+
+def test_cell_assignment_bit_exact(case):
+    m = mic.from_case(case)
+    cells = m.download_cells()
+    ix = nxsearch_np(case.gx, case.marks[abi.MF_X])
+    iy = nxsearch_np(case.gy, case.marks[abi.MF_Y])
+    assert np.array_equal(cells, (ix * (case.gy.size - 1) + iy).astype(np.int32))
+    m.close()
+
+
+def test_marker2nodes(case):
+    m = mic.from_case(case)
+    m.marker2nodes()
+    got = m.download_nodes(M2N_OUT)
+    ref = oracle.Restatement(case.copy())
+    ref.marker2nodes()
+    _check_nodes(node_errors(got, ref.nodes, M2N_OUT))
+    st = m.status()
+    assert st["n_nan"] == 0
+    m.close()
+
+
+def test_center2basic_and_node_rsf(case):
+    m = mic.from_case(case)
+    ref = oracle.Restatement(case.copy())
+    m.marker2nodes(); ref.marker2nodes()
+    m.interpolate_center2basic_old(); ref.center2basic_old()
+    dt = case.params["timestep"]
+    m.compute_before_solve(dt, 0); ref.compute_before_solve(dt, 0)
+    d_gpu = m.compute_after_solve(dt, 0)
+    d_ref = ref.compute_after_solve(dt, 0)
+    got = m.download_nodes(C2B_OUT + RSF_OUT)
+    _check_nodes(node_errors(got, ref.nodes, C2B_OUT + RSF_OUT))
+    assert abs(d_gpu - d_ref) <= 1e-5 * max(abs(d_ref), 1.0)
+    m.close()
+
+
+def test_nodes2markers(case):
+    m = mic.from_case(case)
+    ref = oracle.Restatement(case.copy())
+    m.nodes2markers()
+    ref.nodes2markers()
+    got = m.download_nodes(N2M_OUT)
+    _check_nodes(node_errors(got, ref.nodes, N2M_OUT))
+    mk = m.download_markers(N2M_MARK)
+    errs = marker_errors(mk, ref.marks, N2M_MARK)
+    bad = {k: v for k, v in errs.items() if not v <= TOL}
+    assert not bad, f"marker fields over tolerance: {bad}"
+    m.close()
+
+
+@pytest.mark.parametrize("markmod", [1, 2])
+def test_move(case, markmod):
+    c = case.copy()
+    c.params["markmod"] = markmod
+    m = mic.from_case(c)
+    ref = oracle.Restatement(c.copy())
+    m.moveandrotatemarkers()
+    ref.move()
+    mk = m.download_markers(MOVE_MARK)
+    # a few units of the FP32 offset resolution, 2^-24 cell widths
+    wx = np.diff(c.gx)[nxsearch_np(c.gx, ref.marks[abi.MF_X])]
+    wy = np.diff(c.gy)[nxsearch_np(c.gy, ref.marks[abi.MF_Y])]
+    ex = np.abs(mk[abi.MF_X] - ref.marks[abi.MF_X]) / wx
+    ey = np.abs(mk[abi.MF_Y] - ref.marks[abi.MF_Y]) / wy
+    assert ex.max() <= 3e-7 and ey.max() <= 3e-7, (ex.max(), ey.max())
+    errs = marker_errors(mk, ref.marks, [abi.MF_XX, abi.MF_XY, abi.MF_K, abi.MF_E])
+    bad = {k: v for k, v in errs.items() if not v <= TOL}
+    assert not bad, bad
+    # the cell of every moved marker is nxsearch of its FP64 position
+    cells = m.download_cells()
+    ix = nxsearch_np(c.gx, mk[abi.MF_X])
+    iy = nxsearch_np(c.gy, mk[abi.MF_Y])
+    assert np.array_equal(cells, (ix * (c.gy.size - 1) + iy).astype(np.int32))
+    m.close()
+
+
+def test_full_step_deterministic(case):
+    outs = []
+    for _ in range(2):
+        m = mic.from_case(case)
+        m.step()
+        m.step()
+        outs.append((m.download_nodes([abi.NF_NU_M2C, abi.NF_PHIE, abi.NF_MVX]),
+                     m.download_markers([abi.MF_X, abi.MF_XX])))
+        m.close()
+    for f in outs[0][0]:
+        assert np.array_equal(outs[0][0][f], outs[1][0][f])
+    for f in (abi.MF_X, abi.MF_XX):
+        assert np.array_equal(outs[0][1][f], outs[1][1][f])

@@ -78,7 +78,8 @@ class Status(ctypes.Structure):
         ("n_far_moves", ctypes.c_long), ("n_nan", ctypes.c_long),
         ("newton_iters", ctypes.c_long), ("newton_fallbacks", ctypes.c_long),
         ("newton_nonconv", ctypes.c_long), ("newton_max_res", ctypes.c_double),
-        ("max_cell_count", ctypes.c_long), ("last_error", ctypes.c_int),
+        ("max_cell_count", ctypes.c_long), ("kernel_launches", ctypes.c_long),
+        ("last_error", ctypes.c_int),
     ]
 
 

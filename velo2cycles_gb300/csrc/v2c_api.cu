@@ -1,0 +1,829 @@
+// v2c_api.cu -- the C ABI (include/v2c.h): context life cycle, transfers,
+// and the step entry points that replace the reference's global-array
+// routines.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <vector>
+
+#include "v2c_kernels.h"
+#include "v2c_newton.h"
+
+using namespace v2c;
+
+#define CK(call)                                                   \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) {                                       \
+      ctx->last_error = V2C_ERR_CUDA;                              \
+      ctx->cuda_msg = cudaGetErrorString(e_);                      \
+      return V2C_ERR_CUDA;                                         \
+    }                                                              \
+  } while (0)
+
+struct v2c_ctx {
+  v2c_params p;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  long cap = 0, n = 0;
+  int xn = 0, yn = 0, ncx = 0, ncy = 0;
+  long nn = 0, ncell = 0;
+  // grid
+  double *d_gx = nullptr, *d_gy = nullptr;
+  float *d_wx = nullptr, *d_wy = nullptr, *d_gxf = nullptr, *d_gyf = nullptr;
+  std::vector<double> h_gx, h_gy;
+  bool have_grid = false, have_rock = false;
+  // rock table
+  float *d_rock = nullptr;
+  std::vector<double> h_rt;
+  // nodes
+  float *d_node = nullptr;
+  double *d_node64 = nullptr;  // boundary staging, one FP64 node field
+  uint32_t *d_sticky = nullptr;
+  // markers
+  Markers m{};
+  void *marker_mem[32] = {};
+  int n_marker_mem = 0;
+  bool have_markers = false;
+  // sort
+  SortBufs sb{};
+  bool sorted = false;
+  // staging
+  double *d_stage64 = nullptr, *d_stage64b = nullptr;
+  // bonds
+  std::vector<long> h_bondm, h_bondn;
+  std::vector<double> h_bondv;
+  long bondnum = 0;
+  bool have_bonds = false;
+  int bc_built_compressible = -1, bc_built_tempmod = -1;
+  int bc_n = 0;
+  void *bc_mem = nullptr;
+  BcRows bc{};
+  float *d_bc_scratch = nullptr;
+  // status
+  unsigned long long *d_stat = nullptr;
+  double *d_red = nullptr;
+  long red_cap = 0;
+  int last_error = 0;
+  long launches = 0;  // device kernels launched (instrumentation)
+  const char *cuda_msg = "";
+  // per-marker Newton / network
+  NewtonState nw{};
+  // instrumentation: event pairs per launch group, resolved on demand
+  bool prof = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[V2C_PROF_N];
+  double prof_ms[V2C_PROF_N] = {};
+  long prof_n[V2C_PROF_N] = {};
+  std::vector<cudaEvent_t> ev_pool;
+};
+
+namespace {
+cudaEvent_t ev_get(v2c_ctx *c) {
+  if (!c->ev_pool.empty()) {
+    cudaEvent_t e = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+// RAII bracket of one launch group
+struct Prof {
+  v2c_ctx *c;
+  int g;
+  cudaEvent_t a = nullptr;
+  Prof(v2c_ctx *ctx, int group) : c(ctx), g(group) {
+    if (c->prof) {
+      a = ev_get(c);
+      cudaEventRecord(a, c->stream);
+    }
+  }
+  ~Prof() {
+    if (c->prof) {
+      cudaEvent_t b = ev_get(c);
+      cudaEventRecord(b, c->stream);
+      c->prof_ev[g].push_back({a, b});
+    }
+  }
+};
+void prof_resolve(v2c_ctx *c) {
+  cudaStreamSynchronize(c->stream);
+  for (int g = 0; g < V2C_PROF_N; g++) {
+    for (auto &pr : c->prof_ev[g]) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, pr.first, pr.second);
+      c->prof_ms[g] += ms;
+      c->prof_n[g] += 1;
+      c->ev_pool.push_back(pr.first);
+      c->ev_pool.push_back(pr.second);
+    }
+    c->prof_ev[g].clear();
+  }
+}
+}  // namespace
+
+namespace {
+
+template <class T>
+cudaError_t dalloc(T **p, size_t count) {
+  return cudaMalloc((void **)p, sizeof(T) * (count ? count : 1));
+}
+
+Grid make_grid(const v2c_ctx *c) {
+  Grid g;
+  g.gx = c->d_gx; g.gy = c->d_gy; g.wx = c->d_wx; g.wy = c->d_wy;
+  g.xn = c->xn; g.yn = c->yn; g.ncx = c->ncx; g.ncy = c->ncy; g.nn = c->nn;
+  g.xsize = c->p.xsize; g.ysize = c->p.ysize;
+  return g;
+}
+
+Scal make_scal(const v2c_params &p, const std::vector<double> &rt) {
+  Scal s;
+  s.p = p;
+  s.antid = (p.timesum > 0 && p.antidiffinter == 1);
+  s.phi_reset0 = (p.timesum == p.timestep);
+  s.sticky_cap = (p.stickymod == 1 && p.timesum > 4e7);
+  s.dt = (float)p.timestep;
+  double gg2 = rt.empty() ? 0.0 : rt[V2C_RT_GG * V2C_MAXTMR + 2];
+  s.sticky_nu = (float)(gg2 * p.timestep / 100);
+  s.ln_nubeg = (float)log(p.nubeg);
+  s.ln_nuend = (float)log(p.nuend);
+  return s;
+}
+
+Nodes make_nodes(const v2c_ctx *c) { return Nodes{c->d_node, c->nn}; }
+
+int fail(v2c_ctx *ctx, int code) {
+  if (ctx) ctx->last_error = code;
+  return code;
+}
+
+int check_params(const v2c_params *p) {
+  if (p->xnumx < 4 || p->ynumy < 4) return V2C_ERR_ARG;
+  if (p->interpolationmod != 2) return V2C_ERR_UNSUPPORTED;
+  if (p->rkmod == 3) return V2C_ERR_UNSUPPORTED;
+  if (p->xnumx * p->ynumy > (long)INT32_MAX / 4) return V2C_ERR_CAPACITY;
+  return V2C_OK;
+}
+
+int pick_tx(const v2c_ctx *c) {
+  // enough CTAs for two waves over 152 SMs; halo overhead is one column
+  long rows = (c->yn + 31) / 32;
+  int tx = 32;
+  while (tx > 4 && rows * ((c->xn + tx - 1) / tx) < 2 * 152) tx /= 2;
+  return tx;
+}
+
+}  // namespace
+
+// ================================================================ life cycle
+extern "C" int v2c_create(const v2c_params *p, long max_markers, void *cuda_stream,
+                          v2c_ctx **out) {
+  if (!p || !out || max_markers < 0) return V2C_ERR_ARG;
+  int rc = check_params(p);
+  if (rc) return rc;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return V2C_ERR_CUDA;
+  v2c_ctx *ctx = new v2c_ctx();
+  ctx->p = *p;
+  ctx->cap = max_markers;
+  ctx->xn = (int)p->xnumx; ctx->yn = (int)p->ynumy;
+  ctx->ncx = ctx->xn - 1; ctx->ncy = ctx->yn - 1;
+  ctx->nn = (long)ctx->xn * ctx->yn;
+  ctx->ncell = (long)ctx->ncx * ctx->ncy;
+  if (cuda_stream) {
+    ctx->stream = (cudaStream_t)cuda_stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete ctx;
+      return V2C_ERR_CUDA;
+    }
+    ctx->own_stream = true;
+  }
+#define AL(ptr, cnt)                                                      \
+  if (dalloc(&(ptr), (cnt)) != cudaSuccess) { v2c_destroy(ctx); return V2C_ERR_CUDA; }
+  AL(ctx->d_gx, ctx->xn); AL(ctx->d_gy, ctx->yn);
+  AL(ctx->d_wx, ctx->ncx); AL(ctx->d_wy, ctx->ncy);
+  AL(ctx->d_gxf, ctx->xn); AL(ctx->d_gyf, ctx->yn);
+  AL(ctx->d_rock, (size_t)RK_N * V2C_MAXTMR);
+  AL(ctx->d_node, (size_t)V2C_NF_N * ctx->nn);
+  AL(ctx->d_node64, ctx->nn);
+  AL(ctx->d_sticky, ctx->nn);
+  AL(ctx->d_stat, ST_N);
+  ctx->red_cap = 2 + 2 * ((ctx->nn + 255) / 256);
+  AL(ctx->d_red, ctx->red_cap);
+  cudaMemsetAsync(ctx->d_node, 0, sizeof(float) * V2C_NF_N * ctx->nn, ctx->stream);
+  cudaMemsetAsync(ctx->d_stat, 0, sizeof(unsigned long long) * ST_N, ctx->stream);
+  // markers
+  long cap = max_markers;
+  Markers &m = ctx->m;
+  void **mm = ctx->marker_mem;
+  int k = 0;
+#define AM(field, T)                                                     \
+  if (dalloc(&(m.field), cap) != cudaSuccess) { v2c_destroy(ctx); return V2C_ERR_CUDA; } \
+  mm[k++] = (void *)m.field; ctx->n_marker_mem = k;
+  AM(cell_in, int32_t) AM(cell_out, int32_t) AM(u_in, float) AM(u_out, float)
+  AM(v_in, float) AM(v_out, float) AM(id, int32_t) AM(type, int8_t) AM(flags, uint8_t)
+  AM(tk, float) AM(e, float) AM(p, float) AM(sxx, float) AM(sxy, float) AM(exx, float)
+  AM(exy, float) AM(vx, float) AM(vy, float) AM(phi, float) AM(coh, float) AM(slipv, float)
+  AM(mnu, float)
+#undef AM
+  ctx->n_marker_mem = k;
+  // sort
+  AL(ctx->sb.counts, ctx->ncell); AL(ctx->sb.start, ctx->ncell + 1);
+  AL(ctx->sb.slot, cap); AL(ctx->sb.tmp, cap); AL(ctx->sb.perm, cap);
+  ctx->sb.blocksum_cap = (ctx->ncell + 4095) / 4096 + 1;
+  AL(ctx->sb.blocksum, ctx->sb.blocksum_cap);
+  AL(ctx->d_stage64, cap); AL(ctx->d_stage64b, cap);
+#undef AL
+  if (newton_init(ctx->nw, cap) != cudaSuccess) { v2c_destroy(ctx); return V2C_ERR_CUDA; }
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) { v2c_destroy(ctx); return V2C_ERR_CUDA; }
+  *out = ctx;
+  return V2C_OK;
+}
+
+extern "C" int v2c_destroy(v2c_ctx *ctx) {
+  if (!ctx) return V2C_ERR_ARG;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  void *ptrs[] = {ctx->d_gx, ctx->d_gy, ctx->d_wx, ctx->d_wy, ctx->d_gxf, ctx->d_gyf,
+                  ctx->d_rock, ctx->d_node, ctx->d_node64, ctx->d_sticky, ctx->d_stat, ctx->d_red,
+                  ctx->sb.counts, ctx->sb.start, ctx->sb.slot, ctx->sb.tmp, ctx->sb.perm,
+                  ctx->sb.blocksum, ctx->d_stage64, ctx->d_stage64b, ctx->bc_mem,
+                  ctx->d_bc_scratch};
+  for (void *q : ptrs)
+    if (q) cudaFree(q);
+  for (int i = 0; i < ctx->n_marker_mem; i++)
+    if (ctx->marker_mem[i]) cudaFree(ctx->marker_mem[i]);
+  newton_free(ctx->nw);
+  prof_resolve(ctx);
+  for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return V2C_OK;
+}
+
+extern "C" int v2c_set_params(v2c_ctx *ctx, const v2c_params *p) {
+  if (!ctx || !p) return V2C_ERR_ARG;
+  if (p->xnumx != ctx->p.xnumx || p->ynumy != ctx->p.ynumy) return fail(ctx, V2C_ERR_ARG);
+  int rc = check_params(p);
+  if (rc) return fail(ctx, rc);
+  ctx->p = *p;
+  return V2C_OK;
+}
+
+extern "C" int v2c_set_grid(v2c_ctx *ctx, const double *gx, const double *gy) {
+  if (!ctx || !gx || !gy) return V2C_ERR_ARG;
+  for (int i = 0; i + 1 < ctx->xn; i++)
+    if (!(gx[i + 1] > gx[i])) return fail(ctx, V2C_ERR_ARG);
+  for (int i = 0; i + 1 < ctx->yn; i++)
+    if (!(gy[i + 1] > gy[i])) return fail(ctx, V2C_ERR_ARG);
+  if (gx[ctx->xn - 1] != ctx->p.xsize || gy[ctx->yn - 1] != ctx->p.ysize)
+    return fail(ctx, V2C_ERR_ARG);
+  ctx->h_gx.assign(gx, gx + ctx->xn);
+  ctx->h_gy.assign(gy, gy + ctx->yn);
+  std::vector<float> wx(ctx->ncx), wy(ctx->ncy), gxf(ctx->xn), gyf(ctx->yn);
+  for (int i = 0; i < ctx->ncx; i++) wx[i] = (float)(gx[i + 1] - gx[i]);
+  for (int i = 0; i < ctx->ncy; i++) wy[i] = (float)(gy[i + 1] - gy[i]);
+  for (int i = 0; i < ctx->xn; i++) gxf[i] = (float)gx[i];
+  for (int i = 0; i < ctx->yn; i++) gyf[i] = (float)gy[i];
+  CK(cudaMemcpy(ctx->d_gx, gx, sizeof(double) * ctx->xn, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_gy, gy, sizeof(double) * ctx->yn, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_wx, wx.data(), sizeof(float) * ctx->ncx, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_wy, wy.data(), sizeof(float) * ctx->ncy, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_gxf, gxf.data(), sizeof(float) * ctx->xn, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_gyf, gyf.data(), sizeof(float) * ctx->yn, cudaMemcpyHostToDevice));
+  ctx->have_grid = true;
+  return V2C_OK;
+}
+
+extern "C" int v2c_set_rock_table(v2c_ctx *ctx, const double *rt) {
+  if (!ctx || !rt) return V2C_ERR_ARG;
+  ctx->h_rt.assign(rt, rt + V2C_RT_N * V2C_MAXTMR);
+  std::vector<float> f((size_t)RK_N * V2C_MAXTMR, 0.f);
+  auto R = [&](int r, int t) { return rt[r * V2C_MAXTMR + t]; };
+  auto F = [&](int k, int t) -> float & { return f[(size_t)k * V2C_MAXTMR + t]; };
+  for (int t = 0; t < V2C_MAXTMR; t++) {
+    double nu = R(V2C_RT_NU, t), dh = R(V2C_RT_DH, t), dv = R(V2C_RT_DV, t);
+    double ss = R(V2C_RT_SS, t), mm = R(V2C_RT_MM, t), gg = R(V2C_RT_GG, t);
+    F(RK_GG, t) = (float)gg;
+    F(RK_INV_GG, t) = gg != 0 ? (float)(1.0 / gg) : 0.f;
+    F(RK_NU, t) = (float)nu;
+    F(RK_LNNU, t) = nu > 0 ? (float)log(nu) : 0.f;
+    F(RK_DH, t) = (float)dh; F(RK_DV, t) = (float)dv;
+    F(RK_LNSS, t) = ss > 0 ? (float)log(ss) : 0.f;
+    F(RK_MM, t) = (float)mm;
+    F(RK_RO, t) = (float)R(V2C_RT_RO, t); F(RK_BB, t) = (float)R(V2C_RT_BB, t);
+    F(RK_AA, t) = (float)R(V2C_RT_AA, t); F(RK_CP, t) = (float)R(V2C_RT_CP, t);
+    F(RK_KT, t) = (float)R(V2C_RT_KT, t); F(RK_HT, t) = (float)R(V2C_RT_HT, t);
+    F(RK_KF, t) = (float)R(V2C_RT_KF, t); F(RK_KP, t) = (float)R(V2C_RT_KP, t);
+    F(RK_N0, t) = (float)R(V2C_RT_N0, t); F(RK_N1, t) = (float)R(V2C_RT_N1, t);
+    F(RK_IM, t) = (float)R(V2C_RT_IM, t);
+    int kind;
+    // branch selection of ductilevisc (density_ductilevisc_calc.c:44-66)
+    if (t == 1) kind = VISC_STICKY;
+    else if (dh == 0 && dv == 0 && (ss == 0 || mm == 1.0)) kind = VISC_NEWTON;
+    else if (nu > 0 && (dh != 0 || dv != 0) && ss != 0 && mm != 1.0) kind = VISC_POWER;
+    else kind = VISC_UNDEF;
+    F(RK_KIND, t) = (float)kind;
+  }
+  CK(cudaMemcpy(ctx->d_rock, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
+  ctx->have_rock = true;
+  return V2C_OK;
+}
+
+extern "C" int v2c_set_bonds(v2c_ctx *ctx, const long *bondm, const long *bondn,
+                             const double *bondv, long bondnum) {
+  if (!ctx || !bondm || bondnum < 0 || (bondnum > 0 && (!bondn || !bondv))) return V2C_ERR_ARG;
+  ctx->h_bondm.assign(bondm, bondm + ctx->nn * 4);
+  ctx->h_bondn.assign(bondn, bondn + bondnum * 3);
+  ctx->h_bondv.assign(bondv, bondv + bondnum * 4);
+  ctx->bondnum = bondnum;
+  for (long i = 0; i < ctx->nn * 4; i++)
+    if (bondm[i] < 0 || bondm[i] >= bondnum) return fail(ctx, V2C_ERR_ARG);
+  ctx->have_bonds = true;
+  ctx->bc_built_compressible = -1;
+  return V2C_OK;
+}
+
+// ------------------------------------------------ boundary rows (host side)
+namespace {
+
+struct Resolved {
+  double c;
+  std::vector<std::pair<long, double>> terms;  // (row, coef), identity rows
+};
+
+struct BcBlock {
+  int field;
+  std::vector<char> present;
+  std::vector<long> bond;
+  int kind;  // 0 vx, 1 vy, 2 P, 3 T
+};
+
+long decode(int kind, long bn, long nn) {
+  switch (kind) {
+    case 0: return ((bn - 1) - 1) / 3;
+    case 1: return ((bn - 1) - 2) / 3;
+    case 2: return (bn - 1) / 3;
+    default: return bn - 1 - nn * 3;
+  }
+}
+
+// resolve a boundary row into constant + identity-row terms, references in
+// increasing row order as the frontal elimination folds them in
+bool resolve(const v2c_ctx *ctx, const BcBlock &B, long r, std::map<long, Resolved> &memo,
+             std::vector<char> &busy, Resolved &out) {
+  auto it = memo.find(r);
+  if (it != memo.end()) { out = it->second; return true; }
+  if (busy[r]) return false;
+  busy[r] = 1;
+  long b = B.bond[r];
+  Resolved res;
+  res.c = ctx->h_bondv[b * 4 + 0];
+  std::vector<std::pair<long, double>> refs;
+  for (int k = 0; k < 3; k++) {
+    long bn = ctx->h_bondn[b * 3 + k];
+    if (bn) refs.push_back({decode(B.kind, bn, ctx->nn), ctx->h_bondv[b * 4 + k + 1]});
+  }
+  std::sort(refs.begin(), refs.end(),
+            [](const std::pair<long, double> &a, const std::pair<long, double> &b2) { return a.first < b2.first; });
+  for (auto &rf : refs) {
+    long q = rf.first;
+    if (q < 0 || q >= ctx->nn || !B.present[q]) continue;  // absent rows solve to 0
+    if (!B.bond[q]) {
+      res.terms.push_back({q, rf.second});
+    } else {
+      Resolved sub;
+      if (!resolve(ctx, B, q, memo, busy, sub)) return false;
+      res.c = res.c - sub.c * (-rf.second);
+      for (auto &t : sub.terms) res.terms.push_back({t.first, t.second * rf.second});
+    }
+  }
+  busy[r] = 0;
+  memo[r] = res;
+  out = res;
+  return true;
+}
+
+int build_bc(v2c_ctx *ctx) {
+  const int cm = ctx->p.compressiblemode == 1, tm = ctx->p.tempmod != 0;
+  if (ctx->bc_built_compressible == cm && ctx->bc_built_tempmod == tm) return V2C_OK;
+  std::vector<int> fld, nref, rfield;
+  std::vector<long> node, rnode;
+  std::vector<float> cst, rcoef;
+  const long nn = ctx->nn;
+  const int xn = ctx->xn, yn = ctx->yn;
+  for (int kind = 0; kind < 4; kind++) {
+    if (kind == 3 && !tm) continue;
+    BcBlock B;
+    B.kind = kind;
+    B.field = kind == 0 ? V2C_NF_MVX : kind == 1 ? V2C_NF_MVY : kind == 2 ? V2C_NF_SPPE : V2C_NF_TK;
+    B.present.assign(nn, 0);
+    B.bond.assign(nn, 0);
+    for (int m1 = 0; m1 < xn; m1++)
+      for (int m2 = 0; m2 < yn; m2++) {
+        long m3 = (long)m1 * yn + m2;
+        if (kind == 0 && m2 < yn - 1) { B.present[m3] = 1; B.bond[m3] = ctx->h_bondm[m3 * 3 + 1]; }
+        if (kind == 1 && m1 < xn - 1) { B.present[m3] = 1; B.bond[m3] = ctx->h_bondm[m3 * 3 + 2]; }
+        if (kind == 2 && m1 && m2) { B.present[m3] = 1; B.bond[m3] = cm ? 0 : ctx->h_bondm[m3 * 3]; }
+        if (kind == 3) { B.present[m3] = 1; B.bond[m3] = ctx->h_bondm[3 * nn + m3]; }
+      }
+    std::map<long, Resolved> memo;
+    std::vector<char> busy(nn, 0);
+    for (long r = 0; r < nn; r++) {
+      if (!B.present[r] || !B.bond[r]) continue;
+      Resolved res;
+      if (!resolve(ctx, B, r, memo, busy, res)) return V2C_ERR_UNSUPPORTED;
+      if ((int)res.terms.size() > V2C_BC_MAXREF) return V2C_ERR_UNSUPPORTED;
+      fld.push_back(B.field);
+      node.push_back(r);
+      cst.push_back((float)res.c);
+      nref.push_back((int)res.terms.size());
+      for (int k = 0; k < V2C_BC_MAXREF; k++) {
+        bool h = k < (int)res.terms.size();
+        rfield.push_back(B.field);
+        rnode.push_back(h ? res.terms[k].first : 0);
+        rcoef.push_back(h ? (float)res.terms[k].second : 0.f);
+      }
+    }
+  }
+  int n = (int)fld.size();
+  if (ctx->bc_mem) { cudaFree(ctx->bc_mem); ctx->bc_mem = nullptr; }
+  if (ctx->d_bc_scratch) { cudaFree(ctx->d_bc_scratch); ctx->d_bc_scratch = nullptr; }
+  ctx->bc_n = n;
+  ctx->bc = BcRows{};
+  ctx->bc.n = n;
+  if (n == 0) { ctx->bc_built_compressible = cm; ctx->bc_built_tempmod = tm; return V2C_OK; }
+  size_t M = V2C_BC_MAXREF;
+  size_t bytes = n * (sizeof(int) + sizeof(long) + sizeof(float) + sizeof(int)) +
+                 n * M * (sizeof(int) + sizeof(long) + sizeof(float)) + 64;
+  char *mem;
+  if (cudaMalloc((void **)&mem, bytes) != cudaSuccess) return V2C_ERR_CUDA;
+  if (cudaMalloc((void **)&ctx->d_bc_scratch, sizeof(float) * n) != cudaSuccess) return V2C_ERR_CUDA;
+  ctx->bc_mem = mem;
+  size_t off = 0;
+  auto put = [&](const void *src, size_t sz) {
+    off = (off + 7) & ~size_t(7);
+    void *dst = mem + off;
+    cudaMemcpy(dst, src, sz, cudaMemcpyHostToDevice);
+    off += sz;
+    return dst;
+  };
+  ctx->bc.field = (const int *)put(fld.data(), n * sizeof(int));
+  ctx->bc.node = (const long *)put(node.data(), n * sizeof(long));
+  ctx->bc.c = (const float *)put(cst.data(), n * sizeof(float));
+  ctx->bc.nref = (const int *)put(nref.data(), n * sizeof(int));
+  ctx->bc.rfield = (const int *)put(rfield.data(), n * M * sizeof(int));
+  ctx->bc.rnode = (const long *)put(rnode.data(), n * M * sizeof(long));
+  ctx->bc.rcoef = (const float *)put(rcoef.data(), n * M * sizeof(float));
+  ctx->bc_built_compressible = cm;
+  ctx->bc_built_tempmod = tm;
+  return V2C_OK;
+}
+
+}  // namespace
+
+// ============================================================ marker arrays
+extern "C" int v2c_upload_markers(v2c_ctx *ctx, const double *const *fields,
+                                  const signed char *markt, long n) {
+  if (!ctx || !fields || !markt || n < 0) return V2C_ERR_ARG;
+  if (!fields[V2C_MF_X] || !fields[V2C_MF_Y]) return fail(ctx, V2C_ERR_ARG);
+  if (n > ctx->cap) return fail(ctx, V2C_ERR_CAPACITY);
+  if (!ctx->have_grid) return fail(ctx, V2C_ERR_STATE);
+  for (long i = 0; i < n; i++)
+    if (markt[i] < 0 || markt[i] >= 100) return fail(ctx, V2C_ERR_UNSUPPORTED);
+  cudaStream_t st = ctx->stream;
+  Markers &m = ctx->m;
+  Grid g = make_grid(ctx);
+  ctx->n = n;
+  CK(cudaMemcpyAsync(ctx->d_stage64, fields[V2C_MF_X], sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_stage64b, fields[V2C_MF_Y], sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  launch_assign(g, ctx->d_stage64, ctx->d_stage64b, n, m, ctx->d_stat, st);
+  CK(cudaMemcpyAsync(m.type, markt, n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(m.flags, 0, n, st));
+  struct F { int id; float *dst; } ff[] = {
+      {V2C_MF_K, m.tk}, {V2C_MF_E, m.e}, {V2C_MF_P, m.p}, {V2C_MF_XX, m.sxx},
+      {V2C_MF_XY, m.sxy}, {V2C_MF_EXX, m.exx}, {V2C_MF_EXY, m.exy}, {V2C_MF_VX, m.vx},
+      {V2C_MF_VY, m.vy}, {V2C_MF_PHI, m.phi}, {V2C_MF_C, m.coh}, {V2C_MF_SLIPV, m.slipv}};
+  for (auto &f : ff) {
+    if (fields[f.id]) {
+      CK(cudaMemcpyAsync(ctx->d_stage64, fields[f.id], sizeof(double) * n, cudaMemcpyHostToDevice, st));
+      launch_f64_to_f32(ctx->d_stage64, f.dst, n, st);
+    } else {
+      CK(cudaMemsetAsync(f.dst, 0, sizeof(float) * n, st));
+    }
+  }
+  CK(cudaMemsetAsync(m.mnu, 0, sizeof(float) * n, st));
+  // sort once and store the markers physically in cell order
+  launch_sort(m.cell_in, n, ctx->ncell, ctx->sb, ctx->d_stat, st);
+  const int32_t *perm = ctx->sb.perm;
+  float *tmpf = (float *)ctx->d_stage64;
+  int32_t *tmpi = (int32_t *)ctx->d_stage64;
+  float *fl[] = {m.u_in, m.v_in, m.tk, m.e, m.p, m.sxx, m.sxy, m.exx, m.exy, m.vx,
+                 m.vy, m.phi, m.coh, m.slipv};
+  for (float *f : fl) {
+    launch_gather_f32(f, perm, tmpf, n, st);
+    CK(cudaMemcpyAsync(f, tmpf, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+  }
+  int32_t *il[] = {m.cell_in, m.id};
+  for (int32_t *f : il) {
+    launch_gather_i32(f, perm, tmpi, n, st);
+    CK(cudaMemcpyAsync(f, tmpi, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, st));
+  }
+  launch_gather_i8(m.type, perm, (int8_t *)tmpi, n, st);
+  CK(cudaMemcpyAsync(m.type, tmpi, n, cudaMemcpyDeviceToDevice, st));
+  // the physical order is now sorted: sort again to get the identity perm
+  launch_sort(m.cell_in, n, ctx->ncell, ctx->sb, ctx->d_stat, st);
+  CK(cudaStreamSynchronize(st));
+  CK(cudaGetLastError());
+  ctx->have_markers = true;
+  ctx->sorted = true;
+  return V2C_OK;
+}
+
+extern "C" int v2c_download_markers(v2c_ctx *ctx, double *const *fields, signed char *markt,
+                                    long n) {
+  if (!ctx || !fields || n != ctx->n) return V2C_ERR_ARG;
+  if (!ctx->have_markers) return fail(ctx, V2C_ERR_STATE);
+  cudaStream_t st = ctx->stream;
+  Markers &m = ctx->m;
+  Grid g = make_grid(ctx);
+  if (fields[V2C_MF_X] || fields[V2C_MF_Y]) {
+    launch_positions(g, m, n, ctx->d_stage64, ctx->d_stage64b, st);
+    if (fields[V2C_MF_X])
+      CK(cudaMemcpyAsync(fields[V2C_MF_X], ctx->d_stage64, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    if (fields[V2C_MF_Y])
+      CK(cudaMemcpyAsync(fields[V2C_MF_Y], ctx->d_stage64b, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  struct F { int id; const float *src; } ff[] = {
+      {V2C_MF_K, m.tk}, {V2C_MF_E, m.e}, {V2C_MF_P, m.p}, {V2C_MF_XX, m.sxx},
+      {V2C_MF_XY, m.sxy}, {V2C_MF_EXX, m.exx}, {V2C_MF_EXY, m.exy}, {V2C_MF_VX, m.vx},
+      {V2C_MF_VY, m.vy}, {V2C_MF_PHI, m.phi}, {V2C_MF_C, m.coh}, {V2C_MF_SLIPV, m.slipv}};
+  for (auto &f : ff) {
+    if (!fields[f.id]) continue;
+    launch_unpermute_f32(f.src, m.id, ctx->d_stage64, n, st);
+    CK(cudaMemcpyAsync(fields[f.id], ctx->d_stage64, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  if (markt) {
+    launch_unpermute_i8(m.type, m.id, (int8_t *)ctx->d_stage64, n, st);
+    CK(cudaMemcpyAsync(markt, ctx->d_stage64, n, cudaMemcpyDeviceToHost, st));
+  }
+  if (fields[V2C_MF_D] || fields[V2C_MF_W]) {
+    std::vector<uint8_t> fl(n);
+    launch_unpermute_u8(m.flags, m.id, (uint8_t *)ctx->d_stage64b, n, st);
+    CK(cudaMemcpyAsync(fl.data(), ctx->d_stage64b, n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (long i = 0; i < n; i++)
+      if (fl[i] & MFLAG_RESET) {
+        if (fields[V2C_MF_D]) fields[V2C_MF_D][i] = -1.0;
+        if (fields[V2C_MF_W]) fields[V2C_MF_W][i] = -1.0;
+      }
+  }
+  CK(cudaStreamSynchronize(st));
+  return V2C_OK;
+}
+
+extern "C" int v2c_download_cells(v2c_ctx *ctx, int32_t *cell, long n) {
+  if (!ctx || !cell || n != ctx->n) return V2C_ERR_ARG;
+  launch_unpermute_i32(ctx->m.cell_in, ctx->m.id, (int32_t *)ctx->d_stage64, n, ctx->stream);
+  CK(cudaMemcpyAsync(cell, ctx->d_stage64, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return V2C_OK;
+}
+
+// ============================================================== node arrays
+// node fields live in FP32 on the device; they are converted on the way in
+// and out (the conversion kernels run on the context stream)
+extern "C" int v2c_upload_node_field(v2c_ctx *ctx, int field, const double *src) {
+  if (!ctx || !src || field < 0 || field >= V2C_NF_N) return V2C_ERR_ARG;
+  CK(cudaMemcpyAsync(ctx->d_node64, src, sizeof(double) * ctx->nn, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  launch_node_to_f32(ctx->d_node64, ctx->d_node + (long)field * ctx->nn, ctx->nn, ctx->stream);
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  return V2C_OK;
+}
+
+extern "C" int v2c_download_node_field(v2c_ctx *ctx, int field, double *dst) {
+  if (!ctx || !dst || field < 0 || field >= V2C_NF_N) return V2C_ERR_ARG;
+  launch_node_to_f64(ctx->d_node + (long)field * ctx->nn, ctx->d_node64, ctx->nn, ctx->stream);
+  ctx->launches += 1;
+  CK(cudaMemcpyAsync(dst, ctx->d_node64, sizeof(double) * ctx->nn, cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return V2C_OK;
+}
+
+// ============================================================ the MIC step
+static int ready(v2c_ctx *ctx) {
+  if (!ctx) return V2C_ERR_ARG;
+  if (!ctx->have_grid || !ctx->have_rock || !ctx->have_markers) return fail(ctx, V2C_ERR_STATE);
+  return V2C_OK;
+}
+
+static void swap_positions(v2c_ctx *ctx) {
+  std::swap(ctx->m.cell_in, ctx->m.cell_out);
+  std::swap(ctx->m.u_in, ctx->m.u_out);
+  std::swap(ctx->m.v_in, ctx->m.v_out);
+}
+
+extern "C" int v2c_marker2nodes(v2c_ctx *ctx) {
+  int rc = ready(ctx);
+  if (rc) return rc;
+  cudaStream_t st = ctx->stream;
+  if (!ctx->sorted) {
+    Prof pr(ctx, V2C_PROF_SORT);
+    launch_sort(ctx->m.cell_in, ctx->n, ctx->ncell, ctx->sb, ctx->d_stat, st);
+    ctx->launches += ctx->n > 0 ? 6 : 3;
+    ctx->sorted = true;
+  }
+  if (ctx->have_bonds) {
+    rc = build_bc(ctx);
+    if (rc) return fail(ctx, rc);
+  }
+  M2NArgs a;
+  a.g = make_grid(ctx);
+  a.N = make_nodes(ctx);
+  a.m = ctx->m;
+  a.R = Rock{ctx->d_rock};
+  a.S = make_scal(ctx->p, ctx->h_rt);
+  a.perm = ctx->sb.perm;
+  a.start = ctx->sb.start;
+  a.sticky_key = ctx->d_sticky;
+  a.stat = ctx->d_stat;
+  a.gxf = ctx->d_gxf;
+  a.gyf = ctx->d_gyf;
+  a.TX = pick_tx(ctx);
+  CK(cudaMemsetAsync(ctx->d_sticky, 0, sizeof(uint32_t) * ctx->nn, st));
+  {
+    Prof pr(ctx, V2C_PROF_M2N);
+    launch_m2n(a, st);
+  }
+  {
+    Prof pr(ctx, V2C_PROF_M2N_TAIL);
+    launch_sticky(a.N, ctx->d_sticky, ctx->nn, st);
+    ctx->launches += 2;
+    if (ctx->p.Dphis > 0) { launch_dphis(a.g, a.N, st); ctx->launches += 1; }
+    if (ctx->have_bonds && ctx->bc.n > 0) { launch_bc(ctx->bc, a.N, ctx->d_bc_scratch, st); ctx->launches += 2; }
+  }
+  CK(cudaGetLastError());
+  return V2C_OK;
+}
+
+extern "C" int v2c_center2basic_old(v2c_ctx *ctx) {
+  if (!ctx) return V2C_ERR_ARG;
+  {
+    Prof pr(ctx, V2C_PROF_C2B);
+    launch_c2b_old(make_grid(ctx), make_nodes(ctx), ctx->stream);
+  }
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  return V2C_OK;
+}
+
+extern "C" int v2c_compute_before_solve(v2c_ctx *ctx, double dt, int rk) {
+  if (!ctx) return V2C_ERR_ARG;
+  {
+    Prof pr(ctx, V2C_PROF_BEFORE);
+    launch_before_solve(make_grid(ctx), make_nodes(ctx), make_scal(ctx->p, ctx->h_rt), dt, rk,
+                        ctx->d_stat, ctx->stream);
+  }
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  return V2C_OK;
+}
+
+extern "C" int v2c_compute_after_solve(v2c_ctx *ctx, double dt, int rk, double *deltas) {
+  if (!ctx) return V2C_ERR_ARG;
+  {
+    Prof pr(ctx, V2C_PROF_AFTER);
+    launch_after_solve(make_grid(ctx), make_nodes(ctx), make_scal(ctx->p, ctx->h_rt), dt, rk,
+                       ctx->d_red, ctx->stream);
+  }
+  ctx->launches += 2;
+  CK(cudaGetLastError());
+  if (deltas) {
+    double h[2];
+    CK(cudaMemcpyAsync(h, ctx->d_red, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    *deltas = h[1] > 0 ? sqrt(h[0] / h[1]) : 0.0;
+  }
+  return V2C_OK;
+}
+
+static int n2m_move(v2c_ctx *ctx, int do_n2m, int do_move) {
+  int rc = ready(ctx);
+  if (rc) return rc;
+  cudaStream_t st = ctx->stream;
+  if (!ctx->sorted) {
+    Prof pr(ctx, V2C_PROF_SORT);
+    launch_sort(ctx->m.cell_in, ctx->n, ctx->ncell, ctx->sb, ctx->d_stat, st);
+    ctx->launches += ctx->n > 0 ? 6 : 3;
+    ctx->sorted = true;
+  }
+  N2MArgs a;
+  a.g = make_grid(ctx);
+  a.N = make_nodes(ctx);
+  a.m = ctx->m;
+  a.R = Rock{ctx->d_rock};
+  a.S = make_scal(ctx->p, ctx->h_rt);
+  a.perm = ctx->sb.perm;
+  a.start = ctx->sb.start;
+  a.stat = ctx->d_stat;
+  a.TX = pick_tx(ctx);
+  a.do_n2m = do_n2m;
+  a.do_move = do_move;
+  {
+    Prof pr(ctx, V2C_PROF_N2M_MOVE);
+    launch_n2m_move(a, st);
+  }
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  swap_positions(ctx);
+  if (do_move) {
+    // next step's order: counting sort of the new cells
+    Prof pr(ctx, V2C_PROF_SORT);
+    launch_sort(ctx->m.cell_in, ctx->n, ctx->ncell, ctx->sb, ctx->d_stat, st);
+    ctx->launches += ctx->n > 0 ? 6 : 3;
+    CK(cudaGetLastError());
+  }
+  return V2C_OK;
+}
+
+extern "C" int v2c_nodes2markers(v2c_ctx *ctx) { return n2m_move(ctx, 1, 0); }
+extern "C" int v2c_moveandrotatemarkers(v2c_ctx *ctx) { return n2m_move(ctx, 0, 1); }
+extern "C" int v2c_nodes2markers_move(v2c_ctx *ctx) { return n2m_move(ctx, 1, 1); }
+
+extern "C" int v2c_synchronize(v2c_ctx *ctx) {
+  if (!ctx) return V2C_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaGetLastError());
+  return V2C_OK;
+}
+
+extern "C" int v2c_get_status(v2c_ctx *ctx, v2c_status *out) {
+  if (!ctx || !out) return V2C_ERR_ARG;
+  unsigned long long h[ST_N];
+  CK(cudaMemcpyAsync(h, ctx->d_stat, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  memset(out, 0, sizeof(*out));
+  out->n_markers = ctx->n;
+  out->n_out_of_grid = (long)h[ST_OUT_OF_GRID];
+  out->n_far_moves = (long)h[ST_FAR_MOVES];
+  out->n_nan = (long)h[ST_NAN];
+  out->newton_iters = (long)h[ST_NEWTON_ITERS];
+  out->newton_fallbacks = (long)h[ST_NEWTON_FALLBACK];
+  out->newton_nonconv = (long)h[ST_NEWTON_NONCONV];
+  double r;
+  unsigned long long bits = h[ST_NEWTON_MAXRES_BITS];
+  memcpy(&r, &bits, sizeof(r));
+  out->newton_max_res = r;
+  out->max_cell_count = (long)h[ST_MAX_CELL];
+  out->kernel_launches = ctx->launches;
+  out->last_error = ctx->last_error;
+  return V2C_OK;
+}
+
+// ----------------------------------------------------- internal accessors
+// used by the per-marker Newton launcher (v2c_newton.cu)
+v2c::NewtonState *v2c_ctx_newton(v2c_ctx *ctx) { return &ctx->nw; }
+cudaStream_t v2c_ctx_stream(v2c_ctx *ctx) { return ctx->stream; }
+unsigned long long *v2c_ctx_stat(v2c_ctx *ctx) { return ctx->d_stat; }
+const v2c_params *v2c_ctx_params(v2c_ctx *ctx) { return &ctx->p; }
+
+extern "C" int v2c_set_profiling(v2c_ctx *ctx, int on) {
+  if (!ctx) return V2C_ERR_ARG;
+  prof_resolve(ctx);
+  for (int g = 0; g < V2C_PROF_N; g++) { ctx->prof_ms[g] = 0; ctx->prof_n[g] = 0; }
+  ctx->prof = on != 0;
+  return V2C_OK;
+}
+
+extern "C" int v2c_get_profile(v2c_ctx *ctx, int group, double *ms, long *launches) {
+  if (!ctx || group < 0 || group >= V2C_PROF_N) return V2C_ERR_ARG;
+  prof_resolve(ctx);
+  if (ms) *ms = ctx->prof_ms[group];
+  if (launches) *launches = ctx->prof_n[group];
+  return V2C_OK;
+}
+
+// lets the Newton launcher bracket its own launches
+void v2c_ctx_prof_begin(v2c_ctx *ctx, int group, cudaEvent_t *a) {
+  *a = nullptr;
+  if (ctx->prof) { *a = ev_get(ctx); cudaEventRecord(*a, ctx->stream); }
+}
+void v2c_ctx_prof_end(v2c_ctx *ctx, int group, cudaEvent_t a) {
+  if (ctx->prof && a) {
+    cudaEvent_t b = ev_get(ctx);
+    cudaEventRecord(b, ctx->stream);
+    ctx->prof_ev[group].push_back({a, b});
+  }
+}
+void v2c_ctx_count_launches(v2c_ctx *ctx, long k) { ctx->launches += k; }

@@ -1,0 +1,95 @@
+// v2c_kernels.h -- host-side launchers of the device kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "v2c_internal.cuh"
+
+namespace v2c {
+
+struct SortBufs {
+  int32_t *counts;   // [ncell]
+  int32_t *start;    // [ncell+1]
+  int32_t *slot;     // [cap]
+  int32_t *tmp;      // [cap]
+  int32_t *perm;     // [cap]
+  int32_t *blocksum; // scan scratch
+  long blocksum_cap;
+};
+
+// sort markers by cell (stable by array index): perm and start
+void launch_sort(const int32_t *cell, long n, long ncell, SortBufs &b,
+                 unsigned long long *stat, cudaStream_t st);
+
+// marker2nodes sweep (scatter + node tail) and its follow-ups
+struct M2NArgs {
+  Grid g;
+  Nodes N;
+  Markers m;
+  Rock R;
+  Scal S;
+  const int32_t *perm;
+  const int32_t *start;
+  uint32_t *sticky_key;
+  unsigned long long *stat;
+  const float *gxf, *gyf;  // FP32 line positions (coarse band test)
+  int TX;
+};
+void launch_m2n(const M2NArgs &a, cudaStream_t st);
+void launch_sticky(const Nodes &N, const uint32_t *key, long nn, cudaStream_t st);
+void launch_dphis(const Grid &g, const Nodes &N, cudaStream_t st);
+
+// boundary corrections: flattened rows x[row] = c + sum coef*value[ref]
+struct BcRows {
+  int n;            // rows
+  const int *field; // node field written
+  const long *node; // node written
+  const float *c;   // constant
+  const int *nref;  // number of references (<= V2C_BC_MAXREF)
+  const int *rfield;// [n*MAXREF] field of the referenced value
+  const long *rnode;// [n*MAXREF]
+  const float *rcoef;
+};
+#define V2C_BC_MAXREF 8
+void launch_bc(const BcRows &rows, const Nodes &N, float *scratch, cudaStream_t st);
+void launch_node_to_f32(const double *src, float *dst, long n, cudaStream_t st);
+void launch_node_to_f64(const float *src, double *dst, long n, cudaStream_t st);
+
+void launch_c2b_old(const Grid &g, const Nodes &N, cudaStream_t st);
+void launch_before_solve(const Grid &g, const Nodes &N, const Scal &S, double dt, int rk,
+                         unsigned long long *stat, cudaStream_t st);
+void launch_after_solve(const Grid &g, const Nodes &N, const Scal &S, double dt, int rk,
+                        double *red, cudaStream_t st);
+
+// nodes2markers + move sweep
+struct N2MArgs {
+  Grid g;
+  Nodes N;
+  Markers m;
+  Rock R;
+  Scal S;
+  const int32_t *perm;
+  const int32_t *start;
+  unsigned long long *stat;
+  int TX;
+  int do_n2m, do_move;
+};
+void launch_n2m_move(const N2MArgs &a, cudaStream_t st);
+
+// upload / download helpers
+void launch_assign(const Grid &g, const double *x, const double *y, long n, Markers m,
+                   unsigned long long *stat, cudaStream_t st);
+void launch_f64_to_f32(const double *src, float *dst, long n, cudaStream_t st);
+void launch_gather_f32(const float *src, const int32_t *perm, float *dst, long n, cudaStream_t st);
+void launch_gather_i32(const int32_t *src, const int32_t *perm, int32_t *dst, long n, cudaStream_t st);
+void launch_gather_i8(const int8_t *src, const int32_t *perm, int8_t *dst, long n, cudaStream_t st);
+void launch_gather_u8(const uint8_t *src, const int32_t *perm, uint8_t *dst, long n, cudaStream_t st);
+// out[id[i]] = (double)src[i]
+void launch_unpermute_f32(const float *src, const int32_t *id, double *out, long n, cudaStream_t st);
+void launch_unpermute_i32(const int32_t *src, const int32_t *id, int32_t *out, long n, cudaStream_t st);
+void launch_unpermute_u8(const uint8_t *src, const int32_t *id, uint8_t *out, long n, cudaStream_t st);
+void launch_unpermute_i8(const int8_t *src, const int32_t *id, int8_t *out, long n, cudaStream_t st);
+// FP64 positions in reference numbering
+void launch_positions(const Grid &g, const Markers &m, long n, double *x, double *y,
+                      cudaStream_t st);
+
+}  // namespace v2c

@@ -1,0 +1,466 @@
+// v2c_m2n.cu -- marker2nodes (interpolation.c:55-926) as a deterministic
+// segmented reduction over cell-sorted markers.
+//
+// Tiling.  A CTA owns node rows [j0, j0+TY) and node columns [i0, i0+TX).
+// It sweeps cell columns ci = i0-1 .. i0+TX-1.  For each column it stages the
+// column's markers of cell rows j0-1 .. j0+TY-1 (one contiguous run of the
+// sorted order) in shared memory, evaluating every marker's properties once.
+// Then thread (role, jl) accumulates, for node row j = j0+jl, the
+// contributions of cells (ci, j-1) and (ci, j), which are all the cells of
+// that column that reach node (ci, j) and (ci+1, j) under the
+// interpolationmod=2 stencil (interpolation.c:539-628):
+//   * basic node (ci, j) gets the left-half quadrants of those two cells,
+//     basic node (ci+1, j) the right-half ones -> kept in a register carry
+//     and completed when column ci+1 adds its left halves;
+//   * vx node (ci, j) gets cell (ci, j) if u < 0.5, vx node (ci+1, j) if
+//     u > 0.5 (carry);
+//   * vy node (ci, j) gets cell (ci, j-1) if v > 0.5 and cell (ci, j) if
+//     v < 0.5;
+//   * the centre node (ci+1, j+1) gets cell (ci, j) only.
+// Each node is summed by exactly one thread, in sorted-marker order, with
+// FP32 two-sum compensation; the node tail (normalisation, antidiffusion
+// correction, interpolation.c:714-824) runs in the same thread on the
+// compensated sums, rounding each result once to FP32.
+// No float atomics; the result does not depend on scheduling.
+//
+// Roles (one warp each per 32 node rows): 0 basic-node stress/state group,
+// 1 basic-node thermal group, 2 centre node, 3 vx and vy nodes.
+#include <math.h>
+
+#include "v2c_kernels.h"
+#include "v2c_rheology.cuh"
+
+namespace v2c {
+
+namespace {
+
+constexpr int TY = 32;
+constexpr int NTH = 4 * TY;
+constexpr int CHUNK = 480;
+
+enum {
+  P_U = 0, P_V, P_NU, P_NUG, P_E, P_SXY, P_EXY, P_COH, P_PHI, P_RO, P_ET, P_HT,
+  P_CP, P_KT, P_TK, P_SXX, P_EXX, P_P, P_VX, P_VY, P_N
+};
+
+struct Smem {
+  float p[P_N][CHUNK];
+  uint8_t act[CHUNK];
+};
+
+// stage one marker: properties (recalc_marker_properties.c) and payload
+__device__ __forceinline__ void stage(const M2NArgs &a, Smem &sm, int s, int k, int ci,
+                                      bool owned_col, int j0) {
+  const Grid &g = a.g;
+  const int idx = __ldg(a.perm + s);
+  const int c = a.m.cell_in[idx];
+  const int ix = c / g.ncy, iy = c - ix * g.ncy;
+  const float u = a.m.u_in[idx], v = a.m.v_in[idx];
+  const int t = a.m.type[idx];
+  const bool owned = owned_col && iy >= j0 && iy < j0 + TY;
+  (void)ci;
+
+  // sticky-air flags, interpolation.c:866-916: every marker (no in-grid
+  // test), the last one in reference numbering wins -> max of (id, type)
+  if (owned && (t == 1 || t == 2)) {
+    long m3 = (long)ix * g.yn + iy + 1, q = -1;
+    if (u < 0.5f && v < 0.5f) q = m3;
+    else if (u < 0.5f && v > 0.5f) q = m3 + 1;
+    else if (u > 0.5f && v < 0.5f) q = m3 + g.yn;
+    else if (u > 0.5f && v > 0.5f) q = m3 + g.yn + 1;
+    if (q >= 0 && q < g.nn)
+      atomicMax(a.sticky_key + q, ((uint32_t)a.m.id[idx] << 2) | (uint32_t)t);
+  }
+
+  // strictly inside the model (interpolation.c:219)
+  bool act = true;
+  if (ix == 0 || ix == g.ncx - 1) {
+    double x = g.gx[ix] + (double)u * (g.gx[ix + 1] - g.gx[ix]);
+    act = act && x > 0 && x < g.xsize;
+  }
+  if (iy == 0 || iy == g.ncy - 1) {
+    double y = g.gy[iy] + (double)v * (g.gy[iy + 1] - g.gy[iy]);
+    act = act && y > 0 && y < g.ysize;
+  }
+  sm.act[k] = act;
+  if (!act) return;
+
+  const Axis ax = make_axis(g.wx, g.ncx, ix, u * __ldg(g.wx + ix));
+  const Axis ay = make_axis(g.wy, g.ncy, iy, v * __ldg(g.wy + iy));
+  // pressure at the marker in bar, allinterpomp (interpolation.c:1923)
+  float e, n;
+  long m3 = stencil_centre(g, ax, ay, u > 0.5f, v > 0.5f, e, n);
+  const float mpb = 1e-5f * bil(a.N.f(V2C_NF_PR), m3, g.yn, e, n);
+  const float T = a.m.tk[idx];
+  float mro, mbb;
+  density32(a.R, a.S.p.densimod, t, T, mpb, mro, mbb);
+  const float mkt = conductivity32(a.R, t, T, mpb);
+  const float sxx = a.m.sxx[idx], sxy = a.m.sxy[idx];
+  const float sigin = sqrtf(sxx * sxx + sxy * sxy);
+  const float mnu = ductile_visc32(a.R, a.S, t, sigin, T, mpb);
+
+  // calc_frictionpara: only the state phi feeds the scatter.  Outside a
+  // 1 m margin of the frictional band the FP32 position decides; inside it
+  // the FP64 position does, as in the reference.
+  float phi = a.m.phi[idx];
+  if (t > 0) {
+    const v2c_params &p = a.S.p;
+    float xf = __ldg(a.gxf + ix) + ax.X, yf = __ldg(a.gyf + iy) + ay.X;
+    float rad = fabsf(yf - ((float)p.fault_y + (float)p.fault_slope * xf));
+    Fric fr;
+    if (rad > (float)p.fault_hw + 1.0f) {
+      phi = 50.f;
+    } else {
+      double x = g.gx[ix] + (double)u * (g.gx[ix + 1] - g.gx[ix]);
+      double y = g.gy[iy] + (double)v * (g.gy[iy + 1] - g.gy[iy]);
+      phi = friction_marker(p, a.S.phi_reset0, x, y, t, phi, fr);
+    }
+    // The update is idempotent, so a neighbouring tile that stages this
+    // marker as halo computes the same value whichever phi it reads.
+    if (owned && phi != a.m.phi[idx]) a.m.phi[idx] = phi;
+  }
+  if (owned) a.m.mnu[idx] = mnu;
+  if (owned && !(mnu > 0.f)) atomicAdd(a.stat + ST_NAN, 1ull);
+
+  const float mgg = a.R(RK_GG, t);
+  sm.p[P_U][k] = u;
+  sm.p[P_V][k] = v;
+  sm.p[P_NU][k] = mnu;
+  sm.p[P_NUG][k] = mnu / mgg;
+  sm.p[P_E][k] = a.m.e[idx];
+  sm.p[P_SXY][k] = sxy;
+  sm.p[P_EXY][k] = a.m.exy[idx];
+  sm.p[P_COH][k] = a.m.coh[idx];
+  sm.p[P_PHI][k] = phi;
+  sm.p[P_RO][k] = mro;
+  sm.p[P_ET][k] = mbb;
+  sm.p[P_HT][k] = a.R(RK_HT, t);
+  sm.p[P_CP][k] = a.R(RK_CP, t);
+  sm.p[P_KT][k] = mkt;
+  sm.p[P_TK][k] = T;
+  sm.p[P_SXX][k] = sxx;
+  sm.p[P_EXX][k] = a.m.exx[idx];
+  sm.p[P_P][k] = a.m.p[idx];
+  sm.p[P_VX][k] = a.m.vx[idx];
+  sm.p[P_VY][k] = a.m.vy[idx];
+}
+
+// calc_frictionpara_nodes (calc_RSF.c:298-350), FP64
+__device__ void friction_node(const v2c_params &p, double x, double y, double &mu, double &a,
+                              double &b, double &L, double &V0) {
+  double d = y - (p.fault_y + p.fault_slope * x);
+  double radius = d >= 0 ? d : -d;
+  if (radius <= p.fault_hw) {
+    if (x > p.end_updip && x < p.start_downdip) {
+      a = p.a_vw; b = p.b_vw; L = p.L_vw; V0 = p.V0_vw;
+    } else if (x >= p.start_updip && x <= p.end_updip && p.half_range > 0) {
+      double f = (x - (p.start_updip)) / (2 * p.half_range);
+      a = p.a_vs + f * (p.a_vw - p.a_vs); b = p.b_vs + f * (p.b_vw - p.b_vs);
+      L = p.L_vs + f * (p.L_vw - p.L_vs); V0 = p.V0_vs + f * (p.V0_vw - p.V0_vs);
+    } else if (x >= p.start_downdip && x < p.end_downdip && p.half_range > 0) {
+      double f = (x - (p.start_downdip)) / (2 * p.half_range);
+      a = p.a_vw - f * (p.a_vw - p.a_vs); b = p.b_vw - f * (p.b_vw - p.b_vs);
+      L = p.L_vw - f * (p.L_vw - p.L_vs); V0 = p.V0_vw - f * (p.V0_vw - p.V0_vs);
+    } else {
+      a = p.a_vs; b = p.b_vs; L = p.L_vs; V0 = p.V0_vs;
+    }
+    mu = 0.2;
+  } else {
+    mu = 0.6; a = p.a_hr; b = p.b_hr; L = p.L_hr; V0 = p.V0_hr;
+  }
+}
+
+// role 0 / role 1 accumulation into a named register array
+#define ADD_BASIC_A(A, q, w)                                          \
+  do {                                                                \
+    A[0].add(sm.p[P_NU][q] * (w)); A[1].add(sm.p[P_NUG][q] * (w));    \
+    A[2].add(sm.p[P_E][q] * (w)); A[3].add(sm.p[P_SXY][q] * (w));     \
+    A[4].add(sm.p[P_EXY][q] * (w)); A[5].add(sm.p[P_COH][q] * (w));   \
+    A[6].add(sm.p[P_PHI][q] * (w)); A[7].add(w);                      \
+  } while (0)
+#define ADD_BASIC_B(A, q, w)                                          \
+  do {                                                                \
+    A[0].add(sm.p[P_RO][q] * (w)); A[1].add(sm.p[P_ET][q] * (w));     \
+    A[2].add(sm.p[P_HT][q] * (w)); A[3].add(sm.p[P_CP][q] * (w));     \
+    A[4].add(sm.p[P_KT][q] * (w)); A[5].add(sm.p[P_TK][q] * (w));     \
+    A[6].add(w);                                                      \
+  } while (0)
+
+__global__ void __launch_bounds__(NTH) k_m2n(M2NArgs a) {
+  __shared__ Smem sm;
+  const Grid &g = a.g;
+  const int tid = threadIdx.x, role = tid / TY, jl = tid % TY;
+  const int i0 = blockIdx.x * a.TX, j0 = blockIdx.y * TY;
+  const int j = j0 + jl;
+  const bool jvalid = j < g.yn;
+  const int ncy = g.ncy;
+  const int ci_end = min(i0 + a.TX, g.xn);
+
+  // role 0: nu, nu/G, e, sxy, exy, C, phi, w      role 1: ro, et, ht, cp, kt, tk, w
+  // role 2: nu, nu/G, sxx, exx, p, w (centre)     role 3: vx*ro, ro, w (vx) + vy*ro, ro, w (vy)
+  Acc cur[8], car[8], vy3[3];
+#pragma unroll
+  for (int q = 0; q < 8; q++) { cur[q].zero(); car[q].zero(); }
+#pragma unroll
+  for (int q = 0; q < 3; q++) vy3[q].zero();
+
+  for (int ci = max(i0 - 1, 0); ci < ci_end; ++ci) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) { cur[q] = car[q]; car[q].zero(); }
+#pragma unroll
+    for (int q = 0; q < 3; q++) vy3[q].zero();
+    if (role == 2) {
+#pragma unroll
+      for (int q = 0; q < 8; q++) cur[q].zero();
+    }
+
+    if (ci < g.ncx) {
+      const int jlo = max(j0 - 1, 0), jhi = min(j0 + TY - 1, ncy - 1);
+      const long cb = (long)ci * ncy;
+      const int seg_b = __ldg(a.start + cb + jlo), seg_e = __ldg(a.start + cb + jhi + 1);
+      int lo_b = 0, lo_e = 0, up_b = 0, up_e = 0;
+      float s1lo = 0.f, s1up = 0.f;
+      const float iwx = 1.f / __ldg(g.wx + ci);
+      if (jvalid && j - 1 >= 0 && j - 1 <= ncy - 1) {
+        lo_b = __ldg(a.start + cb + j - 1);
+        lo_e = __ldg(a.start + cb + j);
+        s1lo = iwx / __ldg(g.wy + j - 1);
+      }
+      if (jvalid && j <= ncy - 1) {
+        up_b = __ldg(a.start + cb + j);
+        up_e = __ldg(a.start + cb + j + 1);
+        s1up = iwx / __ldg(g.wy + j);
+      }
+      const bool owned_col = ci >= i0;
+      for (int cs = seg_b; cs < seg_e; cs += CHUNK) {
+        const int ce = min(cs + CHUNK, seg_e);
+        __syncthreads();
+        for (int k = tid; k < ce - cs; k += NTH) stage(a, sm, cs + k, k, ci, owned_col, j0);
+        __syncthreads();
+        // cell (ci, j-1): bottom halves (v > 0.5) reach node row j
+        for (int s = max(lo_b, cs); s < min(lo_e, ce); ++s) {
+          const int q = s - cs;
+          if (!sm.act[q]) continue;
+          const float u = sm.p[P_U][q], v = sm.p[P_V][q];
+          if (role <= 1) {
+            if (!(v > 0.5f)) continue;
+            if (u < 0.5f) {
+              const float w = s1lo * (1.f - 2.f * u) * (2.f * v - 1.f);
+              if (role == 0) ADD_BASIC_A(cur, q, w); else ADD_BASIC_B(cur, q, w);
+            } else if (u > 0.5f) {
+              const float w = s1lo * (2.f * u - 1.f) * (2.f * v - 1.f);
+              if (role == 0) ADD_BASIC_A(car, q, w); else ADD_BASIC_B(car, q, w);
+            }
+          } else if (role == 3) {
+            if (v > 0.5f) {
+              const float w = s1lo * (1.f - fabsf(u - 0.5f)) * v;
+              const float ro = sm.p[P_RO][q];
+              vy3[0].add(sm.p[P_VY][q] * ro * w); vy3[1].add(ro * w); vy3[2].add(w);
+            }
+          }
+        }
+        // cell (ci, j): top halves reach node row j, the whole cell its centre
+        for (int s = max(up_b, cs); s < min(up_e, ce); ++s) {
+          const int q = s - cs;
+          if (!sm.act[q]) continue;
+          const float u = sm.p[P_U][q], v = sm.p[P_V][q];
+          if (role <= 1) {
+            if (!(v < 0.5f)) continue;
+            if (u < 0.5f) {
+              const float w = s1up * (1.f - 2.f * u) * (1.f - 2.f * v);
+              if (role == 0) ADD_BASIC_A(cur, q, w); else ADD_BASIC_B(cur, q, w);
+            } else if (u > 0.5f) {
+              const float w = s1up * (2.f * u - 1.f) * (1.f - 2.f * v);
+              if (role == 0) ADD_BASIC_A(car, q, w); else ADD_BASIC_B(car, q, w);
+            }
+          } else if (role == 2) {
+            const float w = s1up * (1.f - 2.f * fabsf(u - 0.5f)) * (1.f - 2.f * fabsf(v - 0.5f));
+            cur[0].add(sm.p[P_NU][q] * w); cur[1].add(sm.p[P_NUG][q] * w);
+            cur[2].add(sm.p[P_SXX][q] * w); cur[3].add(sm.p[P_EXX][q] * w);
+            cur[4].add(sm.p[P_P][q] * w); cur[5].add(w);
+          } else {
+            const float ro = sm.p[P_RO][q];
+            if (u < 0.5f) {
+              const float w = s1up * (1.f - u) * (1.f - fabsf(v - 0.5f));
+              cur[0].add(sm.p[P_VX][q] * ro * w); cur[1].add(ro * w); cur[2].add(w);
+            } else if (u > 0.5f) {
+              const float w = s1up * u * (1.f - fabsf(v - 0.5f));
+              car[0].add(sm.p[P_VX][q] * ro * w); car[1].add(ro * w); car[2].add(w);
+            }
+            if (v < 0.5f) {
+              const float w = s1up * (1.f - fabsf(u - 0.5f)) * (1.f - v);
+              vy3[0].add(sm.p[P_VY][q] * ro * w); vy3[1].add(ro * w); vy3[2].add(w);
+            }
+          }
+        }
+      }
+    }
+
+    // ------------------------------------------------------ node tail
+    if (ci < i0 || !jvalid) continue;
+    const long m3 = (long)ci * g.yn + j;
+    const Nodes &N = a.N;
+    const int antid = a.S.antid;
+    if (role == 0) {
+      const float ss = cur[7].value();
+      const bool interior = ci >= 1 && j >= 1 && ci < g.xn - 1 && j < g.yn - 1;
+      if (ss != 0.f && interior) {
+        float phin = cur[6].value() / ss, sxyen = cur[3].value() / ss;
+        float exyen = cur[4].value() / ss, pen = cur[2].value() / ss;
+        float phis, sxye, exye, pe;
+        if (antid) {
+          phis = N.f(V2C_NF_PHIS_IT)[m3] + (phin - N.f(V2C_NF_PHIE)[m3]);
+          sxye = N.f(V2C_NF_SXY)[m3] + (sxyen - N.f(V2C_NF_SXYEE)[m3]);
+          exye = N.f(V2C_NF_EXY)[m3] + (exyen - N.f(V2C_NF_EXYEE)[m3]);
+          pe = N.f(V2C_NF_PES)[m3] + (pen - N.f(V2C_NF_PEE)[m3]);
+        } else {
+          phis = phin; sxye = sxyen; exye = exyen; pe = pen;
+        }
+        if (pe < 0.f) pe = 0.f;
+        float nu_m2c = cur[0].value() / ss;
+        N.f(V2C_NF_PHIN)[m3] = phin;
+        N.f(V2C_NF_SXYEN)[m3] = sxyen;
+        N.f(V2C_NF_EXYEN)[m3] = exyen;
+        N.f(V2C_NF_PEN)[m3] = pen;
+        N.f(V2C_NF_PHIS)[m3] = phis;
+        N.f(V2C_NF_SXYE)[m3] = sxye;
+        N.f(V2C_NF_EXYE)[m3] = exye;
+        N.f(V2C_NF_PE)[m3] = pe;
+        N.f(V2C_NF_COHESION)[m3] = cur[5].value() / ss;
+        N.f(V2C_NF_NU_M2C)[m3] = nu_m2c;
+        N.f(V2C_NF_GG)[m3] = nu_m2c / (cur[1].value() / ss);
+      } else {
+        N.f(V2C_NF_PHIN)[m3] = 0; N.f(V2C_NF_SXYEN)[m3] = 0; N.f(V2C_NF_EXYEN)[m3] = 0;
+        N.f(V2C_NF_PHIS)[m3] = 0; N.f(V2C_NF_SXYE)[m3] = 0; N.f(V2C_NF_EXYE)[m3] = 0;
+        N.f(V2C_NF_COHESION)[m3] = 0; N.f(V2C_NF_GG)[m3] = 0;
+      }
+    } else if (role == 1) {
+      const float ss = cur[6].value();
+      const bool interior = ci >= 1 && j >= 1 && ci < g.xn - 1 && j < g.yn - 1;
+      double mu = 0, fa = 0, fb = 0, fL = 0, fV0 = 0;
+      if (ss != 0.f && interior) friction_node(a.S.p, g.gx[ci], g.gy[j], mu, fa, fb, fL, fV0);
+      N.f(V2C_NF_MUS_S)[m3] = (float)mu; N.f(V2C_NF_AS)[m3] = (float)fa; N.f(V2C_NF_BS)[m3] = (float)fb;
+      N.f(V2C_NF_LS)[m3] = (float)fL; N.f(V2C_NF_V0S)[m3] = (float)fV0;
+      if (ss != 0.f) {
+        N.f(V2C_NF_RO)[m3] = cur[0].value() / ss; N.f(V2C_NF_ET)[m3] = cur[1].value() / ss;
+        N.f(V2C_NF_HT)[m3] = cur[2].value() / ss; N.f(V2C_NF_CP)[m3] = cur[3].value() / ss;
+        N.f(V2C_NF_KT)[m3] = cur[4].value() / ss; N.f(V2C_NF_TK)[m3] = cur[5].value() / ss;
+      } else {
+        N.f(V2C_NF_RO)[m3] = 0; N.f(V2C_NF_ET)[m3] = 0; N.f(V2C_NF_HT)[m3] = 0;
+        N.f(V2C_NF_CP)[m3] = 0; N.f(V2C_NF_KT)[m3] = 0; N.f(V2C_NF_TK)[m3] = 0;
+      }
+      // arrays the reference zeroes at the start (interpolation.c:58-153)
+      // and that marker2nodes itself does not fill
+      static const int zl[] = {V2C_NF_NU, V2C_NF_ND, V2C_NF_WTPHISUM, V2C_NF_WTSXXSUM,
+                               V2C_NF_WTVXSUM, V2C_NF_WTVYSUM, V2C_NF_PHISUM, V2C_NF_SXYSUM,
+                               V2C_NF_EXYSUM, V2C_NF_ESUM, V2C_NF_SXXSUM, V2C_NF_EXXSUM,
+                               V2C_NF_VXSUM, V2C_NF_VYSUM, V2C_NF_PSUM, V2C_NF_MRX0,
+                               V2C_NF_MRY0};
+#pragma unroll
+      for (int q = 0; q < (int)(sizeof(zl) / sizeof(zl[0])); q++) N.f(zl[q])[m3] = 0;
+    } else if (role == 2) {
+      // centre node (ci+1, j+1) from cell (ci, j)
+      if (ci < g.ncx && j < ncy) {
+        const long mc = (long)(ci + 1) * g.yn + (j + 1);
+        const float s1 = cur[5].value();
+        if (s1 != 0.f) {
+          float sxxen = cur[2].value() / s1, sppen = cur[4].value() / s1;
+          float exxen = cur[3].value() / s1;
+          float sxxe, sppe, exxe;
+          if (antid) {
+            sxxe = N.f(V2C_NF_SXX)[mc] + (sxxen - N.f(V2C_NF_SXXEE)[mc]);
+            sppe = N.f(V2C_NF_PR)[mc] + (sppen - N.f(V2C_NF_SPPEE)[mc]);
+            exxe = N.f(V2C_NF_EXX)[mc] + (exxen - N.f(V2C_NF_EXXEE)[mc]);
+          } else {
+            sxxe = sxxen; sppe = sppen; exxe = exxen;
+          }
+          if (a.S.p.timesum == 0 && a.S.p.reloadfromDP == 0 && a.S.p.compressiblemode == 1)
+            sppe = (float)a.S.p.nstress;
+          float nd = cur[0].value() / s1;
+          N.f(V2C_NF_SXXEN)[mc] = sxxen; N.f(V2C_NF_SPPEN)[mc] = sppen;
+          N.f(V2C_NF_EXXEN)[mc] = exxen; N.f(V2C_NF_SXXE)[mc] = sxxe;
+          N.f(V2C_NF_SPPE)[mc] = sppe; N.f(V2C_NF_EXXE)[mc] = exxe;
+          N.f(V2C_NF_ND_M2C)[mc] = nd;
+          N.f(V2C_NF_GD)[mc] = nd / (cur[1].value() / s1);
+          N.f(V2C_NF_BM)[mc] = 50e9f;
+          N.f(V2C_NF_DRO)[mc] = 0; N.f(V2C_NF_DRP)[mc] = 0;
+        } else {
+          N.f(V2C_NF_SXXEN)[mc] = 0; N.f(V2C_NF_SPPEN)[mc] = 0; N.f(V2C_NF_EXXEN)[mc] = 0;
+          N.f(V2C_NF_SXXE)[mc] = 0; N.f(V2C_NF_SPPE)[mc] = 0; N.f(V2C_NF_EXXE)[mc] = 0;
+          N.f(V2C_NF_GD)[mc] = 0; N.f(V2C_NF_BM)[mc] = 0;
+          N.f(V2C_NF_DRO)[mc] = 0; N.f(V2C_NF_DRP)[mc] = 0;
+        }
+      }
+      // centre fields of nodes no cell feeds (first column / first row)
+      if (ci == 0 || j == 0) {
+        N.f(V2C_NF_SXXEN)[m3] = 0; N.f(V2C_NF_SPPEN)[m3] = 0; N.f(V2C_NF_EXXEN)[m3] = 0;
+        N.f(V2C_NF_SXXE)[m3] = 0; N.f(V2C_NF_SPPE)[m3] = 0; N.f(V2C_NF_EXXE)[m3] = 0;
+        N.f(V2C_NF_GD)[m3] = 0; N.f(V2C_NF_BM)[m3] = 0;
+        N.f(V2C_NF_DRO)[m3] = 0; N.f(V2C_NF_DRP)[m3] = 0;
+      }
+    } else {
+      const float wx = cur[2].value();
+      if (wx != 0.f) {
+        float mrx0 = cur[1].value();
+        float mvxn = cur[0].value() / mrx0;
+        N.f(V2C_NF_MVXN)[m3] = mvxn;
+        N.f(V2C_NF_MVX)[m3] = antid ? N.f(V2C_NF_VX)[m3] + (mvxn - N.f(V2C_NF_MVXE)[m3]) : mvxn;
+        N.f(V2C_NF_MRX)[m3] = mrx0 / wx;
+      } else {
+        N.f(V2C_NF_MVX)[m3] = 0; N.f(V2C_NF_MRX)[m3] = 0;
+      }
+      const float wy = vy3[2].value();
+      if (wy != 0.f) {
+        float mry0 = vy3[1].value();
+        float mvyn = vy3[0].value() / mry0;
+        N.f(V2C_NF_MVYN)[m3] = mvyn;
+        N.f(V2C_NF_MVY)[m3] = antid ? N.f(V2C_NF_VY)[m3] + (mvyn - N.f(V2C_NF_MVYE)[m3]) : mvyn;
+        N.f(V2C_NF_MRY)[m3] = mry0 / wy;
+      } else {
+        N.f(V2C_NF_MVY)[m3] = 0; N.f(V2C_NF_MRY)[m3] = 0;
+      }
+    }
+  }
+}
+
+__global__ void k_sticky(float *st, const uint32_t *key, long nn) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < nn) {
+    uint32_t k = key[i];
+    st[i] = k ? (float)(k & 3u) : 0.f;
+  }
+}
+
+// ghost copy of the state when it diffuses, interpolation.c:827-859
+__global__ void k_dphis(Grid g, float *phis) {
+  long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (m3 >= g.nn) return;
+  const int yn = g.yn, xn = g.xn;
+  int m22 = (int)(m3 % yn), m11 = (int)(m3 / yn);
+  float v;
+  if (m11 == 0 && m22 >= 1 && m22 <= yn - 2) v = phis[m3 + yn];
+  else if (m11 == xn - 1 && m22 >= 1 && m22 <= yn - 2) v = phis[m3 - yn];
+  else if (m22 == 0 && m11 >= 1 && m11 <= xn - 2) v = phis[m3 + 1];
+  else if (m22 == yn - 1 && m11 > 0 && m11 <= xn - 2) v = phis[m3 - 1];
+  else if ((m11 == 0 || m11 == xn - 1) && (m22 == 0 || m22 == yn - 1)) v = 0.f;
+  else return;
+  // boundary values only read interior ones: no read-after-write hazard
+  phis[m3] = v;
+}
+
+}  // namespace
+
+void launch_m2n(const M2NArgs &a, cudaStream_t st) {
+  dim3 grid((a.g.xn + a.TX - 1) / a.TX, (a.g.yn + TY - 1) / TY);
+  k_m2n<<<grid, NTH, 0, st>>>(a);
+}
+
+void launch_sticky(const Nodes &N, const uint32_t *key, long nn, cudaStream_t st) {
+  k_sticky<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(N.f(V2C_NF_STICKY01), key, nn);
+}
+
+void launch_dphis(const Grid &g, const Nodes &N, cudaStream_t st) {
+  k_dphis<<<(unsigned)((g.nn + 255) / 256), 256, 0, st>>>(g, N.f(V2C_NF_PHIS));
+}
+
+}  // namespace v2c

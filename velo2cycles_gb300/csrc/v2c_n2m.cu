@@ -1,0 +1,453 @@
+// v2c_n2m.cu -- nodes2markers (interpolation.c:929-1490) fused with
+// moveandrotatemarkers (moveandrotatemarkers.c:1-178) in one marker pass.
+//
+// Same tiling as the marker2nodes sweep (see v2c_m2n.cu).  Staging a marker
+// gathers the 19 node fields of interpolate_mechanical from the four
+// staggered stencils in cell-local FP32 coordinates and keeps the quantities
+// the antidiffusion correction scatters back (PHIS, SXY, EXY, ES to basic
+// nodes, PR, SXX, EXX to the centre node, VX*MRO, VY*MRO and MRO to vx/vy
+// nodes).  The tile that owns the marker also applies the marker update and
+// then moves it (Euler or RK4 through four allinteri evaluations,
+// interpolation.c:1688-1758) and rotates its stress; new positions go to
+// the second position buffer so neighbouring tiles still see the old one.
+// The back-scatter sums are formed per node by one thread each, in sorted
+// marker order with two-sum compensation, exactly as in marker2nodes.
+#include <math.h>
+
+#include "v2c_kernels.h"
+#include "v2c_rheology.cuh"
+
+namespace v2c {
+
+namespace {
+
+constexpr int TY = 32;
+constexpr int NTH = 4 * TY;
+constexpr int CHUNK = 640;
+
+enum { Q_U = 0, Q_V, Q_PHIS, Q_SXY, Q_EXY, Q_ES, Q_PR, Q_SXX, Q_EXX, Q_VX, Q_VY, Q_MRO, Q_N };
+
+struct Smem {
+  float q[Q_N][CHUNK];
+};
+
+struct Pos {
+  int ix, iy;
+  float X, Y;  // metres from gx[ix], gy[iy]
+};
+
+// put a position back in the cell that contains it; FP64 search if it
+// crossed more than four cells
+__device__ __forceinline__ void settle(const Grid &g, Pos &p, unsigned long long *stat) {
+  int ix0 = p.ix, iy0 = p.iy;
+  float X0 = p.X, Y0 = p.Y;
+  if (!relocate(g.wx, g.ncx, p.ix, p.X, 4)) {
+    double x = g.gx[ix0] + (double)X0;
+    p.ix = nsearch64(g.gx, g.xn, x);
+    p.X = (float)(x - g.gx[p.ix]);
+    atomicAdd(stat + ST_FAR_MOVES, 1ull);
+  }
+  if (!relocate(g.wy, g.ncy, p.iy, p.Y, 4)) {
+    double y = g.gy[iy0] + (double)Y0;
+    p.iy = nsearch64(g.gy, g.yn, y);
+    p.Y = (float)(y - g.gy[p.iy]);
+    atomicAdd(stat + ST_FAR_MOVES, 1ull);
+  }
+}
+
+// allinteri (interpolation.c:1688-1758): velocity and spin at a point
+__device__ void allinteri(const Grid &g, const Nodes &N, Pos p, float &VX, float &VY,
+                          float &ESP) {
+  // clamp into the model
+  float wx = __ldg(g.wx + p.ix), wy = __ldg(g.wy + p.iy);
+  if (p.ix == 0 && p.X < 0.f) p.X = 0.f;
+  if (p.ix == g.ncx - 1 && p.X > wx) p.X = wx;
+  if (p.iy == 0 && p.Y < 0.f) p.Y = 0.f;
+  if (p.iy == g.ncy - 1 && p.Y > wy) p.Y = wy;
+  float xrat = 2.f / 3.f;
+  if (p.ix == 0 && p.X < 0.5f * wx) xrat = 1.f;
+  if (p.ix == g.ncx - 1 && p.X > 0.5f * wx) xrat = 1.f;
+  if (p.iy == 0 && p.Y < 0.5f * wy) xrat = 1.f;
+  if (p.iy == g.ncy - 1 && p.Y > 0.5f * wy) xrat = 1.f;
+  const Axis ax = make_axis(g.wx, g.ncx, p.ix, p.X);
+  const Axis ay = make_axis(g.wy, g.ncy, p.iy, p.Y);
+  const long yn = g.yn;
+  float e, n;
+  // exy, esp at basic nodes
+  long m3 = stencil_basic(g, ax, ay, e, n);
+  const float EXY = bil(N.f(V2C_NF_EXY), m3, yn, e, n);
+  ESP = bil(N.f(V2C_NF_ESP), m3, yn, e, n);
+  // exx and velocities averaged to pressure nodes
+  m3 = stencil_centre(g, ax, ay, p.X > 0.5f * wx, p.Y > 0.5f * wy, e, n);
+  const float *vx = N.f(V2C_NF_VX), *vy = N.f(V2C_NF_VY);
+  const float EXX = bil(N.f(V2C_NF_EXX), m3, yn, e, n);
+  (void)EXX;
+  float d0 = (1.f - e) * (1.f - n), d1 = (1.f - e) * n, d2 = e * (1.f - n), d3 = e * n;
+  const float vxm1 = __ldg(vx + m3 - 1), vxc = __ldg(vx + m3);
+  VX = (d0 * (vxm1 + __ldg(vx + m3 - yn - 1)) + d1 * (vxc + __ldg(vx + m3 - yn)) +
+        d2 * (__ldg(vx + m3 + yn - 1) + vxm1) + d3 * (__ldg(vx + m3 + yn) + vxc)) *
+       0.5f * (1.f - xrat);
+  const float vyc = __ldg(vy + m3), vyu = __ldg(vy + m3 - yn);
+  VY = (d0 * (vyu + __ldg(vy + m3 - yn - 1)) + d1 * (__ldg(vy + m3 - yn + 1) + vyu) +
+        d2 * (vyc + __ldg(vy + m3 - 1)) + d3 * (__ldg(vy + m3 + 1) + vyc)) *
+       0.5f * (1.f - xrat);
+  // staggered vx and vy
+  m3 = stencil_vx(g, ax, ay, p.Y < 0.5f * wy, g.xn - 2, e, n);
+  VX += bil(vx, m3, yn, e, n) * xrat;
+  m3 = stencil_vy(g, ax, ay, p.X < 0.5f * wx, g.yn - 2, e, n);
+  VY += bil(vy, m3, yn, e, n) * xrat;
+}
+
+// basic-node back-scatter into a named register array
+#define ADD_BS(A, q, w)                                                 \
+  do {                                                                  \
+    A[0].add(sm.q[Q_PHIS][q] * (w)); A[1].add(sm.q[Q_SXY][q] * (w));    \
+    A[2].add(sm.q[Q_EXY][q] * (w)); A[3].add(sm.q[Q_ES][q] * (w));      \
+    A[4].add(w);                                                        \
+  } while (0)
+
+__global__ void __launch_bounds__(NTH) k_n2m_move(N2MArgs a) {
+  __shared__ Smem sm;
+  const Grid &g = a.g;
+  const Nodes &N = a.N;
+  const int tid = threadIdx.x, role = tid / TY, jl = tid % TY;
+  const int i0 = blockIdx.x * a.TX, j0 = blockIdx.y * TY;
+  const int j = j0 + jl;
+  const bool jvalid = j < g.yn;
+  const int ncy = g.ncy;
+  const int ci_end = min(i0 + a.TX, g.xn);
+  const v2c_params &P = a.S.p;
+  const int backscatter = a.do_n2m && P.antidiffinter == 1;
+  const long yn = g.yn;
+
+  // role 0: PHIS, SXY, EXY, ES, w (basic)   role 1: PR, SXX, EXX, w (centre)
+  // role 2: VX*MRO, MRO, w (vx)             role 3: VY*MRO, MRO, w (vy)
+  Acc cur[5], car[5];
+#pragma unroll
+  for (int q = 0; q < 5; q++) { cur[q].zero(); car[q].zero(); }
+
+  for (int ci = max(i0 - 1, 0); ci < ci_end; ++ci) {
+#pragma unroll
+    for (int q = 0; q < 5; q++) { cur[q] = car[q]; car[q].zero(); }
+    if (role == 1 || role == 3) {
+#pragma unroll
+      for (int q = 0; q < 5; q++) cur[q].zero();
+    }
+    if (ci < g.ncx) {
+      const int jlo = max(j0 - 1, 0), jhi = min(j0 + TY - 1, ncy - 1);
+      const long cb = (long)ci * ncy;
+      const int seg_b = __ldg(a.start + cb + jlo), seg_e = __ldg(a.start + cb + jhi + 1);
+      int lo_b = 0, lo_e = 0, up_b = 0, up_e = 0;
+      float s1lo = 0.f, s1up = 0.f;
+      const float iwx = 1.f / __ldg(g.wx + ci);
+      if (jvalid && j - 1 >= 0 && j - 1 <= ncy - 1) {
+        lo_b = __ldg(a.start + cb + j - 1); lo_e = __ldg(a.start + cb + j);
+        s1lo = iwx / __ldg(g.wy + j - 1);
+      }
+      if (jvalid && j <= ncy - 1) {
+        up_b = __ldg(a.start + cb + j); up_e = __ldg(a.start + cb + j + 1);
+        s1up = iwx / __ldg(g.wy + j);
+      }
+      const bool owned_col = ci >= i0;
+      for (int cs = seg_b; cs < seg_e; cs += CHUNK) {
+        const int ce = min(cs + CHUNK, seg_e);
+        if (backscatter) __syncthreads();
+        for (int k = tid; k < ce - cs; k += NTH) {
+          // ---------------------------------------------- stage marker
+          const int idx = __ldg(a.perm + cs + k);
+          const int c = a.m.cell_in[idx];
+          const int ix = c / ncy, iy = c - ix * ncy;
+          const float u = a.m.u_in[idx], v = a.m.v_in[idx];
+          const int t = a.m.type[idx];
+          const bool owned = owned_col && iy >= j0 && iy < j0 + TY;
+          if (!owned && !backscatter) continue;
+          // interpolate_mechanical clamps the point into the model first
+          float uc = u, vc = v;
+          if (ix == 0 && uc < 0.f) uc = 0.f;
+          if (ix == g.ncx - 1 && uc > 1.f) uc = 1.f;
+          if (iy == 0 && vc < 0.f) vc = 0.f;
+          if (iy == g.ncy - 1 && vc > 1.f) vc = 1.f;
+          const float wxc = __ldg(g.wx + ix), wyc = __ldg(g.wy + iy);
+          const Axis ax = make_axis(g.wx, g.ncx, ix, uc * wxc);
+          const Axis ay = make_axis(g.wy, g.ncy, iy, vc * wyc);
+          float e, n;
+          long m3 = stencil_basic(g, ax, ay, e, n);
+          const float EXY = bil(N.f(V2C_NF_EXY), m3, yn, e, n);
+          const float SXY = bil(N.f(V2C_NF_SXY), m3, yn, e, n);
+          const float ES = bil(N.f(V2C_NF_PES), m3, yn, e, n);
+          const float PHIS = bil(N.f(V2C_NF_PHIS_IT), m3, yn, e, n);
+          float EXYE = 0.f, SXYE = 0.f, ESE = 0.f, PHISE = 0.f;
+          if (owned && P.antidiffinter != 1) {
+            EXYE = bil(N.f(V2C_NF_EXYE), m3, yn, e, n);
+            SXYE = bil(N.f(V2C_NF_SXYE), m3, yn, e, n);
+            ESE = bil(N.f(V2C_NF_PE), m3, yn, e, n);
+            PHISE = bil(N.f(V2C_NF_PHIS), m3, yn, e, n);
+          }
+          m3 = stencil_centre(g, ax, ay, uc > 0.5f, vc > 0.5f, e, n);
+          const float EXX = bil(N.f(V2C_NF_EXX), m3, yn, e, n);
+          const float SXX = bil(N.f(V2C_NF_SXX), m3, yn, e, n);
+          const float PR = bil(N.f(V2C_NF_PR), m3, yn, e, n);
+          float EXXE = 0.f, SXXE = 0.f, SPPE = 0.f;
+          if (owned && P.antidiffinter != 1) {
+            EXXE = bil(N.f(V2C_NF_EXXE), m3, yn, e, n);
+            SXXE = bil(N.f(V2C_NF_SXXE), m3, yn, e, n);
+            SPPE = bil(N.f(V2C_NF_SPPE), m3, yn, e, n);
+          }
+          m3 = stencil_vx(g, ax, ay, vc < 0.5f, g.xn - 2, e, n);
+          const float VX = bil(N.f(V2C_NF_VX), m3, yn, e, n);
+          const float MVX = (owned && P.antidiffinter != 1) ? bil(N.f(V2C_NF_MVX), m3, yn, e, n) : 0.f;
+          m3 = stencil_vy(g, ax, ay, uc < 0.5f, g.yn - 2, e, n);
+          const float VY = bil(N.f(V2C_NF_VY), m3, yn, e, n);
+          const float MVY = (owned && P.antidiffinter != 1) ? bil(N.f(V2C_NF_MVY), m3, yn, e, n) : 0.f;
+          if (backscatter) {
+            sm.q[Q_U][k] = uc; sm.q[Q_V][k] = vc;
+            sm.q[Q_PHIS][k] = PHIS; sm.q[Q_SXY][k] = SXY; sm.q[Q_EXY][k] = EXY;
+            sm.q[Q_ES][k] = ES; sm.q[Q_PR][k] = PR; sm.q[Q_SXX][k] = SXX;
+            sm.q[Q_EXX][k] = EXX; sm.q[Q_VX][k] = VX; sm.q[Q_VY][k] = VY;
+            sm.q[Q_MRO][k] = a.R(RK_RO, t);
+          }
+          if (!owned) continue;
+
+          // ------------------------------------- marker update (:943-1011)
+          const bool in_strict = (ix > 0 || u > 0.f) && (ix < g.ncx - 1 || u < 1.f) &&
+                                 (iy > 0 || v > 0.f) && (iy < g.ncy - 1 || v < 1.f);
+          const bool in_grid = (ix > 0 || u >= 0.f) && (ix < g.ncx - 1 || u <= 1.f) &&
+                               (iy > 0 || v >= 0.f) && (iy < g.ncy - 1 || v <= 1.f);
+          float tk = a.m.tk[idx];
+          float phi = a.m.phi[idx], mexx = a.m.exx[idx], mexy = a.m.exy[idx];
+          float msxx = a.m.sxx[idx], msxy = a.m.sxy[idx], mp = a.m.p[idx];
+          float mvx = a.m.vx[idx], mvy = a.m.vy[idx], me = a.m.e[idx];
+          bool changed = false;
+          if (a.do_n2m) {
+            if (in_strict && t < 50 && tk <= 0.f) {
+              if (P.antidiffinter == 1) {
+                msxx = SXX; msxy = SXY; mp = PR; mexx = EXX; mexy = EXY;
+                mvx = VX; mvy = VY; phi = PHIS; me = ES;
+              } else {
+                msxx = SXXE; msxy = SXYE; mp = SPPE; mexx = EXXE; mexy = EXYE;
+                mvx = MVX; mvy = MVY; phi = PHISE; me = ESE;
+              }
+              if (!P.tempmod) tk = (float)P.eps2;
+              changed = true;
+            }
+            if (in_grid && t < 50 && tk > 0.f) {
+              if (P.antidiffinter == 1) {
+                phi = PHIS; mexx = EXX; mexy = EXY; msxx = SXX; msxy = SXY;
+                mp = PR; mvx = VX; mvy = VY; me = ES;
+              } else {
+                phi += (PHIS - PHISE); mexx += (EXX - EXXE); mexy += (EXY - EXYE);
+                msxx += (SXX - SXXE); msxy += (SXY - SXYE); mp += (PR - SPPE);
+                mvx += (VX - MVX); mvy += (VY - MVY); me += (ES - ESE);
+              }
+              changed = true;
+            }
+          }
+
+          // ------------------------------------------ move and rotate
+          int nix = ix, niy = iy;
+          float nu_ = u, nv_ = v;
+          uint8_t flags = a.m.flags[idx];
+          if (a.do_move && !a.R(RK_IM, t) && (in_grid || P.outgrid != 1)) {
+            const float dt = a.S.dt;
+            Pos p0{ix, iy, u * wxc, v * wyc};
+            float vx0, vy0, sp0;
+            float vx1, vy1, sp1;
+            allinteri(g, N, p0, vx1, vy1, sp1);
+            if (P.markmod == 1) {
+              vx0 = vx1; vy0 = vy1; sp0 = sp1;
+            } else {
+              float vx2, vy2, sp2, vx3, vy3, sp3, vx4, vy4, sp4;
+              Pos p = p0;
+              p.X += vx1 * dt / 2.f; p.Y += vy1 * dt / 2.f;
+              settle(g, p, a.stat);
+              allinteri(g, N, p, vx2, vy2, sp2);
+              p = p0;
+              p.X += vx2 * dt / 2.f; p.Y += vy2 * dt / 2.f;
+              settle(g, p, a.stat);
+              allinteri(g, N, p, vx3, vy3, sp3);
+              p = p0;
+              p.X += vx3 * dt; p.Y += vy3 * dt;
+              settle(g, p, a.stat);
+              allinteri(g, N, p, vx4, vy4, sp4);
+              vx0 = (vx1 + 2.f * vx2 + 2.f * vx3 + vx4) / 6.f;
+              vy0 = (vy1 + 2.f * vy2 + 2.f * vy3 + vy4) / 6.f;
+              sp0 = (P.markmod == 2) ? (sp1 + 2.f * sp2 + 2.f * sp3 + sp4) / 6.f : sp1;
+            }
+            if (P.outgrid == 2) {
+              if ((ix == 0 && u < 0.f) || (ix == g.ncx - 1 && u > 1.f)) vy0 = 0.f;
+              if ((iy == 0 && v < 0.f) || (iy == g.ncy - 1 && v > 1.f)) vx0 = 0.f;
+            }
+            // new position: in offset space while the marker stays in its
+            // cell (one FP32 rounding of u), else walked in metres
+            float du = dt * vx0 / wxc, dv = dt * vy0 / wyc;
+            nu_ = u + du;
+            nv_ = v + dv;
+            nix = ix;
+            niy = iy;
+            const bool interior_x = ix > 0 && ix < g.ncx - 1, interior_y = iy > 0 && iy < g.ncy - 1;
+            if (!(nu_ >= 0.f && nu_ < 1.f && (interior_x || (u >= 0.f && u <= 1.f)))) {
+              Pos p{ix, 0, nu_ * wxc, 0.f};
+              settle(g, p, a.stat);
+              nix = p.ix;
+              const float nwx = __ldg(g.wx + nix);
+              nu_ = p.X / nwx;
+              if (p.X < nwx && nu_ >= 1.f) nu_ = nextafterf(1.f, 0.f);
+              if (p.X < 0.5f * nwx && nu_ >= 0.5f) nu_ = nextafterf(0.5f, 0.f);
+              if (p.X > 0.5f * nwx && nu_ <= 0.5f) nu_ = nextafterf(0.5f, 1.f);
+              if (p.X > nwx && nu_ <= 1.f) nu_ = nextafterf(1.f, 2.f);
+            }
+            if (!(nv_ >= 0.f && nv_ < 1.f && (interior_y || (v >= 0.f && v <= 1.f)))) {
+              Pos p{0, iy, 0.f, nv_ * wyc};
+              settle(g, p, a.stat);
+              niy = p.iy;
+              const float nwy = __ldg(g.wy + niy);
+              nv_ = p.Y / nwy;
+              if (p.Y < nwy && nv_ >= 1.f) nv_ = nextafterf(1.f, 0.f);
+              if (p.Y < 0.5f * nwy && nv_ >= 0.5f) nv_ = nextafterf(0.5f, 0.f);
+              if (p.Y > 0.5f * nwy && nv_ <= 0.5f) nv_ = nextafterf(0.5f, 1.f);
+              if (p.Y > nwy && nv_ <= 1.f) nv_ = nextafterf(1.f, 2.f);
+            }
+            (void)interior_x;
+            // stress rotation, moveandrotatemarkers.c:58-76
+            sp0 *= dt;
+            if (P.stoksmod == 1) {
+              float s, cth, s2, c2;
+              sincosf(sp0, &s, &cth);
+              sincosf(2.f * sp0, &s2, &c2);
+              float r1 = msxx * cth * cth - msxx * s * s + msxy * s2;
+              float r3 = 0.5f * (-msxx - msxx) * s2 + msxy * c2;
+              msxx = r1; msxy = r3;
+            } else if (P.stoksmod == 2) {
+              float r1 = msxx + msxy * 2.f * sp0;
+              float r3 = msxy + 0.5f * (-msxx - msxx) * 2.f * sp0;
+              msxx = r1; msxy = r3;
+            }
+            // markers coming from depth, out-of-grid reset (:79-87)
+            double ynew = g.gy[niy] + (double)nv_ * (g.gy[niy + 1] - g.gy[niy]);
+            if (ynew > P.zdeep && vy0 < 0.f && tk < (float)P.tdeep) tk = (float)P.tdeep;
+            const bool out = (nix == 0 && nu_ < 0.f) || (nix == g.ncx - 1 && nu_ > 1.f) ||
+                             (niy == 0 && nv_ < 0.f) || (niy == g.ncy - 1 && nv_ > 1.f);
+            if (out) {
+              tk = 0.f; me = 0.f; flags |= MFLAG_RESET;
+              atomicAdd(a.stat + ST_OUT_OF_GRID, 1ull);
+            }
+            changed = true;
+          }
+          a.m.cell_out[idx] = nix * ncy + niy;
+          a.m.u_out[idx] = nu_;
+          a.m.v_out[idx] = nv_;
+          if (changed) {
+            a.m.phi[idx] = phi; a.m.exx[idx] = mexx; a.m.exy[idx] = mexy;
+            a.m.sxx[idx] = msxx; a.m.sxy[idx] = msxy; a.m.p[idx] = mp;
+            a.m.vx[idx] = mvx; a.m.vy[idx] = mvy; a.m.e[idx] = me;
+            a.m.tk[idx] = tk; a.m.flags[idx] = flags;
+          }
+        }
+        if (!backscatter) continue;
+        __syncthreads();
+        if (!jvalid) continue;
+        // ---------------------------------------------- back-scatter
+        for (int s = max(lo_b, cs); s < min(lo_e, ce); ++s) {  // cell (ci, j-1)
+          const int q = s - cs;
+          const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
+          if (role == 0) {
+            if (!(v > 0.5f)) continue;
+            if (u < 0.5f) {
+              const float w = s1lo * (1.f - 2.f * u) * (2.f * v - 1.f);
+              ADD_BS(cur, q, w);
+            } else if (u > 0.5f) {
+              const float w = s1lo * (2.f * u - 1.f) * (2.f * v - 1.f);
+              ADD_BS(car, q, w);
+            }
+          } else if (role == 3) {
+            if (v > 0.5f) {
+              const float w = s1lo * (1.f - fabsf(u - 0.5f)) * v;
+              const float mro = sm.q[Q_MRO][q];
+              cur[0].add(sm.q[Q_VY][q] * mro * w); cur[1].add(mro * w); cur[2].add(w);
+            }
+          }
+        }
+        for (int s = max(up_b, cs); s < min(up_e, ce); ++s) {  // cell (ci, j)
+          const int q = s - cs;
+          const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
+          if (role == 0) {
+            if (!(v < 0.5f)) continue;
+            if (u < 0.5f) {
+              const float w = s1up * (1.f - 2.f * u) * (1.f - 2.f * v);
+              ADD_BS(cur, q, w);
+            } else if (u > 0.5f) {
+              const float w = s1up * (2.f * u - 1.f) * (1.f - 2.f * v);
+              ADD_BS(car, q, w);
+            }
+          } else if (role == 1) {
+            const float w = s1up * (1.f - 2.f * fabsf(u - 0.5f)) * (1.f - 2.f * fabsf(v - 0.5f));
+            cur[0].add(sm.q[Q_PR][q] * w); cur[1].add(sm.q[Q_SXX][q] * w);
+            cur[2].add(sm.q[Q_EXX][q] * w); cur[3].add(w);
+          } else if (role == 2) {
+            const float mro = sm.q[Q_MRO][q];
+            if (u < 0.5f) {
+              const float w = s1up * (1.f - u) * (1.f - fabsf(v - 0.5f));
+              cur[0].add(sm.q[Q_VX][q] * mro * w); cur[1].add(mro * w); cur[2].add(w);
+            } else if (u > 0.5f) {
+              const float w = s1up * u * (1.f - fabsf(v - 0.5f));
+              car[0].add(sm.q[Q_VX][q] * mro * w); car[1].add(mro * w); car[2].add(w);
+            }
+          } else {
+            if (v < 0.5f) {
+              const float w = s1up * (1.f - fabsf(u - 0.5f)) * (1.f - v);
+              const float mro = sm.q[Q_MRO][q];
+              cur[0].add(sm.q[Q_VY][q] * mro * w); cur[1].add(mro * w); cur[2].add(w);
+            }
+          }
+        }
+      }
+    }
+
+    // ----------------------------------------------- sums and normalisation
+    if (!backscatter || ci < i0 || !jvalid) continue;
+    const long m3 = (long)ci * yn + j;
+    if (role == 0) {
+      const float w = cur[4].value();
+      const float ph = cur[0].value(), sy = cur[1].value(), ey = cur[2].value(), es = cur[3].value();
+      N.f(V2C_NF_PHISUM)[m3] = ph; N.f(V2C_NF_SXYSUM)[m3] = sy;
+      N.f(V2C_NF_EXYSUM)[m3] = ey; N.f(V2C_NF_ESUM)[m3] = es; N.f(V2C_NF_WTPHISUM)[m3] = w;
+      if (w != 0.f && ci >= 1 && j >= 1 && ci < g.xn - 1 && j < g.yn - 1) {
+        N.f(V2C_NF_PHIE)[m3] = ph / w; N.f(V2C_NF_SXYEE)[m3] = sy / w;
+        N.f(V2C_NF_EXYEE)[m3] = ey / w; N.f(V2C_NF_PEE)[m3] = es / w;
+      }
+    } else if (role == 1) {
+      if (ci < g.ncx && j < ncy) {
+        const long mc = (long)(ci + 1) * yn + (j + 1);
+        const float w = cur[3].value();
+        const float ps = cur[0].value(), sx = cur[1].value(), ex = cur[2].value();
+        N.f(V2C_NF_PSUM)[mc] = ps; N.f(V2C_NF_SXXSUM)[mc] = sx;
+        N.f(V2C_NF_EXXSUM)[mc] = ex; N.f(V2C_NF_WTSXXSUM)[mc] = w;
+        if (w != 0.f) {
+          N.f(V2C_NF_SPPEE)[mc] = ps / w; N.f(V2C_NF_SXXEE)[mc] = sx / w;
+          N.f(V2C_NF_EXXEE)[mc] = ex / w;
+        }
+      }
+      if (ci == 0 || j == 0) {
+        N.f(V2C_NF_PSUM)[m3] = 0; N.f(V2C_NF_SXXSUM)[m3] = 0;
+        N.f(V2C_NF_EXXSUM)[m3] = 0; N.f(V2C_NF_WTSXXSUM)[m3] = 0;
+      }
+    } else if (role == 2) {
+      const float w = cur[2].value(), vs = cur[0].value(), mr = cur[1].value();
+      N.f(V2C_NF_VXSUM)[m3] = vs; N.f(V2C_NF_MRX0)[m3] = mr; N.f(V2C_NF_WTVXSUM)[m3] = w;
+      if (w != 0.f) N.f(V2C_NF_MVXE)[m3] = vs / mr;
+    } else {
+      const float w = cur[2].value(), vs = cur[0].value(), mr = cur[1].value();
+      N.f(V2C_NF_VYSUM)[m3] = vs; N.f(V2C_NF_MRY0)[m3] = mr; N.f(V2C_NF_WTVYSUM)[m3] = w;
+      if (w != 0.f) N.f(V2C_NF_MVYE)[m3] = vs / mr;
+    }
+  }
+}
+
+}  // namespace
+
+void launch_n2m_move(const N2MArgs &a, cudaStream_t st) {
+  dim3 grid((a.g.xn + a.TX - 1) / a.TX, (a.g.yn + TY - 1) / TY);
+  k_n2m_move<<<grid, NTH, 0, st>>>(a);
+}
+
+}  // namespace v2c

@@ -1,0 +1,272 @@
+// v2c_nodes.cu -- node loops of the step, one thread per node, FP32.
+//
+//  * interpolate_center2basic_old (interpolation.c:1575-1598)
+//  * compute_before_solve -> calc_vpvisc (plastic.c:2-56, calc_RSF.c:33-169)
+//  * compute_after_solve -> calc_sliprate_after_solve (plastic.c:61-129,
+//    calc_RSF.c:172-221), with a deterministic block-tree + fixed-order sum
+//    for the RMS misfit
+//  * the boundary corrections that end marker2nodes
+//    (momentum_continuity_addmatrix_checkerror.c:1002-1184,
+//    temperature_iterate.c:828-891): the reference solves them with its
+//    frontal Gauss routine; here each boundary row arrives pre-resolved on
+//    the host (v2c_set_bonds) as constant + references to unconstrained
+//    rows, which is the same linear solution.
+//
+// The rate-and-state expressions of calc_RSF.c multiply exp(+-(mu0+b phi)/a)
+// factors that reach e^+-160 for the host-rock state phi = 50; they are
+// evaluated here in log space, which is exact algebra and stays inside FP32
+// range.
+#include <math.h>
+
+#include "v2c_kernels.h"
+
+namespace v2c {
+
+namespace {
+
+inline unsigned nblk(long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// asinh(exp(w)) without forming exp(w)
+__device__ __forceinline__ float asinh_exp(float w) {
+  if (w > 20.f) return w + 0.693147180559945f + 0.25f * __expf(-2.f * w);
+  return asinhf(expf(w));
+}
+
+// log(sinh(s)), s > 0
+__device__ __forceinline__ float log_sinh(float s) {
+  if (s > 10.f) return s - 0.693147180559945f + log1pf(-expf(-2.f * s));
+  return logf(sinhf(s));
+}
+
+// ageing-law state after dt at slip rate V (calc_RSF.c:96-103)
+__device__ __forceinline__ float new_state(float ph, float V, float dt, float L, float V0) {
+  const float x = V * dt / L;
+  if (x <= 1e-6f) {
+    // log(e^ph (1 - x) + V0 dt / L)
+    return ph + log1pf(-x + V0 * dt / L * expf(-ph));
+  }
+  // log(V0/V + (e^ph - V0/V) e^-x) = log(A + B), A = V0/V (1 - e^-x), B = e^(ph-x)
+  const float la = logf(V0 / V) + logf(-expm1f(-x));
+  const float lb = ph - x;
+  const float hi = fmaxf(la, lb), lo = fminf(la, lb);
+  return hi + log1pf(expf(lo - hi));
+}
+
+__global__ void k_c2b_old(Grid g, Nodes N) {
+  long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (m3 >= g.nn) return;
+  const long yn = g.yn;
+  long m2 = m3 % yn, m1 = m3 / yn;
+  if (m1 >= 1 && m2 >= 1 && m1 < g.xn - 1 && m2 < g.yn - 1) {
+    const float *exxe = N.f(V2C_NF_EXXE), *sxxe = N.f(V2C_NF_SXXE), *sppe = N.f(V2C_NF_SPPE);
+    N.f(V2C_NF_EXXES)[m3] = 0.25f * (exxe[m3] + exxe[m3 + 1] + exxe[m3 + yn] + exxe[m3 + yn + 1]);
+    N.f(V2C_NF_SXXES)[m3] = 0.25f * (sxxe[m3] + sxxe[m3 + 1] + sxxe[m3 + yn] + sxxe[m3 + yn + 1]);
+    N.f(V2C_NF_SPPES)[m3] = 0.25f * (sppe[m3] + sppe[m3 + 1] + sppe[m3 + yn] + sppe[m3 + yn + 1]);
+  }
+}
+
+__global__ void k_before(Grid g, Nodes N, Scal S, float dt, int rk, unsigned long long *stat) {
+  long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (m3 >= g.nn) return;
+  const v2c_params &p = S.p;
+  long m2 = m3 % g.yn, m1 = m3 / g.yn;
+  if (!(m1 >= 1 && m2 >= 1 && m1 < g.xn - 1 && m2 < g.yn - 1)) return;
+  const float W = (float)p.faultwidth;
+  const float nP = (p.pmode == 0 || p.timesum == 0) ? (float)p.nstress : N.f(V2C_NF_SPPES)[m3];
+  const float sxxs = N.f(V2C_NF_SXXS)[m3], sxy = N.f(V2C_NF_SXY)[m3];
+  const float sigin = sqrtf(sxxs * sxxs + sxy * sxy);
+  float nu;
+  bool err = false;
+  if (sigin > 0.f || p.RSFmode == 0) {
+    // calc_vpvisc
+    float V = 0.f;
+    if (rk == 0) V = (p.RSFmode == 1 || p.timesum > 0) ? N.f(V2C_NF_RK_SLIPRS_FINAL)[m3] : 0.f;
+    if ((p.rkmod == 0 && rk > 0) || (rk > 0 && rk < 3)) V = N.f(V2C_NF_RK_SLIPRS_SOLVED)[m3];
+    N.f(V2C_NF_PES)[m3] = N.f(V2C_NF_PE)[m3] + V / W * dt;
+    float newstate = 0.f, syield;
+    if (p.RSFmode == 1) {
+      const float L = N.f(V2C_NF_LS)[m3], V0 = N.f(V2C_NF_V0S)[m3], ph = N.f(V2C_NF_PHIS)[m3];
+      newstate = new_state(ph, V, dt, L, V0);
+      const float rad = (p.inertyn == 0) ? 4.3303e+06f * V : 0.f;
+      const float a = N.f(V2C_NF_AS)[m3], b = N.f(V2C_NF_BS)[m3], mu = N.f(V2C_NF_MUS_S)[m3];
+      if (p.power_law_RSF > 0)
+        syield = expf(logf(nP * mu) + a / mu * logf(V / V0) + (newstate * b) / mu) + rad;
+      else
+        syield = nP * a * asinh_exp(logf(V / (2.f * V0)) + (mu + newstate * b) / a) + rad;
+    } else {
+      syield = nP * N.f(V2C_NF_MUS_S)[m3] + N.f(V2C_NF_COHESION)[m3];
+    }
+    const float nm = N.f(V2C_NF_NU_M2C)[m3];
+    float vp;
+    if (p.RSFmode == 1) vp = (syield > 0.f) ? nm * syield / (2.f * nm * V / W + syield) : nm;
+    else vp = nm * syield / (2.f * nm * V / W + syield);
+    N.f(V2C_NF_PHIS_IT)[m3] = newstate;
+    N.f(V2C_NF_SYIELDS)[m3] = syield;
+    N.f(V2C_NF_NUVP_IT)[m3] = vp;
+    N.f(V2C_NF_SLIPRS)[m3] = V;
+    if ((p.timesum > 0 && (isnan(newstate) || isnan(syield) || isnan(vp) || vp == 0.f || isnan(V))) ||
+        V < 0.f || syield < 0.f)
+      err = true;
+    nu = vp;
+  } else {
+    nu = N.f(V2C_NF_NU_M2C)[m3];
+  }
+  N.f(V2C_NF_NU)[m3] = nu;
+  if (isnan(nu) || nu <= 0.f) err = true;
+  if (err) atomicAdd(stat + ST_NAN, 1ull);
+}
+
+// per-block partial sums of (syield - sigin)^2 and counts
+constexpr int AB = 256;
+__global__ void k_after(Grid g, Nodes N, Scal S, float dt, float *part) {
+  __shared__ float sd[AB];
+  __shared__ float sc[AB];
+  long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  float d2 = 0.f, cnt = 0.f;
+  const v2c_params &p = S.p;
+  if (m3 < g.nn) {
+    long m2 = m3 % g.yn, m1 = m3 / g.yn;
+    if (m1 >= 1 && m2 >= 1 && m1 < g.xn - 1 && m2 < g.yn - 1) {
+      const float W = (float)p.faultwidth;
+      const float nps = (p.pmode == 0 || p.timesum == 0) ? (float)p.nstress : N.f(V2C_NF_SPPES)[m3];
+      const float sxxs = N.f(V2C_NF_SXXS)[m3], sxy = N.f(V2C_NF_SXY)[m3];
+      const float sigin = sqrtf(sxxs * sxxs + sxy * sxy);
+      const float a = N.f(V2C_NF_AS)[m3], b = N.f(V2C_NF_BS)[m3], mu = N.f(V2C_NF_MUS_S)[m3];
+      const float V0 = N.f(V2C_NF_V0S)[m3], L = N.f(V2C_NF_LS)[m3], ph = N.f(V2C_NF_PHIS_IT)[m3];
+      float V;
+      if (p.RSFmode == 1) {
+        if (sigin > 0.f) {
+          if (p.power_law_RSF > 0)
+            V = expf(logf(V0) + (mu / a) * logf(sigin / (nps * mu)) + (-ph * b) / a);
+          else
+            V = expf(logf(2.f * V0) + log_sinh(sigin / (a * nps)) - (mu + b * ph) / a);
+          const float ex = N.f(V2C_NF_EXXPL)[m3], ey = N.f(V2C_NF_EXY)[m3];
+          const float Vslip = sqrtf(ex * ex + ey * ey) * W;
+          V = (V <= Vslip) ? V : Vslip;
+          if (V < 1e-40f) V = 1e-40f;
+        } else {
+          V = 0.f;
+        }
+        N.f(V2C_NF_RK_PHIDTS_SOLVED)[m3] = V0 / L * expf(-ph) - V / L;
+      } else {
+        const float G = N.f(V2C_NF_GG)[m3], NUVP = N.f(V2C_NF_NU)[m3], NU = N.f(V2C_NF_NU_M2C)[m3];
+        const float E2EL = sigin / (NUVP / (G * dt + NUVP));
+        const float A = N.f(V2C_NF_SYIELDS)[m3] / E2EL;
+        if (A < 1.f) {
+          const float nup = G * dt * A / (1.f - A);
+          V = W * (sigin / 2.f * (1.f / nup - 1.f / NU));
+        } else {
+          V = 0.f;
+        }
+      }
+      N.f(V2C_NF_RK_SLIPRS_SOLVED)[m3] = V;
+      if (V > 0.f) {
+        const float d = N.f(V2C_NF_SYIELDS)[m3] - sigin;
+        N.f(V2C_NF_RK_DELTAS)[m3] = d;
+        d2 = d * d;
+        cnt = 1.f;
+      } else {
+        N.f(V2C_NF_RK_DELTAS)[m3] = 0.f;
+      }
+    }
+  }
+  sd[threadIdx.x] = d2;
+  sc[threadIdx.x] = cnt;
+  __syncthreads();
+  for (int off = AB / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) {
+      sd[threadIdx.x] += sd[threadIdx.x + off];
+      sc[threadIdx.x] += sc[threadIdx.x + off];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = sd[0];
+    part[2 * blockIdx.x + 1] = sc[0];
+  }
+}
+
+// fold the block partials in block order (single block, fixed order); the
+// few thousand partials are summed in FP64
+__global__ void k_after_fold(const float *part, long nb, double *out) {
+  __shared__ double sd[AB], sc[AB];
+  double d = 0, c = 0;
+  for (long i = threadIdx.x; i < nb; i += AB) {
+    d += part[2 * i];
+    c += part[2 * i + 1];
+  }
+  sd[threadIdx.x] = d;
+  sc[threadIdx.x] = c;
+  __syncthreads();
+  for (int off = AB / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) {
+      sd[threadIdx.x] += sd[threadIdx.x + off];
+      sc[threadIdx.x] += sc[threadIdx.x + off];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = sd[0];
+    out[1] = sc[0];
+  }
+}
+
+__global__ void k_bc(BcRows r, Nodes N, float *scratch) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= r.n) return;
+  float v = r.c[i];
+  for (int k = 0; k < r.nref[i]; k++) {
+    const int q = i * V2C_BC_MAXREF + k;
+    v = v - N.f(r.rfield[q])[r.rnode[q]] * (-r.rcoef[q]);
+  }
+  scratch[i] = v;
+}
+__global__ void k_bc_store(BcRows r, Nodes N, const float *scratch) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < r.n) N.f(r.field[i])[r.node[i]] = scratch[i];
+}
+
+__global__ void k_to_f32(const double *src, float *dst, long n) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (float)src[i];
+}
+__global__ void k_to_f64(const float *src, double *dst, long n) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (double)src[i];
+}
+
+}  // namespace
+
+void launch_c2b_old(const Grid &g, const Nodes &N, cudaStream_t st) {
+  k_c2b_old<<<nblk(g.nn, 256), 256, 0, st>>>(g, N);
+}
+
+void launch_before_solve(const Grid &g, const Nodes &N, const Scal &S, double dt, int rk,
+                         unsigned long long *stat, cudaStream_t st) {
+  k_before<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, S, (float)dt, rk, stat);
+}
+
+void launch_after_solve(const Grid &g, const Nodes &N, const Scal &S, double dt, int rk,
+                        double *red, cudaStream_t st) {
+  (void)rk;
+  long nb = (g.nn + AB - 1) / AB;
+  float *part = (float *)(red + 2);
+  k_after<<<(unsigned)nb, AB, 0, st>>>(g, N, S, (float)dt, part);
+  k_after_fold<<<1, AB, 0, st>>>(part, nb, red);
+}
+
+void launch_bc(const BcRows &rows, const Nodes &N, float *scratch, cudaStream_t st) {
+  if (rows.n <= 0) return;
+  // all rows read first, then stored: a row never sees another's new value
+  k_bc<<<nblk(rows.n, 256), 256, 0, st>>>(rows, N, scratch);
+  k_bc_store<<<nblk(rows.n, 256), 256, 0, st>>>(rows, N, scratch);
+}
+
+void launch_node_to_f32(const double *src, float *dst, long n, cudaStream_t st) {
+  if (n > 0) k_to_f32<<<nblk(n, 256), 256, 0, st>>>(src, dst, n);
+}
+void launch_node_to_f64(const float *src, double *dst, long n, cudaStream_t st) {
+  if (n > 0) k_to_f64<<<nblk(n, 256), 256, 0, st>>>(src, dst, n);
+}
+
+}  // namespace v2c

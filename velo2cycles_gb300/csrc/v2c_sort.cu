@@ -1,0 +1,209 @@
+// v2c_sort.cu -- cell assignment and the counting sort by cell.
+//
+// Cell assignment (upload) bisects the FP64 grid lines exactly like
+// nxsearch/nysearch (interpolation.c:1536-1573), so the integer cell of
+// every marker is bit-identical to the reference's.  The counting sort is
+// stable by array index: counts by integer atomics (order-independent),
+// exclusive scan, scatter into per-cell slots, then each cell's slots are
+// ranked by array index, which fixes the order whatever order the atomics
+// handed the slots out in.
+#include <climits>
+
+#include "v2c_kernels.h"
+
+namespace v2c {
+
+namespace {
+
+__global__ void k_assign(Grid g, const double *x, const double *y, long n, Markers m) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double xi = x[i], yi = y[i];
+  int ix = nsearch64(g.gx, g.xn, xi), iy = nsearch64(g.gy, g.yn, yi);
+  double u = (xi - g.gx[ix]) / (g.gx[ix + 1] - g.gx[ix]);
+  double v = (yi - g.gy[iy]) / (g.gy[iy + 1] - g.gy[iy]);
+  m.cell_in[i] = ix * g.ncy + iy;
+  m.u_in[i] = offset32(u);
+  m.v_in[i] = offset32(v);
+  m.id[i] = (int32_t)i;
+}
+
+__global__ void k_count(const int32_t *cell, long n, int32_t *counts, int32_t *slot) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) slot[i] = atomicAdd(counts + cell[i], 1);
+}
+
+// exclusive scan, three passes: per-block scan of 4 elements per thread
+constexpr int SB = 1024, SE = 4;
+__global__ void k_scan_block(const int32_t *in, long m, int32_t *out, int32_t *bsum) {
+  __shared__ int32_t sh[SB];
+  long base = (long)blockIdx.x * SB * SE + (long)threadIdx.x * SE;
+  int32_t v[SE], s = 0;
+#pragma unroll
+  for (int k = 0; k < SE; k++) {
+    v[k] = (base + k < m) ? in[base + k] : 0;
+    s += v[k];
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int off = 1; off < SB; off <<= 1) {
+    int32_t t = (threadIdx.x >= off) ? sh[threadIdx.x - off] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += t;
+    __syncthreads();
+  }
+  int32_t run = sh[threadIdx.x] - s;
+#pragma unroll
+  for (int k = 0; k < SE; k++) {
+    if (base + k < m) out[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == SB - 1) bsum[blockIdx.x] = sh[SB - 1];
+}
+
+__global__ void k_scan_sums(int32_t *bsum, long nb, int32_t *total_out) {
+  // single block, sequential chunks of SB
+  __shared__ int32_t sh[SB];
+  __shared__ int32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (long c0 = 0; c0 < nb; c0 += SB) {
+    long i = c0 + threadIdx.x;
+    int32_t v = (i < nb) ? bsum[i] : 0;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < SB; off <<= 1) {
+      int32_t t = (threadIdx.x >= off) ? sh[threadIdx.x - off] : 0;
+      __syncthreads();
+      sh[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < nb) bsum[i] = carry + sh[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += sh[SB - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total_out = carry;
+}
+
+__global__ void k_scan_add(int32_t *out, long m, const int32_t *bsum) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < m) out[i] += bsum[i / (SB * SE)];
+}
+
+__global__ void k_slots(const int32_t *cell, long n, const int32_t *start, const int32_t *slot,
+                        int32_t *tmp) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) tmp[start[cell[i]] + slot[i]] = (int32_t)i;
+}
+
+// one warp per cell: rank each entry among the cell's entries (all distinct)
+__global__ void k_rank(const int32_t *start, long ncell, const int32_t *tmp, int32_t *perm,
+                       unsigned long long *stat) {
+  long c = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (c >= ncell) return;
+  int s = start[c], L = start[c + 1] - s;
+  if (lane == 0 && L > 0) atomicMax(stat + ST_MAX_CELL, (unsigned long long)L);
+  if (L == 1) {
+    if (lane == 0) perm[s] = tmp[s];
+    return;
+  }
+  for (int b = 0; b < L; b += 32) {
+    int jj = b + lane;
+    int val = (jj < L) ? tmp[s + jj] : INT_MAX;
+    int rank = 0;
+    for (int b2 = 0; b2 < L; b2 += 32) {
+      int other = (b2 + lane < L) ? tmp[s + b2 + lane] : INT_MAX;
+#pragma unroll 8
+      for (int k = 0; k < 32; k++) rank += (__shfl_sync(V2C_FULL, other, k) < val);
+    }
+    if (jj < L) perm[s + rank] = val;
+  }
+}
+
+__global__ void k_f64_to_f32(const double *src, float *dst, long n) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (float)src[i];
+}
+template <class T>
+__global__ void k_gather(const T *src, const int32_t *perm, T *dst, long n) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[perm[i]];
+}
+__global__ void k_unperm_f32(const float *src, const int32_t *id, double *out, long n) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) out[id[i]] = (double)src[i];
+}
+template <class T>
+__global__ void k_unperm(const T *src, const int32_t *id, T *out, long n) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) out[id[i]] = src[i];
+}
+__global__ void k_positions(Grid g, Markers m, long n, double *x, double *y) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c = m.cell_in[i];
+  int ix = c / g.ncy, iy = c - ix * g.ncy;
+  int k = m.id[i];
+  x[k] = g.gx[ix] + (double)m.u_in[i] * (g.gx[ix + 1] - g.gx[ix]);
+  y[k] = g.gy[iy] + (double)m.v_in[i] * (g.gy[iy + 1] - g.gy[iy]);
+}
+
+inline unsigned nblk(long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+void launch_assign(const Grid &g, const double *x, const double *y, long n, Markers m,
+                   unsigned long long *stat, cudaStream_t st) {
+  (void)stat;
+  if (n > 0) k_assign<<<nblk(n, 256), 256, 0, st>>>(g, x, y, n, m);
+}
+
+void launch_sort(const int32_t *cell, long n, long ncell, SortBufs &b,
+                 unsigned long long *stat, cudaStream_t st) {
+  cudaMemsetAsync(b.counts, 0, sizeof(int32_t) * ncell, st);
+  if (n > 0) k_count<<<nblk(n, 256), 256, 0, st>>>(cell, n, b.counts, b.slot);
+  long nb = (ncell + SB * SE - 1) / (SB * SE);
+  k_scan_block<<<(unsigned)nb, SB, 0, st>>>(b.counts, ncell, b.start, b.blocksum);
+  k_scan_sums<<<1, SB, 0, st>>>(b.blocksum, nb, b.start + ncell);
+  k_scan_add<<<nblk(ncell, 256), 256, 0, st>>>(b.start, ncell, b.blocksum);
+  if (n > 0) {
+    k_slots<<<nblk(n, 256), 256, 0, st>>>(cell, n, b.start, b.slot, b.tmp);
+    k_rank<<<nblk(ncell * 32, 256), 256, 0, st>>>(b.start, ncell, b.tmp, b.perm, stat);
+  }
+}
+
+void launch_f64_to_f32(const double *src, float *dst, long n, cudaStream_t st) {
+  if (n > 0) k_f64_to_f32<<<nblk(n, 256), 256, 0, st>>>(src, dst, n);
+}
+void launch_gather_f32(const float *src, const int32_t *perm, float *dst, long n, cudaStream_t st) {
+  if (n > 0) k_gather<float><<<nblk(n, 256), 256, 0, st>>>(src, perm, dst, n);
+}
+void launch_gather_i32(const int32_t *src, const int32_t *perm, int32_t *dst, long n, cudaStream_t st) {
+  if (n > 0) k_gather<int32_t><<<nblk(n, 256), 256, 0, st>>>(src, perm, dst, n);
+}
+void launch_gather_i8(const int8_t *src, const int32_t *perm, int8_t *dst, long n, cudaStream_t st) {
+  if (n > 0) k_gather<int8_t><<<nblk(n, 256), 256, 0, st>>>(src, perm, dst, n);
+}
+void launch_gather_u8(const uint8_t *src, const int32_t *perm, uint8_t *dst, long n, cudaStream_t st) {
+  if (n > 0) k_gather<uint8_t><<<nblk(n, 256), 256, 0, st>>>(src, perm, dst, n);
+}
+void launch_unpermute_f32(const float *src, const int32_t *id, double *out, long n, cudaStream_t st) {
+  if (n > 0) k_unperm_f32<<<nblk(n, 256), 256, 0, st>>>(src, id, out, n);
+}
+void launch_unpermute_i32(const int32_t *src, const int32_t *id, int32_t *out, long n, cudaStream_t st) {
+  if (n > 0) k_unperm<int32_t><<<nblk(n, 256), 256, 0, st>>>(src, id, out, n);
+}
+void launch_unpermute_u8(const uint8_t *src, const int32_t *id, uint8_t *out, long n, cudaStream_t st) {
+  if (n > 0) k_unperm<uint8_t><<<nblk(n, 256), 256, 0, st>>>(src, id, out, n);
+}
+void launch_unpermute_i8(const int8_t *src, const int32_t *id, int8_t *out, long n, cudaStream_t st) {
+  if (n > 0) k_unperm<int8_t><<<nblk(n, 256), 256, 0, st>>>(src, id, out, n);
+}
+void launch_positions(const Grid &g, const Markers &m, long n, double *x, double *y,
+                      cudaStream_t st) {
+  if (n > 0) k_positions<<<nblk(n, 256), 256, 0, st>>>(g, m, n, x, y);
+}
+
+}  // namespace v2c

@@ -277,11 +277,23 @@ def _bonds(xn: int, yn: int, pinit: float = 10.0e6):
 
 
 def make_case(name: str = "small", seed: int = 0, n_markers: int | None = None,
-              random_fields: bool | None = None, **param_overrides) -> Case:
+              random_fields: bool | None = None, window: tuple | None = None,
+              **param_overrides) -> Case:
     """Build a seeded synthetic state.  `random_fields` switches the marker
-    stress/strain rate to the c2 distributions (default: only for c2)."""
+    stress/strain rate to the c2 distributions (default: only for c2).
+    `window` = (i0, j0, nx, ny) cuts nx x ny grid lines starting at line
+    (i0, j0) out of the configuration: same spacing, materials and fields,
+    coordinates shifted so the window starts at 0 (a bounded sample of a
+    large configuration)."""
     rng = np.random.default_rng(seed)
     gx, gy, mx, my = grid_for(name)
+    XS, YS = float(gx[-1]), float(gy[-1])  # full model, for the physics
+    ox = oy = 0.0
+    if window is not None:
+        i0, j0, nxw, nyw = window
+        ox, oy = float(gx[i0]), float(gy[j0])
+        gx = gx[i0:i0 + nxw] - ox
+        gy = gy[j0:j0 + nyw] - oy
     xn, yn = gx.size, gy.size
     xs, ys = float(gx[-1]), float(gy[-1])
     nn = xn * yn
@@ -306,12 +318,12 @@ def make_case(name: str = "small", seed: int = 0, n_markers: int | None = None,
     fy = (sj + rng.random(n)) / my
     x = gx[ci] + fx * (gx[ci + 1] - gx[ci])
     y = gy[cj] + fy * (gy[cj + 1] - gy[cj])
-    t = _rock_type(x, y, xs)
+    t = _rock_type(x + ox, y + oy, XS)
 
     marks = {}
     marks[abi.MF_X], marks[abi.MF_Y] = x, y
-    marks[abi.MF_K] = _temperature(y, ys) + rng.normal(0, 5.0, n)
-    mvx, mvy, mexx, mexy, _ = _stream(x, y, xs, ys)
+    marks[abi.MF_K] = _temperature(y + oy, YS) + rng.normal(0, 5.0, n)
+    mvx, mvy, mexx, mexy, _ = _stream(x + ox, y + oy, XS, YS)
     if random_fields:
         marks[abi.MF_XX] = rng.normal(0.0, 5e6, n)
         marks[abi.MF_XY] = rng.normal(0.0, 5e6, n)
@@ -325,12 +337,12 @@ def make_case(name: str = "small", seed: int = 0, n_markers: int | None = None,
         marks[abi.MF_EXY] = mexy * (1 + 0.05 * rng.normal(size=n))
         marks[abi.MF_XX] = 2 * eta * marks[abi.MF_EXX] + rng.normal(0, 1e5, n)
         marks[abi.MF_XY] = 2 * eta * marks[abi.MF_EXY] + rng.normal(0, 1e5, n)
-    marks[abi.MF_P] = 3000.0 * 9.81 * y + rng.normal(0, 1e5, n)
+    marks[abi.MF_P] = 3000.0 * 9.81 * (y + oy) + rng.normal(0, 1e5, n)
     marks[abi.MF_E] = np.abs(rng.normal(0, 0.01, n))
     marks[abi.MF_VX] = mvx * (1 + 0.01 * rng.normal(size=n))
     marks[abi.MF_VY] = mvy * (1 + 0.01 * rng.normal(size=n))
     marks[abi.MF_C] = np.zeros(n)
-    r = np.abs(y - 10e3)
+    r = np.abs(y + oy - 10e3)
     marks[abi.MF_PHI] = np.where(r <= 250.0, 8.0, 10.0) + 0.1 * rng.normal(size=n)
     marks[abi.MF_SLIPV] = 10.0 ** rng.uniform(-12, -8, n)
     for f in (abi.MF_D, abi.MF_W, abi.MF_V, abi.MF_C0, abi.MF_FRIC_STATIC,
@@ -353,10 +365,10 @@ def make_case(name: str = "small", seed: int = 0, n_markers: int | None = None,
     def smooth(shape_scale, base):
         return base * (1 + shape_scale * rng.normal(size=nn))
 
-    vx_, _, _, _, _ = _stream(xvx, yvx, xs, ys)
-    _, vy_, _, _, _ = _stream(xvy, yvy, xs, ys)
-    _, _, exx_c, _, _ = _stream(xc, yc, xs, ys)
-    _, _, _, exy_b, esp_b = _stream(xb, yb, xs, ys)
+    vx_, _, _, _, _ = _stream(xvx + ox, yvx + oy, XS, YS)
+    _, vy_, _, _, _ = _stream(xvy + ox, yvy + oy, XS, YS)
+    _, _, exx_c, _, _ = _stream(xc + ox, yc + oy, XS, YS)
+    _, _, _, exy_b, esp_b = _stream(xb + ox, yb + oy, XS, YS)
     nodes[abi.NF_VX] = vx_
     nodes[abi.NF_VY] = vy_
     nodes[abi.NF_MVX] = vx_ * (1 + 1e-3 * rng.normal(size=nn))
@@ -378,11 +390,11 @@ def make_case(name: str = "small", seed: int = 0, n_markers: int | None = None,
     nodes[abi.NF_SXYE] = nodes[abi.NF_SXY] * (1 + 1e-2 * rng.normal(size=nn))
     nodes[abi.NF_SXYEE] = nodes[abi.NF_SXY] * (1 + 1e-2 * rng.normal(size=nn))
     nodes[abi.NF_SXXS] = nodes[abi.NF_SXX] * (1 + 1e-2 * rng.normal(size=nn))
-    nodes[abi.NF_PR] = 3000.0 * 9.81 * yc + 10e6 + rng.normal(0, 1e4, nn)
+    nodes[abi.NF_PR] = 3000.0 * 9.81 * (yc + oy) + 10e6 + rng.normal(0, 1e4, nn)
     nodes[abi.NF_SPPE] = nodes[abi.NF_PR] * (1 + 1e-4 * rng.normal(size=nn))
     nodes[abi.NF_SPPEE] = nodes[abi.NF_PR] * (1 + 1e-4 * rng.normal(size=nn))
     nodes[abi.NF_SPPES] = nodes[abi.NF_PR] * (1 + 1e-4 * rng.normal(size=nn))
-    ph = np.where(np.abs(yb - 10e3) <= 100.0, 8.0, 50.0)
+    ph = np.where(np.abs(yb + oy - 10e3) <= 100.0, 8.0, 50.0)
     nodes[abi.NF_PHIS] = ph + 0.05 * rng.normal(size=nn)
     nodes[abi.NF_PHIS_IT] = ph + 0.05 * rng.normal(size=nn)
     nodes[abi.NF_PHIE] = ph + 0.05 * rng.normal(size=nn)
@@ -397,6 +409,6 @@ def make_case(name: str = "small", seed: int = 0, n_markers: int | None = None,
     nodes[abi.NF_NU_M2C] = 10.0 ** rng.uniform(20, 23, nn)
     nodes[abi.NF_NU] = nodes[abi.NF_NU_M2C].copy()
     nodes[abi.NF_GG] = np.full(nn, 3.0e10)
-    nodes[abi.NF_TK] = _temperature(yb, ys)
+    nodes[abi.NF_TK] = _temperature(yb + oy, YS)
     bondm, bondn, bondv = _bonds(xn, yn)
     return Case(name, p, gx, gy, rt, nodes, marks, t, bondm, bondn, bondv)
