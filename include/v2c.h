@@ -244,7 +244,8 @@ enum {
   V2C_PROF_AFTER,       /* compute_after_solve                         */
   V2C_PROF_N2M_MOVE,    /* nodes2markers + move sweep                  */
   V2C_PROF_SORT,        /* counting sort by cell                       */
-  V2C_PROF_NEWTON,      /* per-marker Newton (with the network guess)  */
+  V2C_PROF_NEWTON,      /* marker physics with the per-marker Newton    */
+  V2C_PROF_PHYS,        /* marker physics without the Newton            */
   V2C_PROF_N
 };
 int v2c_set_profiling(v2c_ctx *ctx, int on);
@@ -291,6 +292,14 @@ int v2c_mlp_save(v2c_ctx *ctx, float *params_host);
 int v2c_mlp_train(v2c_ctx *ctx, const double *states_dev,
                   const double *targets_dev, long n, int epochs, int batch,
                   float lr, uint64_t seed, float *final_loss);
+/* Gradient of the training loss at the loaded parameters on n <= 131072
+ * states, without updating: grad_host[V2C_MLP_NPARAM - 20] (the trainable
+ * parameters, packed as above) and the loss.  For checking the backward
+ * pass against an independent implementation. */
+int v2c_mlp_grad(v2c_ctx *ctx, const double *states_dev,
+                 const double *targets_dev, long n, float *grad_host, float *loss);
+/* Network outputs for n states (device): out_dev[2][n] = (log V, phi). */
+int v2c_mlp_infer(v2c_ctx *ctx, const double *states_dev, long n, float *out_dev);
 
 #ifdef __cplusplus
 }

@@ -1334,8 +1334,11 @@ double v2c_oracle_rsf_residual(const double *st, double W, double V, double *phi
 }
 
 /* safeguarded Newton in u = log V on the bracket [log 1e-40, log(Ts/klin)],
- * bisecting whenever the Newton step leaves the bracket.  Counts residual
- * evaluations as iterations. */
+ * bisecting whenever the Newton step leaves the bracket.  A step below the
+ * floor before F(floor) < 0 is known evaluates at the floor instead; F >= 0
+ * there means the stress cannot drive slip above the floor and the solution
+ * is the floor itself (the reference clamps slip rates at 1e-40,
+ * calc_RSF.c:196).  Counts residual evaluations as iterations. */
 int v2c_oracle_rsf_newton1(const double *st, double W, double u0, double rtol,
                            int maxit, double *V, double *phi, double *tau,
                            double *res) {
@@ -1353,12 +1356,18 @@ int v2c_oracle_rsf_newton1(const double *st, double W, double u0, double rtol,
   if (!(u > ulo)) u = ulo + 0.5 * (uhi - ulo) * 1e-3;
   if (!(u < uhi)) u = uhi - (uhi - ulo) * 1e-3;
   double dF, rel = 1, F;
+  const double floor_u = ulo;
+  int lo_known = 0; /* F(ulo) < 0 established */
   for (int it = 1; it <= maxit; it++) {
     F = rsf_eval(&q, u, &dF, &rel, phi, tau);
     if (rel <= rtol) { *V = exp(u); *res = rel; return it; }
-    if (F < 0) ulo = u; else uhi = u;
+    if (u == floor_u && F >= 0) { /* root below the 1e-40 floor (calc_RSF.c:196) */
+      *V = 1e-40; *res = 0; return it;
+    }
+    if (F < 0) { ulo = u; lo_known = 1; } else uhi = u;
     double un = u - F / dF;
-    if (!(dF > 0) || !(un > ulo) || !(un < uhi)) un = 0.5 * (ulo + uhi);
+    if (!lo_known && dF > 0 && !(un > ulo)) un = floor_u; /* test the floor first */
+    else if (!(dF > 0) || !(un > ulo) || !(un < uhi)) un = 0.5 * (ulo + uhi);
     u = un;
   }
   *V = exp(u);

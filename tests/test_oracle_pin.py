@@ -1,0 +1,95 @@
+"""Pinning the oracle restatement to the reference (CPU).
+
+The reference has no tests or stored answers, so the restatement
+(oracle/v2c_oracle.c) is pinned against the reference's own routines:
+  * compiled from its sources here (oracle/build_ref.sh -> oracle/_ref),
+    on seeded states and flag variants, all six stages of the MIC step,
+    bit-exact in FP64 (both built with -ffp-contract=off);
+  * the committed fixtures tests/golden/ref_micro.npz (reference outputs
+    made by tests/golden/make_golden.py), also bit-exact, which works where
+    the reference sources are absent.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import bindings as B
+from velo2cycles_gb300 import abi, synth
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ref_micro.npz")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    oracle.build()
+
+
+def _compare(r, nodes_ref, marks_ref):
+    bad = [abi.node_field_names()[k] for k in range(abi.NF_N)
+           if not np.array_equal(r.nodes[k], nodes_ref[k], equal_nan=True)]
+    bad += ["marker " + abi.marker_field_names()[k] for k in range(abi.MF_N)
+            if k != abi.MF_SLIPV and not np.array_equal(r.marks[k], marks_ref[k], equal_nan=True)]
+    return bad
+
+
+@pytest.mark.parametrize("name", ["default", "variant"])
+def test_restatement_matches_golden(name):
+    z = np.load(GOLDEN)
+    p = abi.Params.from_buffer_copy(z[f"{name}/params"].tobytes()).to_dict()
+    nodes = {k: z[f"{name}/nodes_in"][k].copy() for k in range(abi.NF_N)}
+    marks = {k: z[f"{name}/marks_in"][k].copy() for k in range(abi.MF_N)}
+    c = synth.Case(name, p, z[f"{name}/gx"], z[f"{name}/gy"], z[f"{name}/rt"], nodes, marks,
+                   z[f"{name}/markt"].copy(), z[f"{name}/bondm"], z[f"{name}/bondn"],
+                   z[f"{name}/bondv"])
+    r = oracle.Restatement(c, phantom=True)
+    assert r.step() == 0
+    bad = _compare(r, z[f"{name}/nodes_out"], z[f"{name}/marks_out"])
+    assert not bad, bad
+
+
+needs_ref = pytest.mark.skipif(not (B.reference_available() or os.path.isdir("/root/reference")),
+                               reason="reference routines not built")
+
+
+@needs_ref
+@pytest.mark.parametrize("variant", [
+    {}, dict(interpolationmod=1), dict(markmod=1), dict(markmod=0, stoksmod=2),
+    dict(antidiffinter=0), dict(timesum=0.0), dict(tempmod=0), dict(Dphis=1.0), dict(pmode=1),
+    dict(timesum=1e8, timestep=1e8), dict(densimod=1, timesum=1e9), dict(power_law_RSF=1),
+    dict(RSFmode=0)])
+def test_restatement_bit_exact_vs_reference(variant):
+    c = synth.make_case("small", 5, **variant)
+    x, y = c.marks[abi.MF_X], c.marks[abi.MF_Y]
+    # markers outside the model, on grid lines and on cell midlines
+    x[:5] = -1.0
+    x[5:10] = c.gx[-1] + 3.0
+    y[10:15] = c.gy[3]
+    x[15:20] = c.gx[7]
+    x[20:25] = 0.5 * (c.gx[4] + c.gx[5])
+    c.markt[30:40] = 1  # sticky-air type
+    c.rt[:, 1] = c.rt[:, 2]
+    ref = B.run_reference(c, nthreads=1)
+    r = oracle.Restatement(c.copy(), phantom=True)
+    r.step()
+    bad = _compare(r, ref["nodes"], ref["marks"])
+    assert not bad, bad
+
+
+@needs_ref
+def test_restatement_bit_exact_nonuniform_grid():
+    c = synth.make_case("c2", 2, n_markers=200000)
+    ref = B.run_reference(c, nthreads=1)
+    r = oracle.Restatement(c.copy(), phantom=True)
+    r.step()
+    assert not _compare(r, ref["nodes"], ref["marks"])
+
+
+def test_nxsearch_ties_and_clamps():
+    g = np.array([0.0, 1.0, 2.0, 4.0, 8.0])
+    assert B.nxsearch(g, 2.0) == 2          # on a line: ties go left of the upper limit
+    assert B.nxsearch(g, -5.0) == 0         # below the grid
+    assert B.nxsearch(g, 8.0) == 3          # last line clamps to n-2
+    assert B.nxsearch(g, 100.0) == 3
+    assert B.nxsearch(g, 3.999) == 2

@@ -172,10 +172,11 @@ int check_params(const v2c_params *p) {
 }
 
 int pick_tx(const v2c_ctx *c) {
-  // enough CTAs for two waves over 152 SMs; halo overhead is one column
+  // widest column strip that still gives 1.5 waves of 6 resident CTAs on
+  // each of the 152 SMs; a strip of tx columns restages one halo column
   long rows = (c->yn + 31) / 32;
   int tx = 32;
-  while (tx > 4 && rows * ((c->xn + tx - 1) / tx) < 2 * 152) tx /= 2;
+  while (tx > 4 && rows * ((c->xn + tx - 1) / tx) < 152 * 6 * 3 / 2) tx /= 2;
   return tx;
 }
 
@@ -231,7 +232,7 @@ extern "C" int v2c_create(const v2c_params *p, long max_markers, void *cuda_stre
   AM(v_in, float) AM(v_out, float) AM(id, int32_t) AM(type, int8_t) AM(flags, uint8_t)
   AM(tk, float) AM(e, float) AM(p, float) AM(sxx, float) AM(sxy, float) AM(exx, float)
   AM(exy, float) AM(vx, float) AM(vy, float) AM(phi, float) AM(coh, float) AM(slipv, float)
-  AM(mnu, float)
+  AM(mnu, float) AM(mkt, float) AM(mro, float)
 #undef AM
   ctx->n_marker_mem = k;
   // sort
@@ -519,6 +520,8 @@ extern "C" int v2c_upload_markers(v2c_ctx *ctx, const double *const *fields,
     }
   }
   CK(cudaMemsetAsync(m.mnu, 0, sizeof(float) * n, st));
+  CK(cudaMemsetAsync(m.mkt, 0, sizeof(float) * n, st));
+  CK(cudaMemsetAsync(m.mro, 0, sizeof(float) * n, st));
   // sort once and store the markers physically in cell order
   launch_sort(m.cell_in, n, ctx->ncell, ctx->sb, ctx->d_stat, st);
   const int32_t *perm = ctx->sb.perm;
@@ -662,6 +665,15 @@ extern "C" int v2c_marker2nodes(v2c_ctx *ctx) {
   a.gyf = ctx->d_gyf;
   a.TX = pick_tx(ctx);
   CK(cudaMemsetAsync(ctx->d_sticky, 0, sizeof(uint32_t) * ctx->nn, st));
+  {
+    PhysArgs ph;
+    ph.g = a.g; ph.N = a.N; ph.m = a.m; ph.R = a.R; ph.S = a.S; ph.n = ctx->n;
+    ph.sticky_key = ctx->d_sticky; ph.stat = ctx->d_stat; ph.gxf = ctx->d_gxf; ph.gyf = ctx->d_gyf;
+    ph.mlp = ctx->nw.have_mlp ? ctx->nw.d_mlp : nullptr;
+    Prof pr(ctx, ctx->p.newton_guess == V2C_GUESS_OFF ? V2C_PROF_PHYS : V2C_PROF_NEWTON);
+    launch_phys(ph, st);
+    ctx->launches += 1;
+  }
   {
     Prof pr(ctx, V2C_PROF_M2N);
     launch_m2n(a, st);

@@ -48,7 +48,8 @@ struct Markers {
   int32_t *id;
   int8_t *type;
   uint8_t *flags;  // bit0: out-of-grid reset (markd = markw = -1)
-  float *tk, *e, *p, *sxx, *sxy, *exx, *exy, *vx, *vy, *phi, *coh, *slipv, *mnu;
+  float *tk, *e, *p, *sxx, *sxy, *exx, *exy, *vx, *vy, *phi, *coh, *slipv;
+  float *mnu, *mkt, *mro;  // per-step results of the marker physics kernel
 };
 enum { MFLAG_RESET = 1 };
 

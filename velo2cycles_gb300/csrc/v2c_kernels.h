@@ -35,6 +35,21 @@ struct M2NArgs {
   int TX;
 };
 void launch_m2n(const M2NArgs &a, cudaStream_t st);
+
+// per-marker physics (+ optional RSF Newton), marker array order
+struct PhysArgs {
+  Grid g;
+  Nodes N;
+  Markers m;
+  Rock R;
+  Scal S;
+  long n;
+  uint32_t *sticky_key;
+  unsigned long long *stat;
+  const float *gxf, *gyf;
+  const float *mlp;  // packed network (device) or null
+};
+void launch_phys(const PhysArgs &a, cudaStream_t st);
 void launch_sticky(const Nodes &N, const uint32_t *key, long nn, cudaStream_t st);
 void launch_dphis(const Grid &g, const Nodes &N, cudaStream_t st);
 

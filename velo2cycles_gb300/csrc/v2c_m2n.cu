@@ -17,6 +17,8 @@
 //   * vy node (ci, j) gets cell (ci, j-1) if v > 0.5 and cell (ci, j) if
 //     v < 0.5;
 //   * the centre node (ci+1, j+1) gets cell (ci, j) only.
+// The per-marker physics ran before, in marker order (v2c_phys.cu); staging
+// only reads the marker fields and those results.
 // Each node is summed by exactly one thread, in sorted-marker order, with
 // FP32 two-sum compensation; the node tail (normalisation, antidiffusion
 // correction, interpolation.c:714-824) runs in the same thread on the
@@ -28,7 +30,7 @@
 #include <math.h>
 
 #include "v2c_kernels.h"
-#include "v2c_rheology.cuh"
+#include "v2c_internal.cuh"
 
 namespace v2c {
 
@@ -36,7 +38,7 @@ namespace {
 
 constexpr int TY = 32;
 constexpr int NTH = 4 * TY;
-constexpr int CHUNK = 480;
+constexpr int CHUNK = 384;
 
 enum {
   P_U = 0, P_V, P_NU, P_NUG, P_E, P_SXY, P_EXY, P_COH, P_PHI, P_RO, P_ET, P_HT,
@@ -48,30 +50,15 @@ struct Smem {
   uint8_t act[CHUNK];
 };
 
-// stage one marker: properties (recalc_marker_properties.c) and payload
-__device__ __forceinline__ void stage(const M2NArgs &a, Smem &sm, int s, int k, int ci,
-                                      bool owned_col, int j0) {
+// stage one marker's scatter payload; the per-marker physics (viscosity,
+// conductivity, density, state update) was done by the marker physics kernel
+__device__ __forceinline__ void stage(const M2NArgs &a, Smem &sm, int s, int k) {
   const Grid &g = a.g;
   const int idx = __ldg(a.perm + s);
   const int c = a.m.cell_in[idx];
   const int ix = c / g.ncy, iy = c - ix * g.ncy;
   const float u = a.m.u_in[idx], v = a.m.v_in[idx];
   const int t = a.m.type[idx];
-  const bool owned = owned_col && iy >= j0 && iy < j0 + TY;
-  (void)ci;
-
-  // sticky-air flags, interpolation.c:866-916: every marker (no in-grid
-  // test), the last one in reference numbering wins -> max of (id, type)
-  if (owned && (t == 1 || t == 2)) {
-    long m3 = (long)ix * g.yn + iy + 1, q = -1;
-    if (u < 0.5f && v < 0.5f) q = m3;
-    else if (u < 0.5f && v > 0.5f) q = m3 + 1;
-    else if (u > 0.5f && v < 0.5f) q = m3 + g.yn;
-    else if (u > 0.5f && v > 0.5f) q = m3 + g.yn + 1;
-    if (q >= 0 && q < g.nn)
-      atomicMax(a.sticky_key + q, ((uint32_t)a.m.id[idx] << 2) | (uint32_t)t);
-  }
-
   // strictly inside the model (interpolation.c:219)
   bool act = true;
   if (ix == 0 || ix == g.ncx - 1) {
@@ -84,61 +71,25 @@ __device__ __forceinline__ void stage(const M2NArgs &a, Smem &sm, int s, int k, 
   }
   sm.act[k] = act;
   if (!act) return;
-
-  const Axis ax = make_axis(g.wx, g.ncx, ix, u * __ldg(g.wx + ix));
-  const Axis ay = make_axis(g.wy, g.ncy, iy, v * __ldg(g.wy + iy));
-  // pressure at the marker in bar, allinterpomp (interpolation.c:1923)
-  float e, n;
-  long m3 = stencil_centre(g, ax, ay, u > 0.5f, v > 0.5f, e, n);
-  const float mpb = 1e-5f * bil(a.N.f(V2C_NF_PR), m3, g.yn, e, n);
   const float T = a.m.tk[idx];
-  float mro, mbb;
-  density32(a.R, a.S.p.densimod, t, T, mpb, mro, mbb);
-  const float mkt = conductivity32(a.R, t, T, mpb);
-  const float sxx = a.m.sxx[idx], sxy = a.m.sxy[idx];
-  const float sigin = sqrtf(sxx * sxx + sxy * sxy);
-  const float mnu = ductile_visc32(a.R, a.S, t, sigin, T, mpb);
-
-  // calc_frictionpara: only the state phi feeds the scatter.  Outside a
-  // 1 m margin of the frictional band the FP32 position decides; inside it
-  // the FP64 position does, as in the reference.
-  float phi = a.m.phi[idx];
-  if (t > 0) {
-    const v2c_params &p = a.S.p;
-    float xf = __ldg(a.gxf + ix) + ax.X, yf = __ldg(a.gyf + iy) + ay.X;
-    float rad = fabsf(yf - ((float)p.fault_y + (float)p.fault_slope * xf));
-    Fric fr;
-    if (rad > (float)p.fault_hw + 1.0f) {
-      phi = 50.f;
-    } else {
-      double x = g.gx[ix] + (double)u * (g.gx[ix + 1] - g.gx[ix]);
-      double y = g.gy[iy] + (double)v * (g.gy[iy + 1] - g.gy[iy]);
-      phi = friction_marker(p, a.S.phi_reset0, x, y, t, phi, fr);
-    }
-    // The update is idempotent, so a neighbouring tile that stages this
-    // marker as halo computes the same value whichever phi it reads.
-    if (owned && phi != a.m.phi[idx]) a.m.phi[idx] = phi;
-  }
-  if (owned) a.m.mnu[idx] = mnu;
-  if (owned && !(mnu > 0.f)) atomicAdd(a.stat + ST_NAN, 1ull);
-
-  const float mgg = a.R(RK_GG, t);
+  const float mnu = a.m.mnu[idx];
+  const float bb = a.R(RK_BB, t);
   sm.p[P_U][k] = u;
   sm.p[P_V][k] = v;
   sm.p[P_NU][k] = mnu;
-  sm.p[P_NUG][k] = mnu / mgg;
+  sm.p[P_NUG][k] = mnu / a.R(RK_GG, t);
   sm.p[P_E][k] = a.m.e[idx];
-  sm.p[P_SXY][k] = sxy;
+  sm.p[P_SXY][k] = a.m.sxy[idx];
   sm.p[P_EXY][k] = a.m.exy[idx];
   sm.p[P_COH][k] = a.m.coh[idx];
-  sm.p[P_PHI][k] = phi;
-  sm.p[P_RO][k] = mro;
-  sm.p[P_ET][k] = mbb;
+  sm.p[P_PHI][k] = a.m.phi[idx];
+  sm.p[P_RO][k] = a.S.p.densimod ? a.m.mro[idx] : a.R(RK_RO, t);
+  sm.p[P_ET][k] = bb / (1.f - bb * (T - 298.15f));  // dencalcomp adiabatic term
   sm.p[P_HT][k] = a.R(RK_HT, t);
   sm.p[P_CP][k] = a.R(RK_CP, t);
-  sm.p[P_KT][k] = mkt;
+  sm.p[P_KT][k] = a.m.mkt[idx];
   sm.p[P_TK][k] = T;
-  sm.p[P_SXX][k] = sxx;
+  sm.p[P_SXX][k] = a.m.sxx[idx];
   sm.p[P_EXX][k] = a.m.exx[idx];
   sm.p[P_P][k] = a.m.p[idx];
   sm.p[P_VX][k] = a.m.vx[idx];
@@ -186,7 +137,7 @@ __device__ void friction_node(const v2c_params &p, double x, double y, double &m
     A[6].add(w);                                                      \
   } while (0)
 
-__global__ void __launch_bounds__(NTH) k_m2n(M2NArgs a) {
+__global__ void __launch_bounds__(NTH, 6) k_m2n(M2NArgs a) {
   __shared__ Smem sm;
   const Grid &g = a.g;
   const int tid = threadIdx.x, role = tid / TY, jl = tid % TY;
@@ -231,11 +182,10 @@ __global__ void __launch_bounds__(NTH) k_m2n(M2NArgs a) {
         up_e = __ldg(a.start + cb + j + 1);
         s1up = iwx / __ldg(g.wy + j);
       }
-      const bool owned_col = ci >= i0;
       for (int cs = seg_b; cs < seg_e; cs += CHUNK) {
         const int ce = min(cs + CHUNK, seg_e);
         __syncthreads();
-        for (int k = tid; k < ce - cs; k += NTH) stage(a, sm, cs + k, k, ci, owned_col, j0);
+        for (int k = tid; k < ce - cs; k += NTH) stage(a, sm, cs + k, k);
         __syncthreads();
         // cell (ci, j-1): bottom halves (v > 0.5) reach node row j
         for (int s = max(lo_b, cs); s < min(lo_e, ce); ++s) {

@@ -23,7 +23,7 @@ namespace {
 
 constexpr int TY = 32;
 constexpr int NTH = 4 * TY;
-constexpr int CHUNK = 640;
+constexpr int CHUNK = 512;
 
 enum { Q_U = 0, Q_V, Q_PHIS, Q_SXY, Q_EXY, Q_ES, Q_PR, Q_SXX, Q_EXX, Q_VX, Q_VY, Q_MRO, Q_N };
 
@@ -106,7 +106,7 @@ __device__ void allinteri(const Grid &g, const Nodes &N, Pos p, float &VX, float
     A[4].add(w);                                                        \
   } while (0)
 
-__global__ void __launch_bounds__(NTH) k_n2m_move(N2MArgs a) {
+__global__ void __launch_bounds__(NTH, 5) k_n2m_move(N2MArgs a) {
   __shared__ Smem sm;
   const Grid &g = a.g;
   const Nodes &N = a.N;

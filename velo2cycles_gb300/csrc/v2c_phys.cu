@@ -1,0 +1,179 @@
+// v2c_phys.cu -- per-marker physics of marker2nodes, in marker array order.
+//
+// For every marker strictly inside the model (interpolation.c:219): pressure
+// at the marker (allinterpomp, interpolation.c:1923), density, thermal
+// conductivity and ductile viscosity with the creep Newton
+// (recalc_marker_properties.c, density_ductilevisc_calc.c), the RSF state
+// update of calc_frictionpara (calc_RSF.c:224-295); for every marker the
+// sticky-air flag candidate (interpolation.c:866-916).  Results go to
+// per-marker arrays (mnu, mkt, mro) the scatter sweep reads.
+//
+// Then, unless disabled, the per-marker visco-elasto-plastic + RSF Newton
+// (v2c_rsf.cuh) from the plain start (previous slip rate) or the network's
+// proposal (v2c_mlp.cuh, evaluated by each warp on the tensor cores), with a
+// fallback to the plain start when the proposal does not converge.
+#include <math.h>
+
+#include "v2c_kernels.h"
+#include "v2c_mlp.cuh"
+#include "v2c_rheology.cuh"
+#include "v2c_rsf.cuh"
+
+namespace v2c {
+
+namespace {
+
+constexpr int PT = 128;  // 4 warps
+
+__device__ __forceinline__ void warp_add(unsigned long long *p, unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(V2C_FULL, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(p, v);
+}
+
+__global__ void __launch_bounds__(PT) k_phys(PhysArgs a) {
+  __shared__ MlpSmem S;
+  const Grid &g = a.g;
+  const int guess = a.S.p.newton_guess;
+  const bool learned = guess == V2C_GUESS_LEARNED && a.mlp != nullptr;
+  if (learned) {
+    mlp_load_smem(S, a.mlp);
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  const long nwarps = (long)gridDim.x * (PT / 32);
+  const long n = a.n;
+  const v2c_params &P = a.S.p;
+  for (long base = ((long)blockIdx.x * (PT / 32) + wl) * 32; base < n; base += nwarps * 32) {
+    const long i = base + lane;
+    const bool valid = i < n;
+    bool act = false, solve = false;
+    float mnu = 0.f, sigin = 0.f;
+    int t = 0;
+    Fric fr{0.f, 0.f, 1.f, 1.f, 0.f};
+    float phi = 0.f;
+    if (valid) {
+      const int c = a.m.cell_in[i];
+      const int ix = c / g.ncy, iy = c - ix * g.ncy;
+      const float u = a.m.u_in[i], v = a.m.v_in[i];
+      t = a.m.type[i];
+      // sticky-air flag candidates: every marker, last in reference order wins
+      if (t == 1 || t == 2) {
+        long m3 = (long)ix * g.yn + iy + 1, q = -1;
+        if (u < 0.5f && v < 0.5f) q = m3;
+        else if (u < 0.5f && v > 0.5f) q = m3 + 1;
+        else if (u > 0.5f && v < 0.5f) q = m3 + g.yn;
+        else if (u > 0.5f && v > 0.5f) q = m3 + g.yn + 1;
+        if (q >= 0 && q < g.nn)
+          atomicMax(a.sticky_key + q, ((uint32_t)a.m.id[i] << 2) | (uint32_t)t);
+      }
+      act = true;
+      if (ix == 0 || ix == g.ncx - 1) {
+        double x = g.gx[ix] + (double)u * (g.gx[ix + 1] - g.gx[ix]);
+        act = act && x > 0 && x < g.xsize;
+      }
+      if (iy == 0 || iy == g.ncy - 1) {
+        double y = g.gy[iy] + (double)v * (g.gy[iy + 1] - g.gy[iy]);
+        act = act && y > 0 && y < g.ysize;
+      }
+      if (act) {
+        const Axis ax = make_axis(g.wx, g.ncx, ix, u * __ldg(g.wx + ix));
+        const Axis ay = make_axis(g.wy, g.ncy, iy, v * __ldg(g.wy + iy));
+        float e, nn;
+        const long m3 = stencil_centre(g, ax, ay, u > 0.5f, v > 0.5f, e, nn);
+        const float mpb = 1e-5f * bil(a.N.f(V2C_NF_PR), m3, g.yn, e, nn);
+        const float T = a.m.tk[i];
+        float mro, mbb;
+        density32(a.R, P.densimod, t, T, mpb, mro, mbb);
+        const float mkt = conductivity32(a.R, t, T, mpb);
+        const float sxx = a.m.sxx[i], sxy = a.m.sxy[i];
+        sigin = sqrtf(sxx * sxx + sxy * sxy);
+        mnu = ductile_visc32(a.R, a.S, t, sigin, T, mpb);
+        // calc_frictionpara: FP32 position away from the band, FP64 near it
+        phi = a.m.phi[i];
+        const float xf = __ldg(a.gxf + ix) + ax.X, yf = __ldg(a.gyf + iy) + ay.X;
+        const float rad = fabsf(yf - ((float)P.fault_y + (float)P.fault_slope * xf));
+        if (t > 0 && rad > (float)P.fault_hw + 1.0f) {
+          phi = 50.f;
+          fr.a = (float)P.a_hr; fr.b = (float)P.b_hr; fr.L = (float)P.L_hr;
+          fr.V0 = (float)P.V0_hr; fr.mu0 = 0.6f;
+        } else {
+          const double x = g.gx[ix] + (double)u * (g.gx[ix + 1] - g.gx[ix]);
+          const double y = g.gy[iy] + (double)v * (g.gy[iy + 1] - g.gy[iy]);
+          phi = friction_marker(P, a.S.phi_reset0, x, y, t, phi, fr);
+        }
+        if (phi != a.m.phi[i]) a.m.phi[i] = phi;
+        a.m.mnu[i] = mnu;
+        a.m.mkt[i] = mkt;
+        if (P.densimod != 0) a.m.mro[i] = mro;
+        if (!(mnu > 0.f)) atomicAdd(a.stat + ST_NAN, 1ull);
+        solve = guess != V2C_GUESS_OFF && t > 0 && mnu > 0.f;
+      }
+    }
+    if (guess == V2C_GUESS_OFF) continue;
+
+    // ------------------------------------------- per-marker RSF Newton
+    RsfState q;
+    float u_plain = 0.f;
+    if (solve) {
+      const float exx = a.m.exx[i], exy = a.m.exy[i];
+      const float edot = sqrtf(exx * exx + exy * exy);
+      const double sn = (P.pmode == 0) ? P.nstress : (double)a.m.p[i];
+      rsf_setup(q, fr.a, fr.b, fr.L, fr.V0, fr.mu0, sn, P.timestep, phi, sigin, edot, mnu,
+                a.R(RK_GG, t), P.faultwidth);
+      const float vold = a.m.slipv[i];
+      u_plain = (vold > 0.f) ? __logf(vold) : -30.f;
+    }
+    float u0 = u_plain;
+    if (learned) {
+      // features: demanded friction, linear stiffness, a, b-a, mu0, phi,
+      // log dt/L, log V0 (oracle/v2c_oracle.c rsf_features)
+      float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      if (solve) {
+        f[0] = log10f((float)(q.Ts / (q.sn * q.c1)));
+        f[1] = log10f((float)(q.klin / (q.sn * q.c1)));
+        f[2] = (float)q.a * 100.f;
+        f[3] = (float)(q.b - q.a) * 100.f;
+        f[4] = (float)q.mu0;
+        f[5] = (float)q.phio;
+        f[6] = log10f((float)(q.dt / q.L));
+        f[7] = log10f((float)q.V0);
+      }
+#pragma unroll
+      for (int k = 0; k < 8; k++) S.xin[wl][lane][k] = f[k];
+      __syncwarp();
+      mlp_warp_forward(S, wl);
+      u0 = S.yout[wl][lane][0];
+      __syncwarp();
+    }
+    unsigned long long it = 0, fb = 0, nc = 0;
+    if (solve) {
+      RsfResult r = rsf_solve(q, u0, P.newton_rtol, P.newton_maxit);
+      it = r.it32 + r.it64;
+      if (!r.ok && learned) {
+        RsfResult r2 = rsf_solve(q, u_plain, P.newton_rtol, P.newton_maxit);
+        it += r2.it32 + r2.it64;
+        fb = 1;
+        r = r2;
+      }
+      if (!r.ok) nc = 1;
+      a.m.slipv[i] = (float)r.V;
+      if (r.res > 0) atomicMax(a.stat + ST_NEWTON_MAXRES_BITS, (unsigned long long)__double_as_longlong(r.res));
+    }
+    warp_add(a.stat + ST_NEWTON_ITERS, it);
+    warp_add(a.stat + ST_NEWTON_FALLBACK, fb);
+    warp_add(a.stat + ST_NEWTON_NONCONV, nc);
+  }
+}
+
+}  // namespace
+
+void launch_phys(const PhysArgs &a, cudaStream_t st) {
+  if (a.n <= 0) return;
+  long warps = (a.n + 31) / 32;
+  long blocks = (warps + PT / 32 - 1) / (PT / 32);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_phys<<<(unsigned)blocks, PT, 0, st>>>(a);
+}
+
+}  // namespace v2c

@@ -51,25 +51,30 @@ __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, in
   float lnv = s0;  // sigin == 0: eta = eta_diff
   if (sigin > 0.f) {
     // eta_disl / eta_diff = (ss / sigin)^(mm-1)
-    float d0 = expf((mm - 1.f) * (R(RK_LNSS, t) - logf(sigin)));
-    float g = expf(logf(R(RK_GG, t) * S.dt) - s0);  // G dt / eta_diff
-    float invS = expf(-s0);
-    float c0 = powf(d0, 1.f / mm);                  // coeff / eta_diff^(1/mm)
-    float em = (mm - 1.f) / mm;
-    float dnew = d0, m_prev = 0.f;
+    const float d0 = exp2f((mm - 1.f) * (R(RK_LNSS, t) - logf(sigin)) * 1.44269504089f);
+    const float g = __expf(__logf(R(RK_GG, t) * S.dt) - s0);  // G dt / eta_diff
+    const float invS = __expf(-s0);
+    const float em = (mm - 1.f) / mm;
+    const float c0 = exp2f(__log2f(d0) / mm);     // coeff / eta_diff^(1/mm)
+    const float emc0 = em * c0;
+    const float p2fac = 2.f * s0 * invS;
+    // |log10(m_k / m_k-1)| < 1e-6  <=>  10^-1e-6 < m_k / m_k-1 < 10^1e-6
+    const float RLO = 0.99999769741f, RHI = 1.00000230259f;
+    float dnew = d0, m_prev = 1.f;
     for (int counter = 1; counter <= 50; counter++) {
-      float dold = dnew;
-      float m = 1.f / (1.f + 1.f / dnew);           // mnu0 / eta_diff
-      float pf = 1.f + dold;                        // (eta_diff + eta_disl_old) / eta_diff
-      float base = pf * (g + m);
-      float f1 = powf(base, em);
-      float f2 = dold - c0 * f1;
+      const float dold = dnew;
+      const float m = __fdividef(dnew, dnew + 1.f);    // mnu0 / eta_diff
+      const float gm = g + m;
+      const float base = (1.f + dold) * gm;            // prefactor (G dt + mnu0) / eta_diff
+      const float f1 = exp2f(em * __log2f(base));      // base^((mm-1)/mm)
+      const float f2 = dold - c0 * f1;
       // pow(eta_diff, 2/(eta_diff+eta_disl_old)) / eta_diff, the reference's
       // extra term of the derivative (density_ductilevisc_calc.c:190-191)
-      float p2 = expf(2.f * s0 * invS / (1.f + dold)) * invS;
-      float df = 1.f - em * c0 * powf(base, -1.f / mm) * ((g + m) + p2);
-      dnew = dold - f2 / df;
-      if (counter > 3 && fabsf(log10f(m / m_prev)) < 1.0e-6f) break;
+      const float p2 = (invS > 1e-30f) ? __expf(__fdividef(p2fac, 1.f + dold)) * invS : 0.f;
+      const float df = 1.f - emc0 * __fdividef(f1, base) * (gm + p2);  // base^(-1/mm) = f1/base
+      dnew = dold - __fdividef(f2, df);
+      const float r = __fdividef(m, m_prev);
+      if (counter > 3 && r > RLO && r < RHI) break;
       m_prev = m;
     }
     lnv = s0 - log1pf(1.f / dnew);
