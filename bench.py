@@ -119,6 +119,22 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ helpers
+def max_over_ranks(x: float, dist, device) -> float:
+    """Largest x over the ranks of the job (x itself when not distributed).
+    The step time of N replicas is the slowest replica's."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(markers_per_rank: int, world: int, ms_max: float) -> float:
+    """Whole-job markers/s: every rank steps its own replica of the workload."""
+    return world * markers_per_rank / (ms_max * 1e-3)
+
+
 def measured_peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -249,12 +265,8 @@ def run_gpu(args, rank: int, world: int) -> None:
         dist.barrier()
     clk = clocks.stop()
     stage_ms = {k: (v[0] / args.steps) for k, v in prof.items() if v[1] > 0}
-    ms = ms_total / args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n / (ms * 1e-3)
+    ms = max_over_ranks(ms_total / args.steps, dist, "cuda")
+    value = replica_throughput(n, world, ms)
 
     # end to end through the C ABI with host node buffers
     nn = case.nodenum
@@ -288,11 +300,7 @@ def run_gpu(args, rank: int, world: int) -> None:
         e2e_step()
     e2.record(stream)
     torch.cuda.synchronize()
-    ms_e2e = s2.elapsed_time(e2) / args.steps
-    if dist:
-        t = torch.tensor([ms_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+    ms_e2e = max_over_ranks(s2.elapsed_time(e2) / args.steps, dist, "cuda")
 
     if rank != 0:
         m.close()
@@ -328,7 +336,7 @@ def run_gpu(args, rank: int, world: int) -> None:
         "roofline": roof,
         "cpu_baseline": ({k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
                          if base else None),
-        "e2e": {"value": world * n / (ms_e2e * 1e-3), "unit": UNIT,
+        "e2e": {"value": replica_throughput(n, world, ms_e2e), "unit": UNIT,
                 "h2d_bytes_per_step": 8 * nn * len(E2E_UP),
                 "d2h_bytes_per_step": 8 * nn * len(E2E_DOWN)},
         "gpu_launches": int(st1["kernel_launches"] - st0["kernel_launches"]),

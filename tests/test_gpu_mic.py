@@ -127,3 +127,42 @@ def test_full_step_deterministic(case):
         assert np.array_equal(outs[0][0][f], outs[1][0][f])
     for f in (abi.MF_X, abi.MF_XX):
         assert np.array_equal(outs[0][1][f], outs[1][1][f])
+
+
+VARIANTS = [dict(stoksmod=2, markmod=2), dict(antidiffinter=0), dict(Dphis=1.0),
+            dict(densimod=1, timesum=1e9), dict(pmode=1, timesum=1e8), dict(timesum=0.0),
+            dict(tempmod=0), dict(power_law_RSF=1), dict(RSFmode=0), dict(markmod=0)]
+
+
+@pytest.mark.parametrize("variant", VARIANTS, ids=lambda v: ",".join(f"{k}={x}" for k, x in v.items()))
+def test_flag_variants_full_step(variant, built_lib, oracle_built):
+    """The whole step under the reference's other flag settings."""
+    c = synth.make_case("small", seed=13, **variant)
+    m = mic.from_case(c)
+    ref = oracle.Restatement(c.copy())
+    dt = c.params["timestep"]
+    m.marker2nodes(); ref.marker2nodes()
+    _check_nodes(node_errors(m.download_nodes(M2N_OUT), ref.nodes, M2N_OUT))
+    m.interpolate_center2basic_old(); ref.center2basic_old()
+    m.compute_before_solve(dt, 0); ref.compute_before_solve(dt, 0)
+    m.compute_after_solve(dt, 0); ref.compute_after_solve(dt, 0)
+    _check_nodes(node_errors(m.download_nodes(C2B_OUT + RSF_OUT), ref.nodes, C2B_OUT + RSF_OUT))
+    m.nodes2markers(); ref.nodes2markers()
+    _check_nodes(node_errors(m.download_nodes(N2M_OUT), ref.nodes, N2M_OUT))
+    m.moveandrotatemarkers(); ref.move()
+    mk = m.download_markers(N2M_MARK + MOVE_MARK)
+    fields = [f for f in N2M_MARK if f not in (abi.MF_X, abi.MF_Y)]
+    errs = marker_errors(mk, ref.marks, fields)
+    bad = {k: v for k, v in errs.items() if not v <= TOL}
+    assert not bad, bad
+    wx = np.diff(c.gx)[nxsearch_np(c.gx, ref.marks[abi.MF_X])]
+    assert (np.abs(mk[abi.MF_X] - ref.marks[abi.MF_X]) / wx).max() <= 3e-7
+    m.close()
+
+
+def test_interpolationmod1_reported_unsupported(built_lib):
+    from velo2cycles_gb300._lib import V2CError
+    c = synth.make_case("tiny", seed=1, interpolationmod=1)
+    with pytest.raises(V2CError) as e:
+        mic.from_case(c)
+    assert e.value.code == abi.ERR_UNSUPPORTED
