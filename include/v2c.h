@@ -301,6 +301,41 @@ int v2c_mlp_grad(v2c_ctx *ctx, const double *states_dev,
 /* Network outputs for n states (device): out_dev[2][n] = (log V, phi). */
 int v2c_mlp_infer(v2c_ctx *ctx, const double *states_dev, long n, float *out_dev);
 
+/* ============================================ allocation-free cell sort
+ * No counterpart in the reference (its marker loops never sort).  Computes,
+ * for n markers at device positions x_dev[n], y_dev[n] on the device grid
+ * lines gx_dev[xnumx], gy_dev[ynumy], the same cell index as the context
+ * path (cell_dev[i] = nxsearch(x)*(ynumy-1) + nysearch(y), bit-exact) and the
+ * same stable counting sort by cell: perm_dev[start_dev[c] ..
+ * start_dev[c+1]) lists the markers of cell c in ascending index, and
+ * start_dev has (xnumx-1)*(ynumy-1)+1 entries.  All pointers are device
+ * pointers; the work is queued on cuda_stream (a cudaStream_t, NULL for the
+ * default stream) and the call returns without waiting for it.
+ *
+ * For callers that cannot let the library allocate: a host program whose
+ * device memory is all handed out by its own pool, or one that cannot afford
+ * the device-wide synchronisation that cudaMalloc/cudaFree bring, and that
+ * needs markers ordered by cell without building a whole context (which
+ * allocates some 40 per-marker arrays).  This call allocates no device or
+ * host memory.  Its only scratch is a fixed array in the library's device
+ * memory, 16 MiB + 4 KiB per device, that holds per-cell counters, so the
+ * grid may have at most V2C_STATIC_SORT_MAX_CELLS cells: larger grids return
+ * V2C_ERR_CAPACITY (with a message on stderr) before anything runs.  The
+ * counters must be zero before they are used; each call zeroes them on its
+ * own stream, so the caller zeroes nothing and the outputs need no initial
+ * value.  The first call on a device looks up the scratch address (set-up,
+ * done once per device with that device current); a caller that captures
+ * streams makes that first call before it begins capturing.  There is one
+ * scratch per device: calls that overlap on the same device (different
+ * streams or host threads without ordering between them) race on it and give
+ * wrong results, so order them. */
+/* 4 Mi cells: a 4001 x 1001 line grid (4 000 000 cells) fits */
+#define V2C_STATIC_SORT_MAX_CELLS 4194304
+int v2c_sort_cells_static(const double *gx_dev, long xnumx, const double *gy_dev,
+                          long ynumy, const double *x_dev, const double *y_dev, long n,
+                          int32_t *cell_dev, int32_t *perm_dev, int32_t *start_dev,
+                          void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
