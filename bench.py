@@ -2,8 +2,9 @@
 """Throughput of the GB300 marker-in-cell step (markers per second).
 
 A step is one pass of the per-timestep MIC pipeline over all markers:
-  marker2nodes (cell-sorted scatter with per-marker rheology, node tail,
-  boundary corrections) -> interpolate_center2basic_old ->
+  marker2nodes (per-marker physics and the per-marker visco-elasto-plastic
+  + rate-and-state Newton to a 1e-10 relative residual, cell-sorted scatter,
+  node tail, boundary corrections) -> interpolate_center2basic_old ->
   compute_before_solve / compute_after_solve (node RSF update) ->
   nodes2markers + moveandrotatemarkers (gather, back-scatter, RK4 advection,
   stress rotation) -> counting sort of the moved markers.
@@ -12,16 +13,25 @@ outputs are the seeded synthetic node fields already on the device.
 
 Workload: the 4001 x 1001 grid with 20 markers per cell (80 M markers,
 synth.make_case("c4")).  Inputs are larger than L2 (the marker arrays alone
-are ~5.6 GB), so no flush is needed between steps.
+are ~5.6 GB), so no flush is needed between steps.  Each step takes the
+next time step of a seeded log-uniform sequence in [1e-3, 1e10] s.
+
+The same steps are timed for four forms of the per-marker Newton: the
+network's start with split precision (the headline `value`), the plain
+start (previous slip rate) with split precision, and both starts with FP64
+throughout.  Every form starts from the same uploaded state.  The start
+network is first trained on the GPU on the model's own Newton problems
+(collected at 8 time steps) with plain FP64 solutions as targets.
 
 `value` is device-timed with CUDA events on the context's stream, inputs
 resident in HBM.  `e2e` is the same step through the C ABI with the node
 fields crossing the host boundary every step, as in the reference time loop
 around its host Stokes solve: the solver outputs are uploaded from pinned
 host memory before nodes2markers and the Stokes inputs are read back after
-marker2nodes.  `--impl reference` times the reference's own C routines
-(compiled from its sources, oracle/_ref) on all host cores on a bounded
-window of the same workload.
+marker2nodes.  `newton_c3` times the Newton alone on 4 M seeded states.
+`--impl reference` times the reference's own C routines (compiled from its
+sources, oracle/_ref) on all host cores on a bounded window of the same
+workload; the reference has no per-marker Newton.
 """
 from __future__ import annotations
 
@@ -202,10 +212,80 @@ def run_reference_arm(args, rank: int) -> None:
 
 
 # ------------------------------------------------------------- GPU arm
+# Newton forms timed on the same steps: (name, start guess, arithmetic)
+MODES = [("learned_split", "GUESS_LEARNED", "NEWTON_SPLIT"),
+         ("plain_split", "GUESS_PLAIN", "NEWTON_SPLIT"),
+         ("plain_fp64", "GUESS_PLAIN", "NEWTON_FP64"),
+         ("learned_fp64", "GUESS_LEARNED", "NEWTON_FP64")]
+
+
+def dt_sequence(k: int, seed: int) -> np.ndarray:
+    """Per-step time steps, log-uniform in [1e-3, 1e10] s (the coseismic to
+    interseismic range of the seismic-cycle runs): each step's slip rates
+    differ from the previous step's, so the previous slip rate is not
+    already the answer."""
+    return 10.0 ** np.random.default_rng(seed).uniform(-3, 10, k)
+
+
+def train_start_network(m, newton, abi, n_train: int, seed: int) -> dict:
+    """Train the start network on the model's own Newton problems, collected
+    at 8 time steps, with targets from the plain FP64 solve."""
+    import torch
+    t0 = time.time()
+    per = max(1, n_train // 8)
+    stride = max(1, m.n // per)
+    dts = dt_sequence(8, seed)
+    parts = []
+    for dt in dts:
+        m.set_params(timestep=float(dt))
+        parts.append(newton.collect_states(m, stride=stride))
+    S = torch.cat(parts, 1).contiguous()
+    m.set_params(newton_precision=abi.NEWTON_FP64)
+    out, it = newton.solve(m, S, abi.GUESS_PLAIN, on_device=True)
+    T = torch.stack([out[abi.RO_V], out[abi.RO_PHI]]).contiguous()
+    loss = newton.train(m, S, T, epochs=4, batch=8192, lr=3e-3, seed=seed)
+    torch.cuda.synchronize()
+    return {"states": int(S.shape[1]), "loss": float(loss), "seconds": time.time() - t0}
+
+
+def newton_c3(m, newton, abi, n: int = 4_000_000) -> dict:
+    """Per-marker Newton alone on n seeded states (the C3 benchmark), each
+    form timed with CUDA events; the network is retrained on these states'
+    plain FP64 solutions first."""
+    import torch
+    S = torch.from_numpy(newton.rsf_states(n, seed=101)).cuda()
+    m.set_params(newton_precision=abi.NEWTON_FP64)
+    out, _ = newton.solve(m, S, abi.GUESS_PLAIN, on_device=True)
+    T = torch.stack([out[abi.RO_V], out[abi.RO_PHI]]).contiguous()
+    newton.train(m, S, T, epochs=4, batch=8192, lr=3e-3, seed=3)
+    res = {}
+    for name, guess, prec in MODES:
+        m.set_params(newton_precision=getattr(abi, prec))
+        newton.solve(m, S, getattr(abi, guess), on_device=True)
+        torch.cuda.synchronize()
+        best, its = None, None
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            o, it = newton.solve(m, S, getattr(abi, guess), on_device=True)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            if best is None or ms < best:
+                best, its = ms, it
+        o = o.cpu().numpy()
+        res[name] = {"ms": best, "states_per_s": n / (best * 1e-3),
+                     "iters_per_state": float(its.abs().double().mean().item()),
+                     "max_residual": float(o[abi.RO_RES].max()),
+                     "nonconverged": int((its < 0).sum().item())}
+    res["states"] = n
+    return res
+
+
 def run_gpu(args, rank: int, world: int) -> None:
     import torch
 
-    from velo2cycles_gb300 import abi, build, mic, synth
+    from velo2cycles_gb300 import abi, build, mic, newton, synth
 
     build.build()
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -228,47 +308,67 @@ def run_gpu(args, rank: int, world: int) -> None:
     m.upload_nodes(case.nodes)
     m.synchronize()
     n = case.n
-    dt = case.params["timestep"]
     log(f"[bench] uploaded in {time.time() - t0:.1f}s")
+    training = train_start_network(m, newton, abi, 4_000_000, seed=11)
+    log(f"[bench] start network trained: {training}")
+    dts = dt_sequence(args.warmup + args.steps, seed=7)
 
-    def step():
+    def step(dt):
+        m.set_params(timestep=float(dt))
         m.marker2nodes()
         m.interpolate_center2basic_old()
         m.compute_before_solve(dt, 0)
         m.compute_after_solve(dt, 0)
         m.nodes2markers_move()
 
-    for _ in range(args.warmup):
-        step()
-    m.synchronize()
+    def run_mode(guess, prec, timed_clock=None):
+        # every form starts from the same uploaded state
+        m.upload_markers(case.marks, case.markt)
+        m.upload_nodes(case.nodes)
+        m.set_params(newton_guess=getattr(abi, guess), newton_precision=getattr(abi, prec))
+        for k in range(args.warmup):
+            step(dts[k])
+        m.synchronize()
+        if timed_clock:
+            timed_clock.start()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        st0 = m.status()
+        m.set_profiling(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(args.steps):
+            step(dts[args.warmup + k])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        st1 = m.status()
+        prof = m.profile()
+        m.set_profiling(False)
+        if dist:
+            dist.barrier()
+        ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dist, "cuda")
+        return {
+            "ms_per_step": ms, "markers_per_s": replica_throughput(n, world, ms),
+            "newton_iters_per_marker": (st1["newton_iters"] - st0["newton_iters"]) / (n * args.steps),
+            "newton_fallbacks": st1["newton_fallbacks"] - st0["newton_fallbacks"],
+            "newton_nonconverged": st1["newton_nonconv"] - st0["newton_nonconv"],
+            "newton_max_residual": st1["newton_max_res"],
+            "stage_ms": {k: v[0] / args.steps for k, v in prof.items() if v[1] > 0},
+            "launches": int(st1["kernel_launches"] - st0["kernel_launches"]),
+        }
 
-    # device-timed steps; the library brackets each kernel group with CUDA
-    # events on its own stream (v2c_set_profiling)
+    modes = {}
     clocks = ClockSampler(local)
-    clocks.start()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    st0 = m.status()
-    m.set_profiling(True)
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    start.record(stream)
-    for _ in range(args.steps):
-        step()
-    end.record(stream)
-    torch.cuda.synchronize()
-    st1 = m.status()
-    prof = m.profile()
-    m.set_profiling(False)
-    ms_total = start.elapsed_time(end)
-    if dist:
-        dist.barrier()
-    clk = clocks.stop()
-    stage_ms = {k: (v[0] / args.steps) for k, v in prof.items() if v[1] > 0}
-    ms = max_over_ranks(ms_total / args.steps, dist, "cuda")
-    value = replica_throughput(n, world, ms)
+    for name, guess, prec in MODES:
+        modes[name] = run_mode(guess, prec, clocks if name == "learned_split" else None)
+        if name == "learned_split":
+            clk = clocks.stop()
+        log(f"[bench] {name}: {modes[name]['ms_per_step']:.2f} ms/step")
+    head = modes["learned_split"]
+    ms, value, stage_ms = head["ms_per_step"], head["markers_per_s"], head["stage_ms"]
 
-    # end to end through the C ABI with host node buffers
+    # end to end through the C ABI with host node buffers, learned split form
     nn = case.nodenum
     up = {getattr(abi, "NF_" + f): torch.from_numpy(case.nodes[getattr(abi, "NF_" + f)]).pin_memory().numpy()
           for f in E2E_UP}
@@ -280,7 +380,8 @@ def run_gpu(args, rank: int, world: int) -> None:
 
     dp = ctypes.POINTER(ctypes.c_double)
 
-    def e2e_step():
+    def e2e_step(dt):
+        m.set_params(timestep=float(dt))
         m.marker2nodes()
         for f, a in down.items():
             call("v2c_download_node_field", m.h, f, a.ctypes.data_as(dp))
@@ -291,16 +392,21 @@ def run_gpu(args, rank: int, world: int) -> None:
             call("v2c_upload_node_field", m.h, f, a.ctypes.data_as(dp))
         m.nodes2markers_move()
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
+    m.upload_markers(case.marks, case.markt)
+    m.upload_nodes(case.nodes)
+    m.set_params(newton_guess=abi.GUESS_LEARNED, newton_precision=abi.NEWTON_SPLIT)
+    for k in range(max(1, args.warmup)):
+        e2e_step(dts[k])
     m.synchronize()
     s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s2.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
+    for k in range(args.steps):
+        e2e_step(dts[args.warmup + k])
     e2.record(stream)
     torch.cuda.synchronize()
     ms_e2e = max_over_ranks(s2.elapsed_time(e2) / args.steps, dist, "cuda")
+
+    c3 = newton_c3(m, newton, abi) if rank == 0 and not args.no_c3 else None
 
     if rank != 0:
         m.close()
@@ -308,7 +414,8 @@ def run_gpu(args, rank: int, world: int) -> None:
             dist.destroy_process_group()
         return
 
-    # roofline of the dominant kernel
+    # roofline of the dominant HBM-streaming kernel (the scatter and the
+    # gather/move sweeps; the per-marker physics + Newton is compute-bound)
     peaks = measured_peaks()
     mpn = n / nn
     dom = max(("m2n", "n2m_move"), key=lambda k: stage_ms.get(k, 0.0))
@@ -327,10 +434,17 @@ def run_gpu(args, rank: int, world: int) -> None:
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 fields, f64 node normalisation", "data": "synthetic",
         "config": {"workload": f"{args.config}: {case.params['xnumx']}x{case.params['ynumy']} grid, "
-                               f"{n} markers ({mpn:.1f}/node), dt={dt:g}s, RK4, interpolationmod=2, "
-                               "antidiffinter=1",
+                               f"{n} markers ({mpn:.1f}/node), RK4, interpolationmod=2, "
+                               "antidiffinter=1, per-marker VEP+RSF Newton to 1e-10, learned "
+                               "start, split precision",
+                   "dt": "per step log-uniform [1e-3, 1e10] s, seeded, same sequence for every form",
                    "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas only"},
         "stage_ms": stage_ms,
+        "newton_forms": modes,
+        "learned_split_vs_plain_fp64": modes["plain_fp64"]["ms_per_step"] / ms,
+        "learned_split_vs_plain_split": modes["plain_split"]["ms_per_step"] / ms,
+        "start_network": training,
+        "newton_c3": c3,
         "step_alg_bytes_per_marker": step_alg,
         "step_roofline_frac": (value / world) * step_alg / (peaks["hbm_gbs"] * 1e9),
         "roofline": roof,
@@ -339,7 +453,7 @@ def run_gpu(args, rank: int, world: int) -> None:
         "e2e": {"value": replica_throughput(n, world, ms_e2e), "unit": UNIT,
                 "h2d_bytes_per_step": 8 * nn * len(E2E_UP),
                 "d2h_bytes_per_step": 8 * nn * len(E2E_DOWN)},
-        "gpu_launches": int(st1["kernel_launches"] - st0["kernel_launches"]),
+        "gpu_launches": head["launches"],
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
@@ -356,6 +470,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c4")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-c3", action="store_true", help="skip the Newton-only C3 block")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

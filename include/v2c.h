@@ -89,10 +89,16 @@ typedef struct v2c_params {
   double newton_rtol;       /* [1e-10] relative residual                      */
   int newton_maxit;         /* [60]                                           */
   int newton_guess;         /* V2C_GUESS_*                                    */
+  int newton_precision;     /* V2C_NEWTON_SPLIT [default] or V2C_NEWTON_FP64  */
 } v2c_params;
 
 /* initial-guess modes of the per-marker Newton */
 enum { V2C_GUESS_PLAIN = 0, V2C_GUESS_LEARNED = 1, V2C_GUESS_OFF = 2 };
+/* arithmetic of the per-marker Newton: SPLIT iterates in FP32 and finishes
+ * with float-float residuals (FP64 only to form the converged residual and
+ * as a fallback); FP64 runs every iteration in FP64.  Both stop at the same
+ * relative residual newton_rtol. */
+enum { V2C_NEWTON_SPLIT = 0, V2C_NEWTON_FP64 = 1 };
 
 /* -------------------------------------------------------------- rock table
  * Per-type coefficients, each a double[V2C_MAXTMR] row, headevps.c:256-272. */
@@ -275,6 +281,17 @@ enum { V2C_RO_V = 0, V2C_RO_PHI, V2C_RO_TAU, V2C_RO_RES, V2C_RO_N };
 
 int v2c_rsf_newton(v2c_ctx *ctx, const double *states_dev, long n, int guess,
                    double *out_dev, int32_t *iters_dev);
+
+/* The per-marker Newton problems the MIC step would solve now, for training
+ * the start network on the running model: the state (layout as for
+ * v2c_rsf_newton, states_dev[V2C_RS_N][cap]) of every stride-th marker in
+ * the context's marker order, computed by the same physics pass as
+ * v2c_marker2nodes but changing no marker or node.  A slot whose marker has
+ * no problem (outside the model, sticky air, zero viscosity) holds NaN in
+ * row V2C_RS_A.  *n_out = slots written = min(cap, ceil(n/stride)).  No
+ * counterpart in the reference. */
+int v2c_collect_newton_states(v2c_ctx *ctx, long stride, double *states_dev, long cap,
+                              long *n_out);
 
 /* Multilayer perceptron 8 -> 64 -> 64 -> 2 that proposes the Newton start.
  * Weights are one packed float32 vector (see V2C_MLP_NPARAM), layout

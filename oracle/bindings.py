@@ -22,9 +22,20 @@ def reference_path() -> str:
     return os.path.join(OUT, "v2c_ref")
 
 
+def _stale() -> bool:
+    outs = [restatement_path(), reference_path()]
+    if not all(os.path.exists(o) for o in outs):
+        return True
+    t = min(os.path.getmtime(o) for o in outs)
+    deps = [os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith((".c", ".h", ".sh"))]
+    deps.append(os.path.join(os.path.dirname(HERE), "include", "v2c.h"))
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
 def build(force: bool = False) -> None:
-    """Compile both checkers with oracle/build_ref.sh (seconds)."""
-    if force or not os.path.exists(restatement_path()) or not os.path.exists(reference_path()):
+    """Compile both checkers with oracle/build_ref.sh (seconds); again when
+    a source or the C-ABI header is newer than the builds."""
+    if force or _stale():
         subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True)
 
 
@@ -183,6 +194,22 @@ def rsf_newton(states: np.ndarray, W=400.0, rtol=1e-10, maxit=200, guess_logV=No
                                       _dp(g) if g is not None else None, _dp(out),
                                       it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
     return out, it, nc
+
+
+def rsf_residual(states: np.ndarray, V: np.ndarray, W=400.0) -> np.ndarray:
+    """FP64 relative residual |F|/(F+T*) of the per-marker problem at the
+    given slip rates (oracle rsf_eval)."""
+    S = np.ascontiguousarray(states, dtype=np.float64)
+    n = S.shape[1]
+    out = np.empty(n)
+    L = _lib()
+    scale = ctypes.c_double()
+    for i in range(n):
+        st = np.ascontiguousarray(S[:, i])
+        F = L.v2c_oracle_rsf_residual(_dp(st), W, float(V[i]), None, None, None,
+                                      ctypes.byref(scale))
+        out[i] = abs(F) / scale.value
+    return out
 
 
 def rsf_features(states: np.ndarray) -> np.ndarray:

@@ -1,8 +1,10 @@
 """Per-marker VEP+RSF Newton and its learned start (GPU).
 
-* the GPU solve (FP32 iterations + FP64 polish) reaches the 1e-10 relative
-  residual on every state and finds the oracle's root (FP64 CPU Newton,
-  oracle/v2c_oracle.c), slip rates within 1e-8 relative;
+* both GPU forms -- split (FP32 iterations, float-float finish) and FP64 --
+  reach the 1e-10 relative residual on every state, recomputed in FP64 by
+  the oracle at the returned slip rate, and find the oracle's root (FP64
+  CPU Newton, oracle/v2c_oracle.c), slip rates within 1e-8 relative; the
+  FP64 form takes the oracle's iteration path;
 * the backward pass of the network (BF16 tensor cores, FP32 accumulate)
   matches the FP64 CPU gradient of the same loss: cosine > 0.999, relative
   norm error < 3e-2 (BF16 operands carry 8 bits of mantissa);
@@ -43,6 +45,31 @@ def test_plain_newton_matches_oracle(ctx):
     assert np.quantile(rel, 0.999) < 1e-8, np.quantile(rel, 0.999)
     st = ctx.status()
     assert st["newton_nonconv"] == 0
+
+
+@pytest.mark.parametrize("precision", [abi.NEWTON_SPLIT, abi.NEWTON_FP64])
+def test_forms_reach_the_oracle_root(ctx, precision):
+    S = newton.rsf_states(20000, seed=31)
+    ref, rit, nc = B.rsf_newton(S, rtol=1e-10, maxit=200)
+    assert nc == 0
+    ctx.set_params(newton_precision=precision)
+    try:
+        out, it = newton.solve(ctx, S, abi.GUESS_PLAIN)
+    finally:
+        ctx.set_params(newton_precision=abi.NEWTON_SPLIT)
+    assert (it >= 0).all(), "non-converged states"
+    assert out[abi.RO_RES].max() <= 1e-10
+    V = out[abi.RO_V]
+    live = V > 1e-40
+    res = B.rsf_residual(S[:, live], V[live])
+    assert res.max() <= 1.5e-10, res.max()
+    rel = np.abs(V / ref[abi.RO_V] - 1)
+    assert np.quantile(rel, 0.999) < 1e-8, np.quantile(rel, 0.999)
+    tau_rel = np.abs(out[abi.RO_TAU] / ref[abi.RO_TAU] - 1)
+    assert np.quantile(tau_rel[live], 0.999) < 1e-8
+    if precision == abi.NEWTON_FP64:
+        # same safeguarded Newton, same start: the same number of steps
+        assert np.mean(it == rit) > 0.99
 
 
 def test_mlp_gradient_matches_oracle(ctx):
@@ -99,3 +126,30 @@ def test_mic_step_runs_newton(ctx):
     v = m.download_markers([abi.MF_SLIPV])[abi.MF_SLIPV]
     assert np.isfinite(v).all() and (v > 0).all()
     m.close()
+
+
+def test_collected_states_are_the_step_problems(ctx):
+    """v2c_collect_newton_states hands out exactly the problems the step
+    solves: solving them gives the slip rates the step writes."""
+    c = synth.make_case("small", seed=9)
+    c.marks[abi.MF_SLIPV][:] = -1.0  # plain start falls back to the same fixed value
+    m = mic.from_case(c)
+    S = newton.collect_states(m)
+    assert S.shape[0] == abi.RS_N and S.shape[1] > 0
+    out, it = newton.solve(m, S, abi.GUESS_PLAIN)
+    assert (it >= 0).all() and out[abi.RO_RES].max() <= 1e-10
+    before = m.download_markers([abi.MF_PHI, abi.MF_XX])
+    m.set_params(newton_guess=abi.GUESS_PLAIN)
+    m.marker2nodes()
+    v = m.download_markers([abi.MF_SLIPV])[abi.MF_SLIPV]
+    solved = v > 0
+    assert solved.sum() == S.shape[1]
+    assert np.array_equal(np.sort(v[solved].astype(np.float32)),
+                          np.sort(out[abi.RO_V].astype(np.float32)))
+    m.close()
+    # collection changed nothing
+    m2 = mic.from_case(c)
+    newton.collect_states(m2, stride=3)
+    after = m2.download_markers([abi.MF_PHI, abi.MF_XX])
+    assert all(np.array_equal(before[k], after[k]) for k in before)
+    m2.close()

@@ -9,6 +9,7 @@ The reference has no tests or stored answers, so the restatement
     made by tests/golden/make_golden.py), also bit-exact, which works where
     the reference sources are absent.
 """
+import json
 import os
 
 import numpy as np
@@ -37,7 +38,8 @@ def _compare(r, nodes_ref, marks_ref):
 @pytest.mark.parametrize("name", ["default", "variant"])
 def test_restatement_matches_golden(name):
     z = np.load(GOLDEN)
-    p = abi.Params.from_buffer_copy(z[f"{name}/params"].tobytes()).to_dict()
+    p = synth.default_params()
+    p.update(json.loads(str(z[f"{name}/params"])))
     nodes = {k: z[f"{name}/nodes_in"][k].copy() for k in range(abi.NF_N)}
     marks = {k: z[f"{name}/marks_in"][k].copy() for k in range(abi.MF_N)}
     c = synth.Case(name, p, z[f"{name}/gx"], z[f"{name}/gy"], z[f"{name}/rt"], nodes, marks,

@@ -52,6 +52,8 @@ _SIGS = {
     "v2c_get_profile": [c_ctx, ctypes.c_int, c_dp, P(ctypes.c_long)],
     "v2c_rsf_newton": [c_ctx, ctypes.c_void_p, ctypes.c_long, ctypes.c_int, ctypes.c_void_p,
                        ctypes.c_void_p],
+    "v2c_collect_newton_states": [c_ctx, ctypes.c_long, ctypes.c_void_p, ctypes.c_long,
+                                  P(ctypes.c_long)],
     "v2c_mlp_load": [c_ctx, c_fp],
     "v2c_mlp_save": [c_ctx, c_fp],
     "v2c_mlp_train": [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_long, ctypes.c_int,

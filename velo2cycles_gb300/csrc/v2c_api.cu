@@ -167,6 +167,9 @@ int check_params(const v2c_params *p) {
   if (p->xnumx < 4 || p->ynumy < 4) return V2C_ERR_ARG;
   if (p->interpolationmod != 2) return V2C_ERR_UNSUPPORTED;
   if (p->rkmod == 3) return V2C_ERR_UNSUPPORTED;
+  if (p->newton_guess < V2C_GUESS_PLAIN || p->newton_guess > V2C_GUESS_OFF) return V2C_ERR_ARG;
+  if (p->newton_precision != V2C_NEWTON_SPLIT && p->newton_precision != V2C_NEWTON_FP64)
+    return V2C_ERR_ARG;
   if (p->xnumx * p->ynumy > (long)INT32_MAX / 4) return V2C_ERR_CAPACITY;
   return V2C_OK;
 }
@@ -689,6 +692,27 @@ extern "C" int v2c_marker2nodes(v2c_ctx *ctx) {
   return V2C_OK;
 }
 
+extern "C" int v2c_collect_newton_states(v2c_ctx *ctx, long stride, double *states_dev,
+                                         long cap, long *n_out) {
+  int rc = ready(ctx);
+  if (rc) return rc;
+  if (stride < 1 || cap < 0 || (cap > 0 && !states_dev) || !n_out) return V2C_ERR_ARG;
+  PhysArgs ph;
+  ph.g = make_grid(ctx); ph.N = make_nodes(ctx); ph.m = ctx->m; ph.R = Rock{ctx->d_rock};
+  ph.S = make_scal(ctx->p, ctx->h_rt); ph.n = ctx->n;
+  ph.sticky_key = ctx->d_sticky; ph.stat = ctx->d_stat; ph.gxf = ctx->d_gxf; ph.gyf = ctx->d_gyf;
+  ph.mlp = nullptr;
+  ph.xs = states_dev; ph.xs_stride = stride; ph.xs_cap = cap;
+  const long slots = (ctx->n + stride - 1) / stride;
+  *n_out = slots < cap ? slots : cap;
+  if (*n_out > 0) {
+    launch_phys(ph, ctx->stream);
+    ctx->launches += 1;
+  }
+  CK(cudaGetLastError());
+  return V2C_OK;
+}
+
 extern "C" int v2c_center2basic_old(v2c_ctx *ctx) {
   if (!ctx) return V2C_ERR_ARG;
   {
@@ -749,6 +773,7 @@ static int n2m_move(v2c_ctx *ctx, int do_n2m, int do_move) {
   a.perm = ctx->sb.perm;
   a.start = ctx->sb.start;
   a.stat = ctx->d_stat;
+  a.gyf = ctx->d_gyf;
   a.TX = pick_tx(ctx);
   a.do_n2m = do_n2m;
   a.do_move = do_move;

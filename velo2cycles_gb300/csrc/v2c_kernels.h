@@ -48,6 +48,11 @@ struct PhysArgs {
   unsigned long long *stat;
   const float *gxf, *gyf;
   const float *mlp;  // packed network (device) or null
+  // collection mode (v2c_collect_newton_states): when xs is set the kernel
+  // writes the Newton state of every xs_stride-th marker to
+  // xs[V2C_RS_N][xs_cap] and changes nothing else
+  double *xs = nullptr;
+  long xs_stride = 1, xs_cap = 0;
 };
 void launch_phys(const PhysArgs &a, cudaStream_t st);
 void launch_sticky(const Nodes &N, const uint32_t *key, long nn, cudaStream_t st);
@@ -85,6 +90,7 @@ struct N2MArgs {
   const int32_t *perm;
   const int32_t *start;
   unsigned long long *stat;
+  const float *gyf;  // FP32 line positions (coarse depth test)
   int TX;
   int do_n2m, do_move;
 };

@@ -25,14 +25,17 @@ enum {
   MLP_OXS = MLP_OXM + 8, MLP_OYM = MLP_OXS + 8, MLP_OYS = MLP_OYM + 2, MLP_NP = MLP_OYS + 2
 };
 
-// shared-memory image of the network used by inference and training
+// Shared-memory image of the network used by inference.  Weight rows are
+// padded (16 -> 24 and 64 -> 72 BF16) so that the eight rows a B-fragment
+// load touches (one per lane group g) fall in distinct banks.
+constexpr int MLP_W1S = 24, MLP_W2S = 72;
 struct MlpSmem {
-  __nv_bfloat16 w1[64][16];   // K padded 8 -> 16 with zeros
-  __nv_bfloat16 w2[64][64];
-  __nv_bfloat16 w3[8][64];    // N padded 2 -> 8 with zeros
+  __nv_bfloat16 w1[64][MLP_W1S];   // K padded 8 -> 16 with zeros
+  __nv_bfloat16 w2[64][MLP_W2S];
+  __nv_bfloat16 w3[8][MLP_W2S];    // N padded 2 -> 8 with zeros
   float b1[64], b2[64], b3[2];
   float xm[8], xis[8], ym[2], ys[2];
-  float xin[4][32][8];        // per-warp feature staging (4 warps)
+  float xin[4][32][9];             // per-warp feature staging (4 warps), padded
   float yout[4][32][2];
 };
 
@@ -88,10 +91,12 @@ __device__ __forceinline__ uint32_t lds_u32(const __nv_bfloat16 *p) {
 
 // One warp evaluates the network for the 32 feature rows this warp staged
 // in S.xin[wl] (raw features, normalised here); results land in
-// S.yout[wl][row][0..1], denormalised.  All 32 lanes must call it.
+// S.yout[wl][row][0..1], denormalised.  The two 16-row m-tiles go through
+// the layers one after the other (fewer live registers than both at once).
+// All 32 lanes must call it.
 __device__ __forceinline__ void mlp_warp_forward(MlpSmem &S, int wl) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
+#pragma unroll 1
   for (int mt = 0; mt < 2; mt++) {
     const int r0 = mt * 16 + g, r1 = r0 + 8;
     // layer 1: X (16x16, K padded) times W1^T

@@ -52,32 +52,28 @@ __device__ __forceinline__ double st_at(const double *S, long n, int k, long i) 
   return S[(long)k * n + i];
 }
 
-__device__ __forceinline__ void state_of(const double *S, long n, long i, double W, RsfState &q,
+__device__ __forceinline__ void state_of(const double *S, long n, long i, double W, RsfIn &in,
                                          double &vold) {
   vold = st_at(S, n, V2C_RS_VOLD, i);
-  rsf_setup(q, st_at(S, n, V2C_RS_A, i), st_at(S, n, V2C_RS_B, i), st_at(S, n, V2C_RS_L, i),
-            st_at(S, n, V2C_RS_V0, i), st_at(S, n, V2C_RS_MU0, i), st_at(S, n, V2C_RS_SN, i),
-            st_at(S, n, V2C_RS_DT, i), st_at(S, n, V2C_RS_PHIOLD, i),
-            st_at(S, n, V2C_RS_TAUOLD, i), st_at(S, n, V2C_RS_EDOT, i), st_at(S, n, V2C_RS_ETA, i),
-            st_at(S, n, V2C_RS_G, i), W);
-}
-
-// network inputs (same definition as the oracle's rsf_features)
-__device__ __forceinline__ void features(const RsfState &q, float *f) {
-  f[0] = (float)log10(q.Ts / (q.sn * q.c1));
-  f[1] = (float)log10(q.klin / (q.sn * q.c1));
-  f[2] = (float)(q.a * 100.0);
-  f[3] = (float)((q.b - q.a) * 100.0);
-  f[4] = (float)q.mu0;
-  f[5] = (float)q.phio;
-  f[6] = (float)log10(q.dt / q.L);
-  f[7] = (float)log10(q.V0);
+  in.a = ff_from_double(st_at(S, n, V2C_RS_A, i));
+  in.b = ff_from_double(st_at(S, n, V2C_RS_B, i));
+  in.L = ff_from_double(st_at(S, n, V2C_RS_L, i));
+  in.V0 = ff_from_double(st_at(S, n, V2C_RS_V0, i));
+  in.mu0 = ff_from_double(st_at(S, n, V2C_RS_MU0, i));
+  in.sn = ff_from_double(st_at(S, n, V2C_RS_SN, i));
+  in.dt = ff_from_double(st_at(S, n, V2C_RS_DT, i));
+  in.phio = ff_from_double(st_at(S, n, V2C_RS_PHIOLD, i));
+  in.tau_old = ff_from_double(st_at(S, n, V2C_RS_TAUOLD, i));
+  in.edot = ff_from_double(st_at(S, n, V2C_RS_EDOT, i));
+  in.eta = ff_from_double(st_at(S, n, V2C_RS_ETA, i));
+  in.G = ff_from_double(st_at(S, n, V2C_RS_G, i));
+  in.W = ff_from_double(W);
 }
 
 // ---------------------------------------------------------- solve states
 __global__ void __launch_bounds__(NT) k_solve_states(const double *S, long n, double W, int guess,
-                                                     const float *mlp, double rtol, int maxit,
-                                                     double *out, int32_t *iters,
+                                                     int fp64, const float *mlp, double rtol,
+                                                     int maxit, double *out, int32_t *iters,
                                                      unsigned long long *stat) {
   __shared__ MlpSmem M;
   const bool learned = guess == V2C_GUESS_LEARNED && mlp;
@@ -90,14 +86,14 @@ __global__ void __launch_bounds__(NT) k_solve_states(const double *S, long n, do
   for (long base = ((long)blockIdx.x * (NT / 32) + wl) * 32; base < n; base += nwarps * 32) {
     const long i = base + lane;
     const bool valid = i < n;
-    RsfState q;
+    RsfIn in;
     double vold = 1e-9;
-    if (valid) state_of(S, n, i, W, q, vold);
-    const float u_plain = (vold > 0) ? (float)log(vold) : -30.f;
+    if (valid) state_of(S, n, i, W, in, vold);
+    const float u_plain = (vold > 0) ? logf((float)vold) : -30.f;
     float u0 = u_plain;
     if (learned) {
       float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      if (valid && q.Ts > 0) features(q, f);
+      if (valid) rsf_features(in, f);
 #pragma unroll
       for (int k = 0; k < 8; k++) M.xin[wl][lane][k] = f[k];
       __syncwarp();
@@ -107,26 +103,24 @@ __global__ void __launch_bounds__(NT) k_solve_states(const double *S, long n, do
     }
     unsigned long long it = 0, fb = 0, nc = 0;
     if (valid) {
-      RsfResult r = rsf_solve(q, u0, rtol, maxit);
-      it = r.it32 + r.it64;
+      // the FP64 form starts from the FP64 log of the previous slip rate
+      const double u_plain64 = (fp64 && vold > 0) ? log(vold) : (double)u_plain;
+      RsfResult r = fp64 ? rsf_solve64(in, learned ? (double)u0 : u_plain64, rtol, maxit)
+                         : rsf_solve_split(in, u0, rtol, maxit);
+      it = r.it32 + r.itff + r.it64;
       if (!r.ok && learned) {
-        RsfResult r2 = rsf_solve(q, u_plain, rtol, maxit);
-        it += r2.it32 + r2.it64;
+        RsfResult r2 = fp64 ? rsf_solve64(in, u_plain64, rtol, maxit)
+                            : rsf_solve_split(in, u_plain, rtol, maxit);
+        it += r2.it32 + r2.itff + r2.it64;
         fb = 1;
         r = r2;
       }
       if (!r.ok) nc = 1;
       out[(long)V2C_RO_V * n + i] = r.V;
       out[(long)V2C_RO_PHI * n + i] = r.phi;
-      // tau_y at the solution, FP64 (the oracle's output)
-      {
-        double dF, rel, ph;
-        const double u = log(r.V);
-        rsf_eval64(q, u, dF, rel, ph);
-        const double w = u - log(2.0 * q.V0) + (q.mu0 + q.b * ph) / q.a;
-        const double A = (w > 20.0) ? w + 0.69314718055994530942 + 0.25 * exp(-2.0 * w) : asinh(exp(w));
-        out[(long)V2C_RO_TAU * n + i] = q.sn * q.a * A + 4.3303e+06 * r.V;
-      }
+      // tau_y = sn a A + 4.3303e6 V at the solution (calc_RSF.c:128), FP64
+      out[(long)V2C_RO_TAU * n + i] =
+          ff_to_double(in.sn) * ff_to_double(in.a) * r.A + RSF_ETA_RAD * r.V;
       out[(long)V2C_RO_RES * n + i] = r.res;
       if (iters) iters[i] = r.ok ? (int32_t)it : -(int32_t)it;
       if (r.res > 0) atomicMax(stat + ST_NEWTON_MAXRES_BITS, (unsigned long long)__double_as_longlong(r.res));
@@ -149,10 +143,10 @@ __global__ void __launch_bounds__(NT) k_infer(const double *S, long n, double W,
     const long i = base + lane;
     float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (i < n) {
-      RsfState q;
+      RsfIn in;
       double vold;
-      state_of(S, n, i, W, q, vold);
-      features(q, f);
+      state_of(S, n, i, W, in, vold);
+      rsf_features(in, f);
     }
 #pragma unroll
     for (int k = 0; k < 8; k++) M.xin[wl][lane][k] = f[k];
@@ -171,11 +165,11 @@ __global__ void __launch_bounds__(NT) k_infer(const double *S, long n, double W,
 __global__ void k_features(const double *S, const double *T, long n, double W, float *X, float *Y) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  RsfState q;
+  RsfIn in;
   double vold;
-  state_of(S, n, i, W, q, vold);
+  state_of(S, n, i, W, in, vold);
   float f[8];
-  features(q, f);
+  rsf_features(in, f);
 #pragma unroll
   for (int k = 0; k < 8; k++) X[i * 8 + k] = f[k];
   Y[i * 2 + 0] = (float)log(T[i]);
@@ -502,6 +496,7 @@ extern "C" int v2c_rsf_newton(v2c_ctx *ctx, const double *states_dev, long n, in
   cudaEvent_t ev;
   v2c_ctx_prof_begin(ctx, V2C_PROF_NEWTON, &ev);
   k_solve_states<<<(unsigned)blocks, NT, 0, st>>>(states_dev, n, p->faultwidth, guess,
+                                                  p->newton_precision == V2C_NEWTON_FP64,
                                                   v2c_ctx_newton(ctx)->d_mlp, p->newton_rtol,
                                                   p->newton_maxit, out_dev, iters_dev,
                                                   v2c_ctx_stat(ctx));

@@ -35,7 +35,8 @@ __global__ void __launch_bounds__(PT) k_phys(PhysArgs a) {
   __shared__ MlpSmem S;
   const Grid &g = a.g;
   const int guess = a.S.p.newton_guess;
-  const bool learned = guess == V2C_GUESS_LEARNED && a.mlp != nullptr;
+  const bool collect = a.xs != nullptr;
+  const bool learned = guess == V2C_GUESS_LEARNED && a.mlp != nullptr && !collect;
   if (learned) {
     mlp_load_smem(S, a.mlp);
     __syncthreads();
@@ -44,6 +45,10 @@ __global__ void __launch_bounds__(PT) k_phys(PhysArgs a) {
   const long nwarps = (long)gridDim.x * (PT / 32);
   const long n = a.n;
   const v2c_params &P = a.S.p;
+  const bool fp64 = P.newton_precision == V2C_NEWTON_FP64;
+  // FP64 scalars of the Newton as float pairs, once per thread
+  const ff dt_ff = ff_from_double(P.timestep), W_ff = ff_from_double(P.faultwidth),
+           sn_ff = ff_from_double(P.nstress);
   for (long base = ((long)blockIdx.x * (PT / 32) + wl) * 32; base < n; base += nwarps * 32) {
     const long i = base + lane;
     const bool valid = i < n;
@@ -58,7 +63,7 @@ __global__ void __launch_bounds__(PT) k_phys(PhysArgs a) {
       const float u = a.m.u_in[i], v = a.m.v_in[i];
       t = a.m.type[i];
       // sticky-air flag candidates: every marker, last in reference order wins
-      if (t == 1 || t == 2) {
+      if ((t == 1 || t == 2) && !collect) {
         long m3 = (long)ix * g.yn + iy + 1, q = -1;
         if (u < 0.5f && v < 0.5f) q = m3;
         else if (u < 0.5f && v > 0.5f) q = m3 + 1;
@@ -102,43 +107,63 @@ __global__ void __launch_bounds__(PT) k_phys(PhysArgs a) {
           const double y = g.gy[iy] + (double)v * (g.gy[iy + 1] - g.gy[iy]);
           phi = friction_marker(P, a.S.phi_reset0, x, y, t, phi, fr);
         }
-        if (phi != a.m.phi[i]) a.m.phi[i] = phi;
-        a.m.mnu[i] = mnu;
-        a.m.mkt[i] = mkt;
-        if (P.densimod != 0) a.m.mro[i] = mro;
-        if (!(mnu > 0.f)) atomicAdd(a.stat + ST_NAN, 1ull);
-        solve = guess != V2C_GUESS_OFF && t > 0 && mnu > 0.f;
+        if (!collect) {
+          if (phi != a.m.phi[i]) a.m.phi[i] = phi;
+          a.m.mnu[i] = mnu;
+          a.m.mkt[i] = mkt;
+          if (P.densimod != 0) a.m.mro[i] = mro;
+          if (!(mnu > 0.f)) atomicAdd(a.stat + ST_NAN, 1ull);
+        }
+        solve = (guess != V2C_GUESS_OFF || collect) && t > 0 && mnu > 0.f;
       }
     }
-    if (guess == V2C_GUESS_OFF) continue;
+    if (guess == V2C_GUESS_OFF && !collect) continue;
 
     // ------------------------------------------- per-marker RSF Newton
-    RsfState q;
+    RsfIn in;
     float u_plain = 0.f;
     if (solve) {
       const float exx = a.m.exx[i], exy = a.m.exy[i];
-      const float edot = sqrtf(exx * exx + exy * exy);
-      const double sn = (P.pmode == 0) ? P.nstress : (double)a.m.p[i];
-      rsf_setup(q, fr.a, fr.b, fr.L, fr.V0, fr.mu0, sn, P.timestep, phi, sigin, edot, mnu,
-                a.R(RK_GG, t), P.faultwidth);
+      in.a = ff_f(fr.a); in.b = ff_f(fr.b); in.L = ff_f(fr.L); in.V0 = ff_f(fr.V0);
+      in.mu0 = ff_f(fr.mu0);
+      in.sn = (P.pmode == 0) ? sn_ff : ff_f(a.m.p[i]);
+      in.dt = dt_ff; in.W = W_ff;
+      in.phio = ff_f(phi);
+      in.tau_old = ff_f(sigin);
+      in.edot = ff_f(sqrtf(exx * exx + exy * exy));
+      in.eta = ff_f(mnu);
+      in.G = ff_f(a.R(RK_GG, t));
       const float vold = a.m.slipv[i];
       u_plain = (vold > 0.f) ? __logf(vold) : -30.f;
     }
+    if (collect) {
+      if (valid && i % a.xs_stride == 0 && i / a.xs_stride < a.xs_cap) {
+        const long c = a.xs_cap, k = i / a.xs_stride;
+        double *x = a.xs + k;
+        if (solve) {
+          x[V2C_RS_VOLD * c] = (double)a.m.slipv[i];
+          x[V2C_RS_PHIOLD * c] = ff_to_double(in.phio);
+          x[V2C_RS_A * c] = ff_to_double(in.a);
+          x[V2C_RS_B * c] = ff_to_double(in.b);
+          x[V2C_RS_L * c] = ff_to_double(in.L);
+          x[V2C_RS_V0 * c] = ff_to_double(in.V0);
+          x[V2C_RS_MU0 * c] = ff_to_double(in.mu0);
+          x[V2C_RS_SN * c] = ff_to_double(in.sn);
+          x[V2C_RS_DT * c] = ff_to_double(in.dt);
+          x[V2C_RS_TAUOLD * c] = ff_to_double(in.tau_old);
+          x[V2C_RS_EDOT * c] = ff_to_double(in.edot);
+          x[V2C_RS_ETA * c] = ff_to_double(in.eta);
+          x[V2C_RS_G * c] = ff_to_double(in.G);
+        } else {
+          x[V2C_RS_A * c] = __longlong_as_double(0x7ff8000000000000ll);  // NaN: no problem
+        }
+      }
+      continue;
+    }
     float u0 = u_plain;
     if (learned) {
-      // features: demanded friction, linear stiffness, a, b-a, mu0, phi,
-      // log dt/L, log V0 (oracle/v2c_oracle.c rsf_features)
       float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      if (solve) {
-        f[0] = log10f((float)(q.Ts / (q.sn * q.c1)));
-        f[1] = log10f((float)(q.klin / (q.sn * q.c1)));
-        f[2] = (float)q.a * 100.f;
-        f[3] = (float)(q.b - q.a) * 100.f;
-        f[4] = (float)q.mu0;
-        f[5] = (float)q.phio;
-        f[6] = log10f((float)(q.dt / q.L));
-        f[7] = log10f((float)q.V0);
-      }
+      if (solve) rsf_features(in, f);
 #pragma unroll
       for (int k = 0; k < 8; k++) S.xin[wl][lane][k] = f[k];
       __syncwarp();
@@ -148,11 +173,13 @@ __global__ void __launch_bounds__(PT) k_phys(PhysArgs a) {
     }
     unsigned long long it = 0, fb = 0, nc = 0;
     if (solve) {
-      RsfResult r = rsf_solve(q, u0, P.newton_rtol, P.newton_maxit);
-      it = r.it32 + r.it64;
+      RsfResult r = fp64 ? rsf_solve64(in, (double)u0, P.newton_rtol, P.newton_maxit)
+                         : rsf_solve_split(in, u0, P.newton_rtol, P.newton_maxit);
+      it = r.it32 + r.itff + r.it64;
       if (!r.ok && learned) {
-        RsfResult r2 = rsf_solve(q, u_plain, P.newton_rtol, P.newton_maxit);
-        it += r2.it32 + r2.it64;
+        RsfResult r2 = fp64 ? rsf_solve64(in, (double)u_plain, P.newton_rtol, P.newton_maxit)
+                            : rsf_solve_split(in, u_plain, P.newton_rtol, P.newton_maxit);
+        it += r2.it32 + r2.itff + r2.it64;
         fb = 1;
         r = r2;
       }

@@ -68,6 +68,23 @@ def solve(mic, states, guess: int = abi.GUESS_PLAIN, on_device: bool = False):
     return out.cpu().numpy(), it.cpu().numpy()
 
 
+def collect_states(mic, stride: int = 1, cap: int | None = None):
+    """Newton states of every stride-th marker of the running model as a
+    float64 device tensor [V2C_RS_N, k] (markers without a problem
+    dropped)."""
+    import torch
+    n = mic.n
+    cap = cap if cap is not None else (n + stride - 1) // stride
+    X = torch.empty((abi.RS_N, cap), dtype=torch.float64, device="cuda")
+    got = ctypes.c_long()
+    call("v2c_collect_newton_states", mic.h, int(stride), ctypes.c_void_p(X.data_ptr()), int(cap),
+         ctypes.byref(got))
+    mic.synchronize()
+    X = X[:, :got.value]
+    keep = ~torch.isnan(X[abi.RS_A])
+    return X[:, keep].contiguous()
+
+
 def train(mic, states, targets, epochs: int = 4, batch: int = 4096, lr: float = 3e-3,
           seed: int = 0) -> float:
     """Train the start-proposal network on the GPU; targets[2, n] =

@@ -50,7 +50,7 @@ def default_params(**kw) -> dict:
         end_downdip=42.0e3, half_range=2.0e3,
         fault_y=10.0e3, fault_hw=100.0, fault_slope=0.0,
         faultwidth=400.0, newton_rtol=1e-10, newton_maxit=60,
-        newton_guess=0,
+        newton_guess=0, newton_precision=0,
     )
     p.update(kw)
     return p
