@@ -309,8 +309,13 @@ def run_gpu(args, rank: int, world: int) -> None:
     m.synchronize()
     n = case.n
     log(f"[bench] uploaded in {time.time() - t0:.1f}s")
-    training = train_start_network(m, newton, abi, 4_000_000, seed=11)
-    log(f"[bench] start network trained: {training}")
+    forms = [f for f in MODES if f[0] in args.forms.split(",")]
+    if not forms or forms[0][0] != "learned_split":
+        raise SystemExit("--forms must start with learned_split (the headline form)")
+    training = None
+    if any(g == "GUESS_LEARNED" for _, g, _ in forms):
+        training = train_start_network(m, newton, abi, 4_000_000, seed=11)
+        log(f"[bench] start network trained: {training}")
     dts = dt_sequence(args.warmup + args.steps, seed=7)
 
     def step(dt):
@@ -360,7 +365,7 @@ def run_gpu(args, rank: int, world: int) -> None:
 
     modes = {}
     clocks = ClockSampler(local)
-    for name, guess, prec in MODES:
+    for name, guess, prec in forms:
         modes[name] = run_mode(guess, prec, clocks if name == "learned_split" else None)
         if name == "learned_split":
             clk = clocks.stop()
@@ -392,19 +397,21 @@ def run_gpu(args, rank: int, world: int) -> None:
             call("v2c_upload_node_field", m.h, f, a.ctypes.data_as(dp))
         m.nodes2markers_move()
 
-    m.upload_markers(case.marks, case.markt)
-    m.upload_nodes(case.nodes)
-    m.set_params(newton_guess=abi.GUESS_LEARNED, newton_precision=abi.NEWTON_SPLIT)
-    for k in range(max(1, args.warmup)):
-        e2e_step(dts[k])
-    m.synchronize()
-    s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s2.record(stream)
-    for k in range(args.steps):
-        e2e_step(dts[args.warmup + k])
-    e2.record(stream)
-    torch.cuda.synchronize()
-    ms_e2e = max_over_ranks(s2.elapsed_time(e2) / args.steps, dist, "cuda")
+    ms_e2e = None
+    if not args.no_e2e:
+        m.upload_markers(case.marks, case.markt)
+        m.upload_nodes(case.nodes)
+        m.set_params(newton_guess=abi.GUESS_LEARNED, newton_precision=abi.NEWTON_SPLIT)
+        for k in range(max(1, args.warmup)):
+            e2e_step(dts[k])
+        m.synchronize()
+        s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s2.record(stream)
+        for k in range(args.steps):
+            e2e_step(dts[args.warmup + k])
+        e2.record(stream)
+        torch.cuda.synchronize()
+        ms_e2e = max_over_ranks(s2.elapsed_time(e2) / args.steps, dist, "cuda")
 
     c3 = newton_c3(m, newton, abi) if rank == 0 and not args.no_c3 else None
 
@@ -441,8 +448,10 @@ def run_gpu(args, rank: int, world: int) -> None:
                    "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas only"},
         "stage_ms": stage_ms,
         "newton_forms": modes,
-        "learned_split_vs_plain_fp64": modes["plain_fp64"]["ms_per_step"] / ms,
-        "learned_split_vs_plain_split": modes["plain_split"]["ms_per_step"] / ms,
+        "learned_split_vs_plain_fp64": (modes["plain_fp64"]["ms_per_step"] / ms
+                                        if "plain_fp64" in modes else None),
+        "learned_split_vs_plain_split": (modes["plain_split"]["ms_per_step"] / ms
+                                         if "plain_split" in modes else None),
         "start_network": training,
         "newton_c3": c3,
         "step_alg_bytes_per_marker": step_alg,
@@ -450,9 +459,9 @@ def run_gpu(args, rank: int, world: int) -> None:
         "roofline": roof,
         "cpu_baseline": ({k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
                          if base else None),
-        "e2e": {"value": replica_throughput(n, world, ms_e2e), "unit": UNIT,
-                "h2d_bytes_per_step": 8 * nn * len(E2E_UP),
-                "d2h_bytes_per_step": 8 * nn * len(E2E_DOWN)},
+        "e2e": ({"value": replica_throughput(n, world, ms_e2e), "unit": UNIT,
+                 "h2d_bytes_per_step": 8 * nn * len(E2E_UP),
+                 "d2h_bytes_per_step": 8 * nn * len(E2E_DOWN)} if ms_e2e else None),
         "gpu_launches": head["launches"],
         "clocks": clk,
     }
@@ -471,6 +480,9 @@ def main():
     ap.add_argument("--config", default="c4")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-c3", action="store_true", help="skip the Newton-only C3 block")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end loop")
+    ap.add_argument("--forms", default=",".join(f[0] for f in MODES),
+                    help="Newton forms to time, comma-separated, learned_split first")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

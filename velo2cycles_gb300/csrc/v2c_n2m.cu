@@ -55,47 +55,63 @@ __device__ __forceinline__ void settle(const Grid &g, Pos &p, unsigned long long
   }
 }
 
+// allinteri's arithmetic (interpolation.c:1688-1758) from precomputed
+// stencils: spin at basic nodes (mb), velocities averaged to the pressure
+// node (mc), blended with the staggered velocities VXs, VYs by xrat
+__device__ __forceinline__ void allinteri_from(const Nodes &N, long yn, long mb, float eb,
+                                               float nb, long mc, float ec, float nc, float VXs,
+                                               float VYs, float xrat, float &VX, float &VY,
+                                               float &ESP) {
+  ESP = bil(N.f(V2C_NF_ESP), mb, yn, eb, nb);
+  const float *vx = N.f(V2C_NF_VX), *vy = N.f(V2C_NF_VY);
+  const float d0 = (1.f - ec) * (1.f - nc), d1 = (1.f - ec) * nc, d2 = ec * (1.f - nc),
+              d3 = ec * nc;
+  const float vxm1 = __ldg(vx + mc - 1), vxc = __ldg(vx + mc);
+  VX = (d0 * (vxm1 + __ldg(vx + mc - yn - 1)) + d1 * (vxc + __ldg(vx + mc - yn)) +
+        d2 * (__ldg(vx + mc + yn - 1) + vxm1) + d3 * (__ldg(vx + mc + yn) + vxc)) *
+       0.5f * (1.f - xrat);
+  const float vyc = __ldg(vy + mc), vyu = __ldg(vy + mc - yn);
+  VY = (d0 * (vyu + __ldg(vy + mc - yn - 1)) + d1 * (__ldg(vy + mc - yn + 1) + vyu) +
+        d2 * (vyc + __ldg(vy + mc - 1)) + d3 * (__ldg(vy + mc + 1) + vyc)) *
+       0.5f * (1.f - xrat);
+  VX += VXs * xrat;
+  VY += VYs * xrat;
+}
+
+// allinteri's weight of the staggered velocities: 2/3, or 1 in the outer
+// half of a boundary cell.  X, Y: clamped position in metres from the cell's
+// lines; wx, wy: the cell's widths.
+__device__ __forceinline__ float allinteri_xrat(const Grid &g, int ix, int iy, float X, float Y,
+                                                float wx, float wy) {
+  float xrat = 2.f / 3.f;
+  if (ix == 0 && X < 0.5f * wx) xrat = 1.f;
+  if (ix == g.ncx - 1 && X > 0.5f * wx) xrat = 1.f;
+  if (iy == 0 && Y < 0.5f * wy) xrat = 1.f;
+  if (iy == g.ncy - 1 && Y > 0.5f * wy) xrat = 1.f;
+  return xrat;
+}
+
 // allinteri (interpolation.c:1688-1758): velocity and spin at a point
 __device__ void allinteri(const Grid &g, const Nodes &N, Pos p, float &VX, float &VY,
                           float &ESP) {
   // clamp into the model
-  float wx = __ldg(g.wx + p.ix), wy = __ldg(g.wy + p.iy);
+  const float wx = __ldg(g.wx + p.ix), wy = __ldg(g.wy + p.iy);
   if (p.ix == 0 && p.X < 0.f) p.X = 0.f;
   if (p.ix == g.ncx - 1 && p.X > wx) p.X = wx;
   if (p.iy == 0 && p.Y < 0.f) p.Y = 0.f;
   if (p.iy == g.ncy - 1 && p.Y > wy) p.Y = wy;
-  float xrat = 2.f / 3.f;
-  if (p.ix == 0 && p.X < 0.5f * wx) xrat = 1.f;
-  if (p.ix == g.ncx - 1 && p.X > 0.5f * wx) xrat = 1.f;
-  if (p.iy == 0 && p.Y < 0.5f * wy) xrat = 1.f;
-  if (p.iy == g.ncy - 1 && p.Y > 0.5f * wy) xrat = 1.f;
+  const float xrat = allinteri_xrat(g, p.ix, p.iy, p.X, p.Y, wx, wy);
   const Axis ax = make_axis(g.wx, g.ncx, p.ix, p.X);
   const Axis ay = make_axis(g.wy, g.ncy, p.iy, p.Y);
   const long yn = g.yn;
-  float e, n;
-  // exy, esp at basic nodes
-  long m3 = stencil_basic(g, ax, ay, e, n);
-  const float EXY = bil(N.f(V2C_NF_EXY), m3, yn, e, n);
-  ESP = bil(N.f(V2C_NF_ESP), m3, yn, e, n);
-  // exx and velocities averaged to pressure nodes
-  m3 = stencil_centre(g, ax, ay, p.X > 0.5f * wx, p.Y > 0.5f * wy, e, n);
-  const float *vx = N.f(V2C_NF_VX), *vy = N.f(V2C_NF_VY);
-  const float EXX = bil(N.f(V2C_NF_EXX), m3, yn, e, n);
-  (void)EXX;
-  float d0 = (1.f - e) * (1.f - n), d1 = (1.f - e) * n, d2 = e * (1.f - n), d3 = e * n;
-  const float vxm1 = __ldg(vx + m3 - 1), vxc = __ldg(vx + m3);
-  VX = (d0 * (vxm1 + __ldg(vx + m3 - yn - 1)) + d1 * (vxc + __ldg(vx + m3 - yn)) +
-        d2 * (__ldg(vx + m3 + yn - 1) + vxm1) + d3 * (__ldg(vx + m3 + yn) + vxc)) *
-       0.5f * (1.f - xrat);
-  const float vyc = __ldg(vy + m3), vyu = __ldg(vy + m3 - yn);
-  VY = (d0 * (vyu + __ldg(vy + m3 - yn - 1)) + d1 * (__ldg(vy + m3 - yn + 1) + vyu) +
-        d2 * (vyc + __ldg(vy + m3 - 1)) + d3 * (__ldg(vy + m3 + 1) + vyc)) *
-       0.5f * (1.f - xrat);
-  // staggered vx and vy
-  m3 = stencil_vx(g, ax, ay, p.Y < 0.5f * wy, g.xn - 2, e, n);
-  VX += bil(vx, m3, yn, e, n) * xrat;
+  float eb, nb, ec, nc, e, n;
+  const long mb = stencil_basic(g, ax, ay, eb, nb);
+  const long mc = stencil_centre(g, ax, ay, p.X > 0.5f * wx, p.Y > 0.5f * wy, ec, nc);
+  long m3 = stencil_vx(g, ax, ay, p.Y < 0.5f * wy, g.xn - 2, e, n);
+  const float VXs = bil(N.f(V2C_NF_VX), m3, yn, e, n);
   m3 = stencil_vy(g, ax, ay, p.X < 0.5f * wx, g.yn - 2, e, n);
-  VY += bil(vy, m3, yn, e, n) * xrat;
+  const float VYs = bil(N.f(V2C_NF_VY), m3, yn, e, n);
+  allinteri_from(N, yn, mb, eb, nb, mc, ec, nc, VXs, VYs, xrat, VX, VY, ESP);
 }
 
 // basic-node back-scatter into a named register array
@@ -170,30 +186,30 @@ __global__ void __launch_bounds__(NTH, 5) k_n2m_move(N2MArgs a) {
           const float wxc = __ldg(g.wx + ix), wyc = __ldg(g.wy + iy);
           const Axis ax = make_axis(g.wx, g.ncx, ix, uc * wxc);
           const Axis ay = make_axis(g.wy, g.ncy, iy, vc * wyc);
-          float e, n;
-          long m3 = stencil_basic(g, ax, ay, e, n);
-          const float EXY = bil(N.f(V2C_NF_EXY), m3, yn, e, n);
-          const float SXY = bil(N.f(V2C_NF_SXY), m3, yn, e, n);
-          const float ES = bil(N.f(V2C_NF_PES), m3, yn, e, n);
-          const float PHIS = bil(N.f(V2C_NF_PHIS_IT), m3, yn, e, n);
+          float eb, nb, ec, ncc, e, n;
+          const long mb = stencil_basic(g, ax, ay, eb, nb);
+          const float EXY = bil(N.f(V2C_NF_EXY), mb, yn, eb, nb);
+          const float SXY = bil(N.f(V2C_NF_SXY), mb, yn, eb, nb);
+          const float ES = bil(N.f(V2C_NF_PES), mb, yn, eb, nb);
+          const float PHIS = bil(N.f(V2C_NF_PHIS_IT), mb, yn, eb, nb);
           float EXYE = 0.f, SXYE = 0.f, ESE = 0.f, PHISE = 0.f;
           if (owned && P.antidiffinter != 1) {
-            EXYE = bil(N.f(V2C_NF_EXYE), m3, yn, e, n);
-            SXYE = bil(N.f(V2C_NF_SXYE), m3, yn, e, n);
-            ESE = bil(N.f(V2C_NF_PE), m3, yn, e, n);
-            PHISE = bil(N.f(V2C_NF_PHIS), m3, yn, e, n);
+            EXYE = bil(N.f(V2C_NF_EXYE), mb, yn, eb, nb);
+            SXYE = bil(N.f(V2C_NF_SXYE), mb, yn, eb, nb);
+            ESE = bil(N.f(V2C_NF_PE), mb, yn, eb, nb);
+            PHISE = bil(N.f(V2C_NF_PHIS), mb, yn, eb, nb);
           }
-          m3 = stencil_centre(g, ax, ay, uc > 0.5f, vc > 0.5f, e, n);
-          const float EXX = bil(N.f(V2C_NF_EXX), m3, yn, e, n);
-          const float SXX = bil(N.f(V2C_NF_SXX), m3, yn, e, n);
-          const float PR = bil(N.f(V2C_NF_PR), m3, yn, e, n);
+          const long mc = stencil_centre(g, ax, ay, uc > 0.5f, vc > 0.5f, ec, ncc);
+          const float EXX = bil(N.f(V2C_NF_EXX), mc, yn, ec, ncc);
+          const float SXX = bil(N.f(V2C_NF_SXX), mc, yn, ec, ncc);
+          const float PR = bil(N.f(V2C_NF_PR), mc, yn, ec, ncc);
           float EXXE = 0.f, SXXE = 0.f, SPPE = 0.f;
           if (owned && P.antidiffinter != 1) {
-            EXXE = bil(N.f(V2C_NF_EXXE), m3, yn, e, n);
-            SXXE = bil(N.f(V2C_NF_SXXE), m3, yn, e, n);
-            SPPE = bil(N.f(V2C_NF_SPPE), m3, yn, e, n);
+            EXXE = bil(N.f(V2C_NF_EXXE), mc, yn, ec, ncc);
+            SXXE = bil(N.f(V2C_NF_SXXE), mc, yn, ec, ncc);
+            SPPE = bil(N.f(V2C_NF_SPPE), mc, yn, ec, ncc);
           }
-          m3 = stencil_vx(g, ax, ay, vc < 0.5f, g.xn - 2, e, n);
+          long m3 = stencil_vx(g, ax, ay, vc < 0.5f, g.xn - 2, e, n);
           const float VX = bil(N.f(V2C_NF_VX), m3, yn, e, n);
           const float MVX = (owned && P.antidiffinter != 1) ? bil(N.f(V2C_NF_MVX), m3, yn, e, n) : 0.f;
           m3 = stencil_vy(g, ax, ay, uc < 0.5f, g.yn - 2, e, n);
@@ -207,6 +223,14 @@ __global__ void __launch_bounds__(NTH, 5) k_n2m_move(N2MArgs a) {
             sm.q[Q_MRO][k] = a.R(RK_RO, t);
           }
           if (!owned) continue;
+          // first allinteri evaluation of the move, at the marker itself:
+          // allinteri's clamped point is the gather's (uc, vc), so its
+          // stencils and staggered velocities are the gather's
+          float vx1 = 0.f, vy1 = 0.f, sp1 = 0.f;
+          if (a.do_move)
+            allinteri_from(N, yn, mb, eb, nb, mc, ec, ncc, VX, VY,
+                           allinteri_xrat(g, ix, iy, uc * wxc, vc * wyc, wxc, wyc), vx1, vy1,
+                           sp1);
 
           // ------------------------------------- marker update (:943-1011)
           const bool in_strict = (ix > 0 || u > 0.f) && (ix < g.ncx - 1 || u < 1.f) &&
@@ -251,8 +275,6 @@ __global__ void __launch_bounds__(NTH, 5) k_n2m_move(N2MArgs a) {
             const float dt = a.S.dt;
             Pos p0{ix, iy, u * wxc, v * wyc};
             float vx0, vy0, sp0;
-            float vx1, vy1, sp1;
-            allinteri(g, N, p0, vx1, vy1, sp1);
             if (P.markmod == 1) {
               vx0 = vx1; vy0 = vy1; sp0 = sp1;
             } else {
@@ -311,9 +333,9 @@ __global__ void __launch_bounds__(NTH, 5) k_n2m_move(N2MArgs a) {
             // stress rotation, moveandrotatemarkers.c:58-76
             sp0 *= dt;
             if (P.stoksmod == 1) {
-              float s, cth, s2, c2;
+              float s, cth;
               sincosf(sp0, &s, &cth);
-              sincosf(2.f * sp0, &s2, &c2);
+              const float s2 = 2.f * s * cth, c2 = cth * cth - s * s;  // sin, cos of 2 sp0
               float r1 = msxx * cth * cth - msxx * s * s + msxy * s2;
               float r3 = 0.5f * (-msxx - msxx) * s2 + msxy * c2;
               msxx = r1; msxy = r3;
@@ -322,9 +344,13 @@ __global__ void __launch_bounds__(NTH, 5) k_n2m_move(N2MArgs a) {
               float r3 = msxy + 0.5f * (-msxx - msxx) * 2.f * sp0;
               msxx = r1; msxy = r3;
             }
-            // markers coming from depth, out-of-grid reset (:79-87)
-            double ynew = g.gy[niy] + (double)nv_ * (g.gy[niy + 1] - g.gy[niy]);
-            if (ynew > P.zdeep && vy0 < 0.f && tk < (float)P.tdeep) tk = (float)P.tdeep;
+            // markers coming from depth, out-of-grid reset (:79-87); the
+            // FP64 position only when the FP32 one is within 1 m of zdeep
+            if (vy0 < 0.f && tk < (float)P.tdeep &&
+                __ldg(a.gyf + niy) + nv_ * __ldg(g.wy + niy) > (float)P.zdeep - 1.f - 1e-6f * fabsf((float)P.zdeep)) {
+              const double ynew = g.gy[niy] + (double)nv_ * (g.gy[niy + 1] - g.gy[niy]);
+              if (ynew > P.zdeep) tk = (float)P.tdeep;
+            }
             const bool out = (nix == 0 && nu_ < 0.f) || (nix == g.ncx - 1 && nu_ > 1.f) ||
                              (niy == 0 && nv_ < 0.f) || (niy == g.ncy - 1 && nv_ > 1.f);
             if (out) {

@@ -90,10 +90,16 @@ __global__ void __launch_bounds__(NT) k_solve_states(const double *S, long n, do
     double vold = 1e-9;
     if (valid) state_of(S, n, i, W, in, vold);
     const float u_plain = (vold > 0) ? logf((float)vold) : -30.f;
+    // split form: states whose load is certainly below the floor's yield
+    // are done with one FP32 evaluation; a warp with no other state skips
+    // the network
+    bool at_floor = false;
+    float A_floor = 0.f;
+    if (valid && !fp64) at_floor = rsf_floor_certain(rsf32_of(in), A_floor);
     float u0 = u_plain;
-    if (learned) {
+    if (learned && __any_sync(V2C_FULL, valid && !at_floor)) {
       float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      if (valid) rsf_features(in, f);
+      if (valid && !at_floor) rsf_features(in, f);
 #pragma unroll
       for (int k = 0; k < 8; k++) M.xin[wl][lane][k] = f[k];
       __syncwarp();
@@ -105,12 +111,13 @@ __global__ void __launch_bounds__(NT) k_solve_states(const double *S, long n, do
     if (valid) {
       // the FP64 form starts from the FP64 log of the previous slip rate
       const double u_plain64 = (fp64 && vold > 0) ? log(vold) : (double)u_plain;
-      RsfResult r = fp64 ? rsf_solve64(in, learned ? (double)u0 : u_plain64, rtol, maxit)
-                         : rsf_solve_split(in, u0, rtol, maxit);
+      RsfResult r = at_floor ? rsf_floor_result(in, A_floor)
+                  : fp64     ? rsf_solve64(in, learned ? (double)u0 : u_plain64, rtol, maxit)
+                             : rsf_solve_split(in, rsf32_of(in), u0, rtol, maxit);
       it = r.it32 + r.itff + r.it64;
       if (!r.ok && learned) {
         RsfResult r2 = fp64 ? rsf_solve64(in, u_plain64, rtol, maxit)
-                            : rsf_solve_split(in, u_plain, rtol, maxit);
+                            : rsf_solve_split(in, rsf32_of(in), u_plain, rtol, maxit);
         it += r2.it32 + r2.itff + r2.it64;
         fb = 1;
         r = r2;

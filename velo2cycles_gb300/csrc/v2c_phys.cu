@@ -160,10 +160,16 @@ __global__ void __launch_bounds__(PT) k_phys(PhysArgs a) {
       }
       continue;
     }
+    // split form: markers whose load is certainly below the floor's yield
+    // are done with one FP32 evaluation, and a warp with no other marker
+    // skips the network
+    bool at_floor = false;
+    float A_floor = 0.f;
+    if (solve && !fp64) at_floor = rsf_floor_certain(rsf32_of(in), A_floor);
     float u0 = u_plain;
-    if (learned) {
+    if (learned && __any_sync(V2C_FULL, solve && !at_floor)) {
       float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      if (solve) rsf_features(in, f);
+      if (solve && !at_floor) rsf_features(in, f);
 #pragma unroll
       for (int k = 0; k < 8; k++) S.xin[wl][lane][k] = f[k];
       __syncwarp();
@@ -173,12 +179,13 @@ __global__ void __launch_bounds__(PT) k_phys(PhysArgs a) {
     }
     unsigned long long it = 0, fb = 0, nc = 0;
     if (solve) {
-      RsfResult r = fp64 ? rsf_solve64(in, (double)u0, P.newton_rtol, P.newton_maxit)
-                         : rsf_solve_split(in, u0, P.newton_rtol, P.newton_maxit);
+      RsfResult r = at_floor ? rsf_floor_result(in, A_floor)
+                  : fp64     ? rsf_solve64(in, (double)u0, P.newton_rtol, P.newton_maxit)
+                             : rsf_solve_split(in, rsf32_of(in), u0, P.newton_rtol, P.newton_maxit);
       it = r.it32 + r.itff + r.it64;
       if (!r.ok && learned) {
         RsfResult r2 = fp64 ? rsf_solve64(in, (double)u_plain, P.newton_rtol, P.newton_maxit)
-                            : rsf_solve_split(in, u_plain, P.newton_rtol, P.newton_maxit);
+                            : rsf_solve_split(in, rsf32_of(in), u_plain, P.newton_rtol, P.newton_maxit);
         it += r2.it32 + r2.itff + r2.it64;
         fb = 1;
         r = r2;

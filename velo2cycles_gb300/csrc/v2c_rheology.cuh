@@ -135,6 +135,8 @@ __device__ __forceinline__ float friction_marker(const v2c_params &p, int phi_re
 // the upper-left stencil node and the weights (e, n).
 
 // basic (shear) nodes, interpolation.c:1067-1080: m10 clamped to [1, xn-3]
+// Stencil weights use the fast reciprocal division (__fdividef, 2 ulp): the
+// denominators are cell widths, far inside its range.
 __device__ __forceinline__ long stencil_basic(const Grid &g, const Axis &ax, const Axis &ay,
                                               float &e, float &n) {
   int m10 = ax.i, m20 = ay.i;
@@ -143,8 +145,8 @@ __device__ __forceinline__ long stencil_basic(const Grid &g, const Axis &ax, con
   if (m20 < 1) m20 = 1;
   if (m20 > g.yn - 3) m20 = g.yn - 3;
   int kx = m10 - ax.i, ky = m20 - ay.i;
-  e = (ax.X - ax.G(kx)) / (ax.G(kx + 1) - ax.G(kx));
-  n = (ay.X - ay.G(ky)) / (ay.G(ky + 1) - ay.G(ky));
+  e = __fdividef(ax.X - ax.G(kx), ax.G(kx + 1) - ax.G(kx));
+  n = __fdividef(ay.X - ay.G(ky), ay.G(ky + 1) - ay.G(ky));
   return (long)m10 * g.yn + m20;
 }
 
@@ -158,8 +160,8 @@ __device__ __forceinline__ long stencil_centre(const Grid &g, const Axis &ax, co
   if (m10 < 1) m10 = 1;
   if (m20 < 1) m20 = 1;
   int kx = m10 - ax.i, ky = m20 - ay.i;
-  e = (ax.X - (ax.G(kx - 1) + ax.G(kx)) * 0.5f) / ((ax.G(kx + 1) - ax.G(kx - 1)) * 0.5f);
-  n = (ay.X - (ay.G(ky - 1) + ay.G(ky)) * 0.5f) / ((ay.G(ky + 1) - ay.G(ky - 1)) * 0.5f);
+  e = __fdividef(ax.X - (ax.G(kx - 1) + ax.G(kx)) * 0.5f, (ax.G(kx + 1) - ax.G(kx - 1)) * 0.5f);
+  n = __fdividef(ay.X - (ay.G(ky - 1) + ay.G(ky)) * 0.5f, (ay.G(ky + 1) - ay.G(ky - 1)) * 0.5f);
   return (long)m10 * g.yn + m20;
 }
 
@@ -173,8 +175,8 @@ __device__ __forceinline__ long stencil_vx(const Grid &g, const Axis &ax, const 
   if (m20 < 0) m20 = 0;
   if (m20 > g.yn - 3) m20 = g.yn - 3;
   int kx = m10 - ax.i, ky = m20 - ay.i;
-  e = (ax.X - ax.G(kx)) / (ax.G(kx + 1) - ax.G(kx));
-  n = (ay.X - (ay.G(ky) + ay.G(ky + 1)) * 0.5f) / ((ay.G(ky + 2) - ay.G(ky)) * 0.5f);
+  e = __fdividef(ax.X - ax.G(kx), ax.G(kx + 1) - ax.G(kx));
+  n = __fdividef(ay.X - (ay.G(ky) + ay.G(ky + 1)) * 0.5f, (ay.G(ky + 2) - ay.G(ky)) * 0.5f);
   return (long)m10 * g.yn + m20;
 }
 
@@ -187,8 +189,8 @@ __device__ __forceinline__ long stencil_vy(const Grid &g, const Axis &ax, const 
   if (m20 < 0) m20 = 0;
   if (m20 > yclamp_hi) m20 = yclamp_hi;
   int kx = m10 - ax.i, ky = m20 - ay.i;
-  e = (ax.X - (ax.G(kx) + ax.G(kx + 1)) * 0.5f) / ((ax.G(kx + 2) - ax.G(kx)) * 0.5f);
-  n = (ay.X - ay.G(ky)) / (ay.G(ky + 1) - ay.G(ky));
+  e = __fdividef(ax.X - (ax.G(kx) + ax.G(kx + 1)) * 0.5f, (ax.G(kx + 2) - ax.G(kx)) * 0.5f);
+  n = __fdividef(ay.X - ay.G(ky), ay.G(ky + 1) - ay.G(ky));
   return (long)m10 * g.yn + m20;
 }
 

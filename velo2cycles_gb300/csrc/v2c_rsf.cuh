@@ -146,7 +146,6 @@ __device__ __forceinline__ RsfResult rsf_solve64(const RsfIn &in, double u0, dou
 // ------------------------------------------------- float-float residual
 struct RsfFF {
   ff Ts, klin, snac1, ephio, V0dtL, dtL, V0s, ln2V0, mu0, b, inv_a;
-  float uhi;  // log(T*/klin)
 };
 
 // 2^64 and 2^-64: V is carried as Vs = V 2^64 so that V down to the 1e-40
@@ -168,7 +167,6 @@ __device__ __forceinline__ void rsf_setup_ff(RsfFF &q, const RsfIn &in) {
   q.mu0 = in.mu0;
   q.b = in.b;
   q.inv_a = ff_div(ff_f(1.f), in.a);
-  q.uhi = logf(__fdiv_rn(q.Ts.hi, q.klin.hi));
 }
 
 // F and lhs = F + T* at u (float-float); phi and A at u.  Mirrors
@@ -236,13 +234,22 @@ __device__ __forceinline__ void rsf_features(const RsfIn &in, float *f) {
 
 // ------------------------------------------------------- FP32 residual
 struct Rsf32 {
-  float a, b, L, V0, mu0, dt, ephio, Ts, snac1, klin, lg2V0;
+  float a, b, L, V0, mu0, dt, ephio, Ts, snac1, klin, lg2V0, uhi;
 };
-__device__ __forceinline__ Rsf32 rsf32_of(const RsfIn &in, const RsfFF &q) {
+// FP32 constants straight from the inputs (no float-float set-up needed
+// for the FP32 phase)
+__device__ __forceinline__ Rsf32 rsf32_of(const RsfIn &in) {
   Rsf32 r;
   r.a = in.a.hi; r.b = in.b.hi; r.L = in.L.hi; r.V0 = in.V0.hi; r.mu0 = in.mu0.hi;
-  r.dt = in.dt.hi; r.ephio = q.ephio.hi; r.Ts = q.Ts.hi; r.snac1 = q.snac1.hi;
-  r.klin = q.klin.hi; r.lg2V0 = q.ln2V0.hi;
+  r.dt = in.dt.hi;
+  const float Gdt = in.G.hi * in.dt.hi;
+  r.Ts = in.tau_old.hi + 2.f * Gdt * in.edot.hi;
+  const float c1 = 1.f + Gdt / in.eta.hi;
+  r.klin = 4330300.f * c1 + 2.f * Gdt / in.W.hi;
+  r.snac1 = in.sn.hi * in.a.hi * c1;
+  r.ephio = expf(in.phio.hi);
+  r.lg2V0 = logf(2.f * in.V0.hi);
+  r.uhi = logf(r.Ts / r.klin);
   return r;
 }
 __device__ __forceinline__ float rsf_eval32(const Rsf32 &q, float u, float &dF, float &lhs) {
@@ -296,24 +303,37 @@ __device__ __forceinline__ float rsf_newton32(const Rsf32 &q, float u0, float ul
   return u;
 }
 
+// True when F(floor) > 0 is certain from the FP32 residual alone (margin
+// 1e-3 of the scale, two orders above the FP32 evaluation error): the load
+// cannot drive slip above the 1e-40 floor, and the floor is the solution
+// (the rule of the FP64 form at the floor).
+// A_floor: the friction term asinh(..) at the floor (FP32), for tau_y.
+__device__ __forceinline__ bool rsf_floor_certain(const Rsf32 &q, float &A_floor) {
+  A_floor = 0.f;
+  if (!(q.Ts > 0.f) || !(q.uhi > (float)RSF_LOG_FLOOR)) return false;  // degenerate: FP64 decides
+  float dF, lhs;
+  const float F = rsf_eval32(q, (float)RSF_LOG_FLOOR, dF, lhs);
+  A_floor = lhs / q.snac1;  // klin V is below 1e-30 of lhs at the floor
+  return F >= 1e-3f * lhs;
+}
+
 // Split solve from the start u0 (FP32 phase, float-float phase, FP64
-// fallback).
-__device__ __forceinline__ RsfResult rsf_solve_split(const RsfIn &in, float u0, double rtol,
-                                                     int maxit) {
+// fallback).  q32 = rsf32_of(in).
+__device__ __forceinline__ RsfResult rsf_solve_split(const RsfIn &in, const Rsf32 &q32, float u0,
+                                                     double rtol, int maxit) {
   RsfResult r{};
   r.phi = in.phio.hi;
-  RsfFF q;
-  rsf_setup_ff(q, in);
-  if (!(q.Ts.hi > 0.f) || !(q.uhi > (float)RSF_LOG_FLOOR)) {
-    // degenerate: decided in FP64 as the FP64 form does
+  const float floor32 = (float)RSF_LOG_FLOOR;
+  if (!(q32.Ts > 0.f) || !(q32.uhi > floor32)) {
+    // degenerate in FP32: decided in FP64 as the FP64 form does
     RsfState s;
     rsf_setup64(s, in);
     if (rsf_degenerate(s.Ts, s.klin)) { r.V = 1e-40; r.ok = true; return r; }
   }
-  const Rsf32 q32 = rsf32_of(in, q);
-  const float floor32 = (float)RSF_LOG_FLOOR;
   float dF32;
-  const float u32 = rsf_newton32(q32, u0, floor32, q.uhi, maxit, r.it32, dF32);
+  const float u32 = rsf_newton32(q32, u0, floor32, q32.uhi, maxit, r.it32, dF32);
+  RsfFF q;
+  rsf_setup_ff(q, in);
   const ff floor_u = ff_from_double(RSF_LOG_FLOOR);
   ff u = (u32 <= floor32 + 1e-6f) ? floor_u : ff_f(u32);
   for (int k = 0; k < 4; k++) {
@@ -339,6 +359,18 @@ __device__ __forceinline__ RsfResult rsf_solve_split(const RsfIn &in, float u0, 
   RsfState s;
   rsf_setup64(s, in);
   rsf_newton64(s, ff_to_double(u), rtol, maxit, true, r);
+  return r;
+}
+
+// The floor as a result (one FP32 residual evaluation)
+__device__ __forceinline__ RsfResult rsf_floor_result(const RsfIn &in, float A_floor) {
+  RsfResult r{};
+  r.phi = in.phio.hi;
+  r.A = A_floor;
+  r.V = 1e-40;
+  r.res = 0;
+  r.it32 = 1;
+  r.ok = true;
   return r;
 }
 
