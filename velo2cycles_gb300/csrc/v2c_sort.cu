@@ -28,9 +28,23 @@ __global__ void k_assign(Grid g, const double *x, const double *y, long n, Marke
   m.id[i] = (int32_t)i;
 }
 
+// Markers of one cell are mostly adjacent in memory, so the lanes of a warp
+// share few cells: one atomic per distinct cell in the warp (the leader adds
+// the group's size), each lane's slot is the group's base plus its rank
+// among the group's lanes.
 __global__ void k_count(const int32_t *cell, long n, int32_t *counts, int32_t *slot) {
-  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i < n) slot[i] = atomicAdd(counts + cell[i], 1);
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const bool valid = i < n;
+  const int c = valid ? cell[i] : -1;
+  const unsigned act = __ballot_sync(V2C_FULL, valid);
+  if (!valid) return;
+  const unsigned grp = __match_any_sync(act, c);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(grp) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counts + c, __popc(grp));
+  base = __shfl_sync(grp, base, leader);
+  slot[i] = base + __popc(grp & ((1u << lane) - 1));
 }
 
 // exclusive scan, three passes: per-block scan of 4 elements per thread
@@ -97,29 +111,50 @@ __global__ void k_slots(const int32_t *cell, long n, const int32_t *start, const
   if (i < n) tmp[start[cell[i]] + slot[i]] = (int32_t)i;
 }
 
-// one warp per cell: rank each entry among the cell's entries (all distinct)
-__global__ void k_rank(const int32_t *start, long ncell, const int32_t *tmp, int32_t *perm,
-                       unsigned long long *stat) {
-  long c = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (c >= ncell) return;
-  int s = start[c], L = start[c + 1] - s;
-  if (lane == 0 && L > 0) atomicMax(stat + ST_MAX_CELL, (unsigned long long)L);
-  if (L == 1) {
-    if (lane == 0) perm[s] = tmp[s];
+// One warp ranks the L distinct entries of a cell's slots (any order) and
+// writes them in ascending order.
+__device__ __forceinline__ void rank_segment(const int32_t *tmp, int32_t *perm, int L, int lane) {
+  if (L <= 32) {
+    const int val = (lane < L) ? tmp[lane] : INT_MAX;
+    int rank = 0;
+#pragma unroll
+    for (int k = 0; k < 32; k++) rank += (__shfl_sync(V2C_FULL, val, k) < val);
+    if (lane < L) perm[rank] = val;
     return;
   }
   for (int b = 0; b < L; b += 32) {
-    int jj = b + lane;
-    int val = (jj < L) ? tmp[s + jj] : INT_MAX;
+    const int jj = b + lane;
+    const int val = (jj < L) ? tmp[jj] : INT_MAX;
     int rank = 0;
     for (int b2 = 0; b2 < L; b2 += 32) {
-      int other = (b2 + lane < L) ? tmp[s + b2 + lane] : INT_MAX;
+      const int other = (b2 + lane < L) ? tmp[b2 + lane] : INT_MAX;
 #pragma unroll 8
       for (int k = 0; k < 32; k++) rank += (__shfl_sync(V2C_FULL, other, k) < val);
     }
-    if (jj < L) perm[s + rank] = val;
+    if (jj < L) perm[rank] = val;
   }
+}
+
+// one warp per cell: rank each entry among the cell's entries (all distinct);
+// the largest cell count goes to the status counter once per block
+__global__ void k_rank(const int32_t *start, long ncell, const int32_t *tmp, int32_t *perm,
+                       unsigned long long *stat) {
+  __shared__ int bmax;
+  if (threadIdx.x == 0) bmax = 0;
+  __syncthreads();
+  const long c = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c < ncell) {
+    const int s = start[c], L = start[c + 1] - s;
+    if (lane == 0 && L > 0) atomicMax(&bmax, L);
+    if (L == 1) {
+      if (lane == 0) perm[s] = tmp[s];
+    } else if (L > 1) {
+      rank_segment(tmp + s, perm + s, L, lane);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && bmax > 0) atomicMax(stat + ST_MAX_CELL, (unsigned long long)bmax);
 }
 
 __global__ void k_f64_to_f32(const double *src, float *dst, long n) {
