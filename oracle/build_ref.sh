@@ -47,7 +47,7 @@ if [ -f "$OUT/src/headevps.c" ]; then
   MODEL=""
   case "$(uname -m)" in x86_64) MODEL="-mcmodel=medium" ;; esac
   $CC -std=gnu99 -O3 -fopenmp -fcommon -w -ffp-contract=off $MODEL \
-      -I"$OUT/src" -o "$OUT/v2c_ref" "$HERE/ref_harness.c" -lm
+      -I"$OUT/src" -I"$HERE/../include" -o "$OUT/v2c_ref" "$HERE/ref_harness.c" -lm
 else
   echo "build_ref.sh: reference sources not found; built the restatement only" >&2
 fi

@@ -34,7 +34,11 @@ MOVE_MARK = [abi.MF_X, abi.MF_Y, abi.MF_XX, abi.MF_XY, abi.MF_K, abi.MF_E]
 # Viscosity-derived node fields carry the FP32 Arrhenius factor
 # exp((E+PV)/RT) of the power-law rocks; an FP32 temperature perturbs its
 # exponent by ~6e-8 relative, i.e. ~2e-6 relative on exp(40).
-VISCOUS = {abi.NF_NU_M2C, abi.NF_GG, abi.NF_ND_M2C, abi.NF_GD, abi.NF_NUVP_IT, abi.NF_NU}
+# The state rate RK_phidts_solved = V0/L e^-phi - V/L (calc_RSF.c:202) is a
+# difference of two terms that carries the same error through the slip rate
+# inverted from those viscosities.
+VISCOUS = {abi.NF_NU_M2C, abi.NF_GG, abi.NF_ND_M2C, abi.NF_GD, abi.NF_NUVP_IT, abi.NF_NU,
+           abi.NF_RK_PHIDTS_SOLVED}
 
 
 def rel_err(a: np.ndarray, b: np.ndarray) -> float:

@@ -144,8 +144,12 @@ def test_collected_states_are_the_step_problems(ctx):
     v = m.download_markers([abi.MF_SLIPV])[abi.MF_SLIPV]
     solved = v > 0
     assert solved.sum() == S.shape[1]
-    assert np.array_equal(np.sort(v[solved].astype(np.float32)),
-                          np.sort(out[abi.RO_V].astype(np.float32)))
+    # the same problems: the same slip rates up to the freedom the 1e-10
+    # residual leaves (the two kernels may round their FP32 iterates
+    # differently)
+    a_, b_ = np.sort(v[solved]), np.sort(out[abi.RO_V].astype(np.float32).astype(np.float64))
+    rel = np.abs(a_ - b_) / b_
+    assert np.quantile(rel, 0.999) < 1e-6 and rel.max() < 1e-3, (np.quantile(rel, 0.999), rel.max())
     m.close()
     # collection changed nothing
     m2 = mic.from_case(c)

@@ -46,6 +46,16 @@ __device__ __forceinline__ void warp_add(unsigned long long *p, unsigned long lo
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(V2C_FULL, v, o);
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(p, v);
 }
+// largest value over the warp, one atomic per warp (non-negative doubles
+// order like their bit patterns)
+__device__ __forceinline__ void warp_max_bits(unsigned long long *p, unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_down_sync(V2C_FULL, v, o);
+    v = w > v ? w : v;
+  }
+  if ((threadIdx.x & 31) == 0 && v) atomicMax(p, v);
+}
 
 // state column k of sample i (column-major [V2C_RS_N][n])
 __device__ __forceinline__ double st_at(const double *S, long n, int k, long i) {
@@ -71,12 +81,15 @@ __device__ __forceinline__ void state_of(const double *S, long n, long i, double
 }
 
 // ---------------------------------------------------------- solve states
-__global__ void __launch_bounds__(NT) k_solve_states(const double *S, long n, double W, int guess,
-                                                     int fp64, const float *mlp, double rtol,
-                                                     int maxit, double *out, int32_t *iters,
-                                                     unsigned long long *stat) {
+// one instantiation per (arithmetic, start) pair
+template <bool FP64, bool LEARNED>
+__global__ void __launch_bounds__(NT, 4) k_solve_states(const double *S, long n, double W,
+                                                        const float *mlp, double rtol, int maxit,
+                                                        double *out, int32_t *iters,
+                                                        unsigned long long *stat) {
   __shared__ MlpSmem M;
-  const bool learned = guess == V2C_GUESS_LEARNED && mlp;
+  const bool learned = LEARNED;
+  const bool fp64 = FP64;
   if (learned) {
     mlp_load_smem(M, mlp);
     __syncthreads();
@@ -107,7 +120,7 @@ __global__ void __launch_bounds__(NT) k_solve_states(const double *S, long n, do
       u0 = M.yout[wl][lane][0];
       __syncwarp();
     }
-    unsigned long long it = 0, fb = 0, nc = 0;
+    unsigned long long it = 0, fb = 0, nc = 0, resbits = 0;
     if (valid) {
       // the FP64 form starts from the FP64 log of the previous slip rate
       const double u_plain64 = (fp64 && vold > 0) ? log(vold) : (double)u_plain;
@@ -130,8 +143,9 @@ __global__ void __launch_bounds__(NT) k_solve_states(const double *S, long n, do
           ff_to_double(in.sn) * ff_to_double(in.a) * r.A + RSF_ETA_RAD * r.V;
       out[(long)V2C_RO_RES * n + i] = r.res;
       if (iters) iters[i] = r.ok ? (int32_t)it : -(int32_t)it;
-      if (r.res > 0) atomicMax(stat + ST_NEWTON_MAXRES_BITS, (unsigned long long)__double_as_longlong(r.res));
+      if (r.res > 0) resbits = (unsigned long long)__double_as_longlong(r.res);
     }
+    warp_max_bits(stat + ST_NEWTON_MAXRES_BITS, resbits);
     warp_add(stat + ST_NEWTON_ITERS, it);
     warp_add(stat + ST_NEWTON_FALLBACK, fb);
     warp_add(stat + ST_NEWTON_NONCONV, nc);
@@ -502,11 +516,13 @@ extern "C" int v2c_rsf_newton(v2c_ctx *ctx, const double *states_dev, long n, in
   if (blocks > 152 * 16) blocks = 152 * 16;
   cudaEvent_t ev;
   v2c_ctx_prof_begin(ctx, V2C_PROF_NEWTON, &ev);
-  k_solve_states<<<(unsigned)blocks, NT, 0, st>>>(states_dev, n, p->faultwidth, guess,
-                                                  p->newton_precision == V2C_NEWTON_FP64,
-                                                  v2c_ctx_newton(ctx)->d_mlp, p->newton_rtol,
-                                                  p->newton_maxit, out_dev, iters_dev,
-                                                  v2c_ctx_stat(ctx));
+  const bool fp64 = p->newton_precision == V2C_NEWTON_FP64;
+  const bool learned = guess == V2C_GUESS_LEARNED;
+  const float *mlp = v2c_ctx_newton(ctx)->d_mlp;
+  auto kern = fp64 ? (learned ? k_solve_states<true, true> : k_solve_states<true, false>)
+                   : (learned ? k_solve_states<false, true> : k_solve_states<false, false>);
+  kern<<<(unsigned)blocks, NT, 0, st>>>(states_dev, n, p->faultwidth, mlp, p->newton_rtol,
+                                        p->newton_maxit, out_dev, iters_dev, v2c_ctx_stat(ctx));
   v2c_ctx_prof_end(ctx, V2C_PROF_NEWTON, ev);
   v2c_ctx_count_launches(ctx, 1);
   CKR(cudaGetLastError());

@@ -30,13 +30,29 @@ __device__ __forceinline__ void warp_add(unsigned long long *p, unsigned long lo
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(V2C_FULL, v, o);
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(p, v);
 }
+// largest value over the warp, one atomic per warp (non-negative doubles
+// order like their bit patterns)
+__device__ __forceinline__ void warp_max_bits(unsigned long long *p, unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_down_sync(V2C_FULL, v, o);
+    v = w > v ? w : v;
+  }
+  if ((threadIdx.x & 31) == 0 && v) atomicMax(p, v);
+}
 
-__global__ void __launch_bounds__(PT) k_phys(PhysArgs a) {
+// One instantiation per path, so each kernel carries only its own code:
+// MODE = PHYS_OFF (no Newton), PHYS_SPLIT, PHYS_FP64, PHYS_COLLECT; LEARNED =
+// the network's start (split and FP64 only).
+enum { PHYS_OFF = 0, PHYS_SPLIT, PHYS_FP64, PHYS_COLLECT };
+
+template <int MODE, bool LEARNED>
+__global__ void __launch_bounds__(PT, 5) k_phys(PhysArgs a) {
   __shared__ MlpSmem S;
   const Grid &g = a.g;
-  const int guess = a.S.p.newton_guess;
-  const bool collect = a.xs != nullptr;
-  const bool learned = guess == V2C_GUESS_LEARNED && a.mlp != nullptr && !collect;
+  const int guess = MODE == PHYS_OFF ? V2C_GUESS_OFF : V2C_GUESS_PLAIN;
+  const bool collect = MODE == PHYS_COLLECT;
+  const bool learned = LEARNED;
   if (learned) {
     mlp_load_smem(S, a.mlp);
     __syncthreads();
@@ -45,7 +61,7 @@ __global__ void __launch_bounds__(PT) k_phys(PhysArgs a) {
   const long nwarps = (long)gridDim.x * (PT / 32);
   const long n = a.n;
   const v2c_params &P = a.S.p;
-  const bool fp64 = P.newton_precision == V2C_NEWTON_FP64;
+  const bool fp64 = MODE == PHYS_FP64;
   // FP64 scalars of the Newton as float pairs, once per thread
   const ff dt_ff = ff_from_double(P.timestep), W_ff = ff_from_double(P.faultwidth),
            sn_ff = ff_from_double(P.nstress);
@@ -177,7 +193,7 @@ __global__ void __launch_bounds__(PT) k_phys(PhysArgs a) {
       u0 = S.yout[wl][lane][0];
       __syncwarp();
     }
-    unsigned long long it = 0, fb = 0, nc = 0;
+    unsigned long long it = 0, fb = 0, nc = 0, resbits = 0;
     if (solve) {
       RsfResult r = at_floor ? rsf_floor_result(in, A_floor)
                   : fp64     ? rsf_solve64(in, (double)u0, P.newton_rtol, P.newton_maxit)
@@ -191,9 +207,10 @@ __global__ void __launch_bounds__(PT) k_phys(PhysArgs a) {
         r = r2;
       }
       if (!r.ok) nc = 1;
-      a.m.slipv[i] = (float)r.V;
-      if (r.res > 0) atomicMax(a.stat + ST_NEWTON_MAXRES_BITS, (unsigned long long)__double_as_longlong(r.res));
+      a.m.slipv[i] = r.Vf;
+      if (r.res > 0) resbits = (unsigned long long)__double_as_longlong(r.res);
     }
+    warp_max_bits(a.stat + ST_NEWTON_MAXRES_BITS, resbits);
     warp_add(a.stat + ST_NEWTON_ITERS, it);
     warp_add(a.stat + ST_NEWTON_FALLBACK, fb);
     warp_add(a.stat + ST_NEWTON_NONCONV, nc);
@@ -207,7 +224,16 @@ void launch_phys(const PhysArgs &a, cudaStream_t st) {
   long warps = (a.n + 31) / 32;
   long blocks = (warps + PT / 32 - 1) / (PT / 32);
   if (blocks > 152 * 16) blocks = 152 * 16;
-  k_phys<<<(unsigned)blocks, PT, 0, st>>>(a);
+  const v2c_params &p = a.S.p;
+  const bool learned = p.newton_guess == V2C_GUESS_LEARNED && a.mlp != nullptr;
+  const bool fp64 = p.newton_precision == V2C_NEWTON_FP64;
+  const unsigned nb = (unsigned)blocks;
+  if (a.xs) k_phys<PHYS_COLLECT, false><<<nb, PT, 0, st>>>(a);
+  else if (p.newton_guess == V2C_GUESS_OFF) k_phys<PHYS_OFF, false><<<nb, PT, 0, st>>>(a);
+  else if (fp64 && learned) k_phys<PHYS_FP64, true><<<nb, PT, 0, st>>>(a);
+  else if (fp64) k_phys<PHYS_FP64, false><<<nb, PT, 0, st>>>(a);
+  else if (learned) k_phys<PHYS_SPLIT, true><<<nb, PT, 0, st>>>(a);
+  else k_phys<PHYS_SPLIT, false><<<nb, PT, 0, st>>>(a);
 }
 
 }  // namespace v2c

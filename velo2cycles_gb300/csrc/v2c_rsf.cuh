@@ -89,6 +89,7 @@ __device__ __forceinline__ double rsf_eval64(const RsfState &q, double u, double
 
 struct RsfResult {
   double V, res, A;  // slip rate, relative residual, friction term at V
+  float Vf;          // slip rate in FP32 (what a marker stores)
   float phi;
   int it32, itff, it64;
   bool ok;
@@ -114,8 +115,8 @@ __device__ __forceinline__ void rsf_newton64(const RsfState &q, double u, double
     r.it64++;
     r.phi = (float)ph;
     r.A = A;
-    if (rel <= rtol) { r.V = exp(u); r.res = rel; r.ok = true; return; }
-    if (u == floor_u && F >= 0) { r.V = 1e-40; r.res = 0; r.ok = true; return; }
+    if (rel <= rtol) { r.V = exp(u); r.Vf = (float)r.V; r.res = rel; r.ok = true; return; }
+    if (u == floor_u && F >= 0) { r.V = 1e-40; r.Vf = 1e-40f; r.res = 0; r.ok = true; return; }
     if (F < 0) { ulo = u; lo_known = true; } else uhi = u;
     double un = u - F / dF;
     if (!lo_known && dF > 0 && !(un > ulo)) un = floor_u;
@@ -123,6 +124,7 @@ __device__ __forceinline__ void rsf_newton64(const RsfState &q, double u, double
     u = un;
   }
   r.V = exp(u);
+  r.Vf = (float)r.V;
   r.res = rel;
 }
 
@@ -138,7 +140,7 @@ __device__ __forceinline__ RsfResult rsf_solve64(const RsfIn &in, double u0, dou
   RsfState q;
   rsf_setup64(q, in);
   r.phi = in.phio.hi;
-  if (rsf_degenerate(q.Ts, q.klin)) { r.V = 1e-40; r.ok = true; return r; }
+  if (rsf_degenerate(q.Ts, q.klin)) { r.V = 1e-40; r.Vf = 1e-40f; r.ok = true; return r; }
   rsf_newton64(q, u0, rtol, maxit, false, r);
   return r;
 }
@@ -328,7 +330,7 @@ __device__ __forceinline__ RsfResult rsf_solve_split(const RsfIn &in, const Rsf3
     // degenerate in FP32: decided in FP64 as the FP64 form does
     RsfState s;
     rsf_setup64(s, in);
-    if (rsf_degenerate(s.Ts, s.klin)) { r.V = 1e-40; r.ok = true; return r; }
+    if (rsf_degenerate(s.Ts, s.klin)) { r.V = 1e-40; r.Vf = 1e-40f; r.ok = true; return r; }
   }
   float dF32;
   const float u32 = rsf_newton32(q32, u0, floor32, q32.uhi, maxit, r.it32, dF32);
@@ -336,22 +338,29 @@ __device__ __forceinline__ RsfResult rsf_solve_split(const RsfIn &in, const Rsf3
   rsf_setup_ff(q, in);
   const ff floor_u = ff_from_double(RSF_LOG_FLOOR);
   ff u = (u32 <= floor32 + 1e-6f) ? floor_u : ff_f(u32);
+  // the ratio |F|/(F+T*) needs a few significant digits: F and F+T* come
+  // from the float-float evaluation (absolute error ~1e-13 of F+T*), the
+  // ratio is taken in FP32
+  const float rtolf = (float)rtol;
   for (int k = 0; k < 4; k++) {
     ff lhs, phi, A, Vs;
     const ff F = rsf_eval_ff(q, u, lhs, phi, A, Vs);
     r.itff++;
-    const double F64 = ff_to_double(F), l64 = ff_to_double(lhs);
-    const double rel = fabs(F64) / l64;
+    const float rel = fabsf(F.hi) / lhs.hi;
     r.phi = phi.hi;
-    r.A = ff_to_double(A);
-    if (rel <= rtol) {
+    if (rel <= rtolf) {
+      r.A = ff_to_double(A);
       r.V = ff_to_double(Vs) * 5.4210108624275222e-20;
+      r.Vf = Vs.hi * V2C_TWOM64;
       r.res = rel;
       r.ok = true;
       return r;
     }
     const bool at_floor = u.hi == floor_u.hi && u.lo == floor_u.lo;
-    if (at_floor && F.hi >= 0.f) { r.V = 1e-40; r.res = 0; r.ok = true; return r; }
+    if (at_floor && F.hi >= 0.f) {
+      r.V = 1e-40; r.Vf = 1e-40f; r.res = 0; r.ok = true;
+      return r;
+    }
     if (!(dF32 > 0.f)) break;
     u = ff_add_f(u, -F.hi / dF32);
   }
@@ -368,6 +377,7 @@ __device__ __forceinline__ RsfResult rsf_floor_result(const RsfIn &in, float A_f
   r.phi = in.phio.hi;
   r.A = A_floor;
   r.V = 1e-40;
+  r.Vf = 1e-40f;
   r.res = 0;
   r.it32 = 1;
   r.ok = true;
