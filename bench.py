@@ -53,12 +53,17 @@ UNIT = "markers/s"
 
 # algorithmic bytes per marker (FP32/int32 canonical form, each persistent
 # field counted once per read and once per write; node fields spread over
-# the markers per node).  Derivation in the design doc.
-ALG_BYTES = {
-    "m2n": 57 + 4,            # marker reads + phi write
-    "n2m_move": 17 + 48,      # marker reads + writes
-}
-NODE_FIELDS = {"m2n": 18 + 39, "n2m_move": 10 + 24}
+# the markers per node) of the three marker sweeps:
+#   m2n:  marker reads 57 B (cell, u, v, type, T, stresses, strain rates, P,
+#         e, phi, velocities, cohesion, the physics results) + phi write 4 B;
+#         18 node fields read, 39 written
+#   n2m:  reads cell, u, v, type, T 17 B; writes the 9 updated fields 36 B;
+#         19 node fields read, 15 back-scatter sums written
+#   move: reads cell, u, v, type, T, sxx, sxy 25 B; writes cell, u, v, sxx,
+#         sxy 20 B; 5 node fields read (vx, vy, esp and the two pressure-node
+#         velocity averages)
+ALG_BYTES = {"m2n": 57 + 4, "n2m": 17 + 36, "move": 25 + 20}
+NODE_FIELDS = {"m2n": 18 + 39, "n2m": 19 + 15, "move": 5}
 STEP_MARKER_BYTES = 57 + 48
 STEP_NODE_FIELDS = 94
 
@@ -425,7 +430,7 @@ def run_gpu(args, rank: int, world: int) -> None:
     # gather/move sweeps; the per-marker physics + Newton is compute-bound)
     peaks = measured_peaks()
     mpn = n / nn
-    dom = max(("m2n", "n2m_move"), key=lambda k: stage_ms.get(k, 0.0))
+    dom = max(("m2n", "n2m", "move"), key=lambda k: stage_ms.get(k, 0.0))
     alg = n * (ALG_BYTES[dom] + NODE_FIELDS[dom] * 4 / mpn)
     achieved = alg / (stage_ms[dom] * 1e-3) / 1e9
     tr = ncu_traffic(dom)

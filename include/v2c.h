@@ -248,10 +248,11 @@ enum {
   V2C_PROF_C2B,         /* interpolate_center2basic_old                */
   V2C_PROF_BEFORE,      /* compute_before_solve                        */
   V2C_PROF_AFTER,       /* compute_after_solve                         */
-  V2C_PROF_N2M_MOVE,    /* nodes2markers + move sweep                  */
+  V2C_PROF_N2M,         /* nodes2markers: gather, update, back-scatter */
   V2C_PROF_SORT,        /* counting sort by cell                       */
   V2C_PROF_NEWTON,      /* marker physics with the per-marker Newton    */
   V2C_PROF_PHYS,        /* marker physics without the Newton            */
+  V2C_PROF_MOVE,        /* moveandrotatemarkers                        */
   V2C_PROF_N
 };
 int v2c_set_profiling(v2c_ctx *ctx, int on);

@@ -44,6 +44,7 @@ struct v2c_ctx {
   float *d_node = nullptr;
   double *d_node64 = nullptr;  // boundary staging, one FP64 node field
   uint32_t *d_sticky = nullptr;
+  float *d_vxp = nullptr, *d_vyp = nullptr;  // move: velocities at pressure nodes
   // markers
   Markers m{};
   void *marker_mem[32] = {};
@@ -218,6 +219,7 @@ extern "C" int v2c_create(const v2c_params *p, long max_markers, void *cuda_stre
   AL(ctx->d_node, (size_t)V2C_NF_N * ctx->nn);
   AL(ctx->d_node64, ctx->nn);
   AL(ctx->d_sticky, ctx->nn);
+  AL(ctx->d_vxp, ctx->nn); AL(ctx->d_vyp, ctx->nn);
   AL(ctx->d_stat, ST_N);
   ctx->red_cap = 2 + 2 * ((ctx->nn + 255) / 256);
   AL(ctx->d_red, ctx->red_cap);
@@ -255,7 +257,8 @@ extern "C" int v2c_destroy(v2c_ctx *ctx) {
   if (!ctx) return V2C_ERR_ARG;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   void *ptrs[] = {ctx->d_gx, ctx->d_gy, ctx->d_wx, ctx->d_wy, ctx->d_gxf, ctx->d_gyf,
-                  ctx->d_rock, ctx->d_node, ctx->d_node64, ctx->d_sticky, ctx->d_stat, ctx->d_red,
+                  ctx->d_rock, ctx->d_node, ctx->d_node64, ctx->d_sticky, ctx->d_vxp, ctx->d_vyp,
+                  ctx->d_stat, ctx->d_red,
                   ctx->sb.counts, ctx->sb.start, ctx->sb.slot, ctx->sb.tmp, ctx->sb.perm,
                   ctx->sb.blocksum, ctx->d_stage64, ctx->d_stage64b, ctx->bc_mem,
                   ctx->d_bc_scratch};
@@ -774,23 +777,30 @@ static int n2m_move(v2c_ctx *ctx, int do_n2m, int do_move) {
   a.start = ctx->sb.start;
   a.stat = ctx->d_stat;
   a.gyf = ctx->d_gyf;
+  a.vxp = ctx->d_vxp;
+  a.vyp = ctx->d_vyp;
+  a.n = ctx->n;
   a.TX = pick_tx(ctx);
-  a.do_n2m = do_n2m;
-  a.do_move = do_move;
-  {
-    Prof pr(ctx, V2C_PROF_N2M_MOVE);
-    launch_n2m_move(a, st);
+  a.do_n2m = 1;
+  if (do_n2m) {
+    Prof pr(ctx, V2C_PROF_N2M);
+    launch_n2m(a, st);
+    ctx->launches += 1;
   }
-  ctx->launches += 1;
-  CK(cudaGetLastError());
-  swap_positions(ctx);
   if (do_move) {
+    {
+      Prof pr(ctx, V2C_PROF_MOVE);
+      launch_move(a, st);
+      ctx->launches += ctx->n > 0 ? 2 : 1;
+    }
+    CK(cudaGetLastError());
+    swap_positions(ctx);
     // next step's order: counting sort of the new cells
     Prof pr(ctx, V2C_PROF_SORT);
     launch_sort(ctx->m.cell_in, ctx->n, ctx->ncell, ctx->sb, ctx->d_stat, st);
     ctx->launches += ctx->n > 0 ? 6 : 3;
-    CK(cudaGetLastError());
   }
+  CK(cudaGetLastError());
   return V2C_OK;
 }
 

@@ -91,10 +91,15 @@ struct N2MArgs {
   const int32_t *start;
   unsigned long long *stat;
   const float *gyf;  // FP32 line positions (coarse depth test)
+  float *vxp, *vyp;  // velocities averaged to pressure nodes [nn] (scratch)
+  long n;            // markers
   int TX;
-  int do_n2m, do_move;
+  int do_n2m;
 };
-void launch_n2m_move(const N2MArgs &a, cudaStream_t st);
+// nodes2markers: gather, marker update, back-scatter (cell-column tiles)
+void launch_n2m(const N2MArgs &a, cudaStream_t st);
+// moveandrotatemarkers: one thread per marker, new positions to *_out
+void launch_move(const N2MArgs &a, cudaStream_t st);
 
 // upload / download helpers
 void launch_assign(const Grid &g, const double *x, const double *y, long n, Markers m,

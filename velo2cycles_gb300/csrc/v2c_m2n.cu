@@ -77,14 +77,14 @@ __device__ __forceinline__ void stage(const M2NArgs &a, Smem &sm, int s, int k) 
   sm.p[P_U][k] = u;
   sm.p[P_V][k] = v;
   sm.p[P_NU][k] = mnu;
-  sm.p[P_NUG][k] = mnu / a.R(RK_GG, t);
+  sm.p[P_NUG][k] = mnu * a.R(RK_INV_GG, t);
   sm.p[P_E][k] = a.m.e[idx];
   sm.p[P_SXY][k] = a.m.sxy[idx];
   sm.p[P_EXY][k] = a.m.exy[idx];
   sm.p[P_COH][k] = a.m.coh[idx];
   sm.p[P_PHI][k] = a.m.phi[idx];
   sm.p[P_RO][k] = a.S.p.densimod ? a.m.mro[idx] : a.R(RK_RO, t);
-  sm.p[P_ET][k] = bb / (1.f - bb * (T - 298.15f));  // dencalcomp adiabatic term
+  sm.p[P_ET][k] = __fdividef(bb, 1.f - bb * (T - 298.15f));  // dencalcomp adiabatic term
   sm.p[P_HT][k] = a.R(RK_HT, t);
   sm.p[P_CP][k] = a.R(RK_CP, t);
   sm.p[P_KT][k] = a.m.mkt[idx];
@@ -96,9 +96,10 @@ __device__ __forceinline__ void stage(const M2NArgs &a, Smem &sm, int s, int k) 
   sm.p[P_VY][k] = a.m.vy[idx];
 }
 
-// calc_frictionpara_nodes (calc_RSF.c:298-350), FP64
-__device__ void friction_node(const v2c_params &p, double x, double y, double &mu, double &a,
-                              double &b, double &L, double &V0) {
+// calc_frictionpara_nodes (calc_RSF.c:298-350), FP64; out of line, taken
+// only for nodes within 1 m of the frictional band (see node_friction)
+__device__ __noinline__ void friction_node(const v2c_params &p, double x, double y, double &mu,
+                                           double &a, double &b, double &L, double &V0) {
   double d = y - (p.fault_y + p.fault_slope * x);
   double radius = d >= 0 ? d : -d;
   if (radius <= p.fault_hw) {
@@ -119,6 +120,23 @@ __device__ void friction_node(const v2c_params &p, double x, double y, double &m
   } else {
     mu = 0.6; a = p.a_hr; b = p.b_hr; L = p.L_hr; V0 = p.V0_hr;
   }
+}
+
+// Friction parameters of node (ci, j): outside the band (the FP32 distance
+// clears the half-width by more than 1 m, far above its rounding) they are
+// the constants of the far field; near the band the FP64 rule decides.
+__device__ __forceinline__ void node_friction(const M2NArgs &a, int ci, int j, float &mu,
+                                              float &fa, float &fb, float &fL, float &fV0) {
+  const v2c_params &p = a.S.p;
+  const float xf = __ldg(a.gxf + ci), yf = __ldg(a.gyf + j);
+  const float rad = fabsf(yf - ((float)p.fault_y + (float)p.fault_slope * xf));
+  if (rad > (float)p.fault_hw + 1.0f) {
+    mu = 0.6f; fa = (float)p.a_hr; fb = (float)p.b_hr; fL = (float)p.L_hr; fV0 = (float)p.V0_hr;
+    return;
+  }
+  double dmu, da, db, dL, dV0;
+  friction_node(p, a.g.gx[ci], a.g.gy[j], dmu, da, db, dL, dV0);
+  mu = (float)dmu; fa = (float)da; fb = (float)db; fL = (float)dL; fV0 = (float)dV0;
 }
 
 // role 0 / role 1 accumulation into a named register array
@@ -255,8 +273,8 @@ __global__ void __launch_bounds__(NTH, 6) k_m2n(M2NArgs a) {
       const float ss = cur[7].value();
       const bool interior = ci >= 1 && j >= 1 && ci < g.xn - 1 && j < g.yn - 1;
       if (ss != 0.f && interior) {
-        float phin = cur[6].value() / ss, sxyen = cur[3].value() / ss;
-        float exyen = cur[4].value() / ss, pen = cur[2].value() / ss;
+        float phin = __fdividef(cur[6].value(), ss), sxyen = __fdividef(cur[3].value(), ss);
+        float exyen = __fdividef(cur[4].value(), ss), pen = __fdividef(cur[2].value(), ss);
         float phis, sxye, exye, pe;
         if (antid) {
           phis = N.f(V2C_NF_PHIS_IT)[m3] + (phin - N.f(V2C_NF_PHIE)[m3]);
@@ -267,7 +285,7 @@ __global__ void __launch_bounds__(NTH, 6) k_m2n(M2NArgs a) {
           phis = phin; sxye = sxyen; exye = exyen; pe = pen;
         }
         if (pe < 0.f) pe = 0.f;
-        float nu_m2c = cur[0].value() / ss;
+        float nu_m2c = __fdividef(cur[0].value(), ss);
         N.f(V2C_NF_PHIN)[m3] = phin;
         N.f(V2C_NF_SXYEN)[m3] = sxyen;
         N.f(V2C_NF_EXYEN)[m3] = exyen;
@@ -276,9 +294,9 @@ __global__ void __launch_bounds__(NTH, 6) k_m2n(M2NArgs a) {
         N.f(V2C_NF_SXYE)[m3] = sxye;
         N.f(V2C_NF_EXYE)[m3] = exye;
         N.f(V2C_NF_PE)[m3] = pe;
-        N.f(V2C_NF_COHESION)[m3] = cur[5].value() / ss;
+        N.f(V2C_NF_COHESION)[m3] = __fdividef(cur[5].value(), ss);
         N.f(V2C_NF_NU_M2C)[m3] = nu_m2c;
-        N.f(V2C_NF_GG)[m3] = nu_m2c / (cur[1].value() / ss);
+        N.f(V2C_NF_GG)[m3] = __fdividef(nu_m2c, __fdividef(cur[1].value(), ss));
       } else {
         N.f(V2C_NF_PHIN)[m3] = 0; N.f(V2C_NF_SXYEN)[m3] = 0; N.f(V2C_NF_EXYEN)[m3] = 0;
         N.f(V2C_NF_PHIS)[m3] = 0; N.f(V2C_NF_SXYE)[m3] = 0; N.f(V2C_NF_EXYE)[m3] = 0;
@@ -287,14 +305,14 @@ __global__ void __launch_bounds__(NTH, 6) k_m2n(M2NArgs a) {
     } else if (role == 1) {
       const float ss = cur[6].value();
       const bool interior = ci >= 1 && j >= 1 && ci < g.xn - 1 && j < g.yn - 1;
-      double mu = 0, fa = 0, fb = 0, fL = 0, fV0 = 0;
-      if (ss != 0.f && interior) friction_node(a.S.p, g.gx[ci], g.gy[j], mu, fa, fb, fL, fV0);
-      N.f(V2C_NF_MUS_S)[m3] = (float)mu; N.f(V2C_NF_AS)[m3] = (float)fa; N.f(V2C_NF_BS)[m3] = (float)fb;
-      N.f(V2C_NF_LS)[m3] = (float)fL; N.f(V2C_NF_V0S)[m3] = (float)fV0;
+      float mu = 0.f, fa = 0.f, fb = 0.f, fL = 0.f, fV0 = 0.f;
+      if (ss != 0.f && interior) node_friction(a, ci, j, mu, fa, fb, fL, fV0);
+      N.f(V2C_NF_MUS_S)[m3] = mu; N.f(V2C_NF_AS)[m3] = fa; N.f(V2C_NF_BS)[m3] = fb;
+      N.f(V2C_NF_LS)[m3] = fL; N.f(V2C_NF_V0S)[m3] = fV0;
       if (ss != 0.f) {
-        N.f(V2C_NF_RO)[m3] = cur[0].value() / ss; N.f(V2C_NF_ET)[m3] = cur[1].value() / ss;
-        N.f(V2C_NF_HT)[m3] = cur[2].value() / ss; N.f(V2C_NF_CP)[m3] = cur[3].value() / ss;
-        N.f(V2C_NF_KT)[m3] = cur[4].value() / ss; N.f(V2C_NF_TK)[m3] = cur[5].value() / ss;
+        N.f(V2C_NF_RO)[m3] = __fdividef(cur[0].value(), ss); N.f(V2C_NF_ET)[m3] = __fdividef(cur[1].value(), ss);
+        N.f(V2C_NF_HT)[m3] = __fdividef(cur[2].value(), ss); N.f(V2C_NF_CP)[m3] = __fdividef(cur[3].value(), ss);
+        N.f(V2C_NF_KT)[m3] = __fdividef(cur[4].value(), ss); N.f(V2C_NF_TK)[m3] = __fdividef(cur[5].value(), ss);
       } else {
         N.f(V2C_NF_RO)[m3] = 0; N.f(V2C_NF_ET)[m3] = 0; N.f(V2C_NF_HT)[m3] = 0;
         N.f(V2C_NF_CP)[m3] = 0; N.f(V2C_NF_KT)[m3] = 0; N.f(V2C_NF_TK)[m3] = 0;
@@ -314,8 +332,8 @@ __global__ void __launch_bounds__(NTH, 6) k_m2n(M2NArgs a) {
         const long mc = (long)(ci + 1) * g.yn + (j + 1);
         const float s1 = cur[5].value();
         if (s1 != 0.f) {
-          float sxxen = cur[2].value() / s1, sppen = cur[4].value() / s1;
-          float exxen = cur[3].value() / s1;
+          float sxxen = __fdividef(cur[2].value(), s1), sppen = __fdividef(cur[4].value(), s1);
+          float exxen = __fdividef(cur[3].value(), s1);
           float sxxe, sppe, exxe;
           if (antid) {
             sxxe = N.f(V2C_NF_SXX)[mc] + (sxxen - N.f(V2C_NF_SXXEE)[mc]);
@@ -326,12 +344,12 @@ __global__ void __launch_bounds__(NTH, 6) k_m2n(M2NArgs a) {
           }
           if (a.S.p.timesum == 0 && a.S.p.reloadfromDP == 0 && a.S.p.compressiblemode == 1)
             sppe = (float)a.S.p.nstress;
-          float nd = cur[0].value() / s1;
+          float nd = __fdividef(cur[0].value(), s1);
           N.f(V2C_NF_SXXEN)[mc] = sxxen; N.f(V2C_NF_SPPEN)[mc] = sppen;
           N.f(V2C_NF_EXXEN)[mc] = exxen; N.f(V2C_NF_SXXE)[mc] = sxxe;
           N.f(V2C_NF_SPPE)[mc] = sppe; N.f(V2C_NF_EXXE)[mc] = exxe;
           N.f(V2C_NF_ND_M2C)[mc] = nd;
-          N.f(V2C_NF_GD)[mc] = nd / (cur[1].value() / s1);
+          N.f(V2C_NF_GD)[mc] = nd / (__fdividef(cur[1].value(), s1));
           N.f(V2C_NF_BM)[mc] = 50e9f;
           N.f(V2C_NF_DRO)[mc] = 0; N.f(V2C_NF_DRP)[mc] = 0;
         } else {

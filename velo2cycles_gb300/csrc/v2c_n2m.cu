@@ -56,26 +56,16 @@ __device__ __forceinline__ void settle(const Grid &g, Pos &p, unsigned long long
 }
 
 // allinteri's arithmetic (interpolation.c:1688-1758) from precomputed
-// stencils: spin at basic nodes (mb), velocities averaged to the pressure
-// node (mc), blended with the staggered velocities VXs, VYs by xrat
-__device__ __forceinline__ void allinteri_from(const Nodes &N, long yn, long mb, float eb,
-                                               float nb, long mc, float ec, float nc, float VXs,
-                                               float VYs, float xrat, float &VX, float &VY,
-                                               float &ESP) {
+// stencils: spin at basic nodes (mb), the velocities averaged to pressure
+// nodes (vxp, vyp, see k_vel_pnodes) at the pressure stencil (mc), blended
+// with the staggered velocities VXs, VYs by xrat
+__device__ __forceinline__ void allinteri_from(const Nodes &N, const float *vxp, const float *vyp,
+                                               long yn, long mb, float eb, float nb, long mc,
+                                               float ec, float nc, float VXs, float VYs,
+                                               float xrat, float &VX, float &VY, float &ESP) {
   ESP = bil(N.f(V2C_NF_ESP), mb, yn, eb, nb);
-  const float *vx = N.f(V2C_NF_VX), *vy = N.f(V2C_NF_VY);
-  const float d0 = (1.f - ec) * (1.f - nc), d1 = (1.f - ec) * nc, d2 = ec * (1.f - nc),
-              d3 = ec * nc;
-  const float vxm1 = __ldg(vx + mc - 1), vxc = __ldg(vx + mc);
-  VX = (d0 * (vxm1 + __ldg(vx + mc - yn - 1)) + d1 * (vxc + __ldg(vx + mc - yn)) +
-        d2 * (__ldg(vx + mc + yn - 1) + vxm1) + d3 * (__ldg(vx + mc + yn) + vxc)) *
-       0.5f * (1.f - xrat);
-  const float vyc = __ldg(vy + mc), vyu = __ldg(vy + mc - yn);
-  VY = (d0 * (vyu + __ldg(vy + mc - yn - 1)) + d1 * (__ldg(vy + mc - yn + 1) + vyu) +
-        d2 * (vyc + __ldg(vy + mc - 1)) + d3 * (__ldg(vy + mc + 1) + vyc)) *
-       0.5f * (1.f - xrat);
-  VX += VXs * xrat;
-  VY += VYs * xrat;
+  VX = bil(vxp, mc, yn, ec, nc) * (1.f - xrat) + VXs * xrat;
+  VY = bil(vyp, mc, yn, ec, nc) * (1.f - xrat) + VYs * xrat;
 }
 
 // allinteri's weight of the staggered velocities: 2/3, or 1 in the outer
@@ -92,8 +82,9 @@ __device__ __forceinline__ float allinteri_xrat(const Grid &g, int ix, int iy, f
 }
 
 // allinteri (interpolation.c:1688-1758): velocity and spin at a point
-__device__ void allinteri(const Grid &g, const Nodes &N, Pos p, float &VX, float &VY,
-                          float &ESP) {
+__device__ __forceinline__ void allinteri(const Grid &g, const Nodes &N, const float *vxp,
+                                          const float *vyp, Pos p, float &VX, float &VY,
+                                          float &ESP) {
   // clamp into the model
   const float wx = __ldg(g.wx + p.ix), wy = __ldg(g.wy + p.iy);
   if (p.ix == 0 && p.X < 0.f) p.X = 0.f;
@@ -111,7 +102,7 @@ __device__ void allinteri(const Grid &g, const Nodes &N, Pos p, float &VX, float
   const float VXs = bil(N.f(V2C_NF_VX), m3, yn, e, n);
   m3 = stencil_vy(g, ax, ay, p.X < 0.5f * wx, g.yn - 2, e, n);
   const float VYs = bil(N.f(V2C_NF_VY), m3, yn, e, n);
-  allinteri_from(N, yn, mb, eb, nb, mc, ec, nc, VXs, VYs, xrat, VX, VY, ESP);
+  allinteri_from(N, vxp, vyp, yn, mb, eb, nb, mc, ec, nc, VXs, VYs, xrat, VX, VY, ESP);
 }
 
 // basic-node back-scatter into a named register array
@@ -122,7 +113,7 @@ __device__ void allinteri(const Grid &g, const Nodes &N, Pos p, float &VX, float
     A[4].add(w);                                                        \
   } while (0)
 
-__global__ void __launch_bounds__(NTH, 5) k_n2m_move(N2MArgs a) {
+__global__ void __launch_bounds__(NTH, 6) k_n2m(N2MArgs a) {
   __shared__ Smem sm;
   const Grid &g = a.g;
   const Nodes &N = a.N;
@@ -223,15 +214,6 @@ __global__ void __launch_bounds__(NTH, 5) k_n2m_move(N2MArgs a) {
             sm.q[Q_MRO][k] = a.R(RK_RO, t);
           }
           if (!owned) continue;
-          // first allinteri evaluation of the move, at the marker itself:
-          // allinteri's clamped point is the gather's (uc, vc), so its
-          // stencils and staggered velocities are the gather's
-          float vx1 = 0.f, vy1 = 0.f, sp1 = 0.f;
-          if (a.do_move)
-            allinteri_from(N, yn, mb, eb, nb, mc, ec, ncc, VX, VY,
-                           allinteri_xrat(g, ix, iy, uc * wxc, vc * wyc, wxc, wyc), vx1, vy1,
-                           sp1);
-
           // ------------------------------------- marker update (:943-1011)
           const bool in_strict = (ix > 0 || u > 0.f) && (ix < g.ncx - 1 || u < 1.f) &&
                                  (iy > 0 || v > 0.f) && (iy < g.ncy - 1 || v < 1.f);
@@ -267,106 +249,11 @@ __global__ void __launch_bounds__(NTH, 5) k_n2m_move(N2MArgs a) {
             }
           }
 
-          // ------------------------------------------ move and rotate
-          int nix = ix, niy = iy;
-          float nu_ = u, nv_ = v;
-          uint8_t flags = a.m.flags[idx];
-          if (a.do_move && !a.R(RK_IM, t) && (in_grid || P.outgrid != 1)) {
-            const float dt = a.S.dt;
-            Pos p0{ix, iy, u * wxc, v * wyc};
-            float vx0, vy0, sp0;
-            if (P.markmod == 1) {
-              vx0 = vx1; vy0 = vy1; sp0 = sp1;
-            } else {
-              float vx2, vy2, sp2, vx3, vy3, sp3, vx4, vy4, sp4;
-              Pos p = p0;
-              p.X += vx1 * dt / 2.f; p.Y += vy1 * dt / 2.f;
-              settle(g, p, a.stat);
-              allinteri(g, N, p, vx2, vy2, sp2);
-              p = p0;
-              p.X += vx2 * dt / 2.f; p.Y += vy2 * dt / 2.f;
-              settle(g, p, a.stat);
-              allinteri(g, N, p, vx3, vy3, sp3);
-              p = p0;
-              p.X += vx3 * dt; p.Y += vy3 * dt;
-              settle(g, p, a.stat);
-              allinteri(g, N, p, vx4, vy4, sp4);
-              vx0 = (vx1 + 2.f * vx2 + 2.f * vx3 + vx4) / 6.f;
-              vy0 = (vy1 + 2.f * vy2 + 2.f * vy3 + vy4) / 6.f;
-              sp0 = (P.markmod == 2) ? (sp1 + 2.f * sp2 + 2.f * sp3 + sp4) / 6.f : sp1;
-            }
-            if (P.outgrid == 2) {
-              if ((ix == 0 && u < 0.f) || (ix == g.ncx - 1 && u > 1.f)) vy0 = 0.f;
-              if ((iy == 0 && v < 0.f) || (iy == g.ncy - 1 && v > 1.f)) vx0 = 0.f;
-            }
-            // new position: in offset space while the marker stays in its
-            // cell (one FP32 rounding of u), else walked in metres
-            float du = dt * vx0 / wxc, dv = dt * vy0 / wyc;
-            nu_ = u + du;
-            nv_ = v + dv;
-            nix = ix;
-            niy = iy;
-            const bool interior_x = ix > 0 && ix < g.ncx - 1, interior_y = iy > 0 && iy < g.ncy - 1;
-            if (!(nu_ >= 0.f && nu_ < 1.f && (interior_x || (u >= 0.f && u <= 1.f)))) {
-              Pos p{ix, 0, nu_ * wxc, 0.f};
-              settle(g, p, a.stat);
-              nix = p.ix;
-              const float nwx = __ldg(g.wx + nix);
-              nu_ = p.X / nwx;
-              if (p.X < nwx && nu_ >= 1.f) nu_ = nextafterf(1.f, 0.f);
-              if (p.X < 0.5f * nwx && nu_ >= 0.5f) nu_ = nextafterf(0.5f, 0.f);
-              if (p.X > 0.5f * nwx && nu_ <= 0.5f) nu_ = nextafterf(0.5f, 1.f);
-              if (p.X > nwx && nu_ <= 1.f) nu_ = nextafterf(1.f, 2.f);
-            }
-            if (!(nv_ >= 0.f && nv_ < 1.f && (interior_y || (v >= 0.f && v <= 1.f)))) {
-              Pos p{0, iy, 0.f, nv_ * wyc};
-              settle(g, p, a.stat);
-              niy = p.iy;
-              const float nwy = __ldg(g.wy + niy);
-              nv_ = p.Y / nwy;
-              if (p.Y < nwy && nv_ >= 1.f) nv_ = nextafterf(1.f, 0.f);
-              if (p.Y < 0.5f * nwy && nv_ >= 0.5f) nv_ = nextafterf(0.5f, 0.f);
-              if (p.Y > 0.5f * nwy && nv_ <= 0.5f) nv_ = nextafterf(0.5f, 1.f);
-              if (p.Y > nwy && nv_ <= 1.f) nv_ = nextafterf(1.f, 2.f);
-            }
-            (void)interior_x;
-            // stress rotation, moveandrotatemarkers.c:58-76
-            sp0 *= dt;
-            if (P.stoksmod == 1) {
-              float s, cth;
-              sincosf(sp0, &s, &cth);
-              const float s2 = 2.f * s * cth, c2 = cth * cth - s * s;  // sin, cos of 2 sp0
-              float r1 = msxx * cth * cth - msxx * s * s + msxy * s2;
-              float r3 = 0.5f * (-msxx - msxx) * s2 + msxy * c2;
-              msxx = r1; msxy = r3;
-            } else if (P.stoksmod == 2) {
-              float r1 = msxx + msxy * 2.f * sp0;
-              float r3 = msxy + 0.5f * (-msxx - msxx) * 2.f * sp0;
-              msxx = r1; msxy = r3;
-            }
-            // markers coming from depth, out-of-grid reset (:79-87); the
-            // FP64 position only when the FP32 one is within 1 m of zdeep
-            if (vy0 < 0.f && tk < (float)P.tdeep &&
-                __ldg(a.gyf + niy) + nv_ * __ldg(g.wy + niy) > (float)P.zdeep - 1.f - 1e-6f * fabsf((float)P.zdeep)) {
-              const double ynew = g.gy[niy] + (double)nv_ * (g.gy[niy + 1] - g.gy[niy]);
-              if (ynew > P.zdeep) tk = (float)P.tdeep;
-            }
-            const bool out = (nix == 0 && nu_ < 0.f) || (nix == g.ncx - 1 && nu_ > 1.f) ||
-                             (niy == 0 && nv_ < 0.f) || (niy == g.ncy - 1 && nv_ > 1.f);
-            if (out) {
-              tk = 0.f; me = 0.f; flags |= MFLAG_RESET;
-              atomicAdd(a.stat + ST_OUT_OF_GRID, 1ull);
-            }
-            changed = true;
-          }
-          a.m.cell_out[idx] = nix * ncy + niy;
-          a.m.u_out[idx] = nu_;
-          a.m.v_out[idx] = nv_;
           if (changed) {
             a.m.phi[idx] = phi; a.m.exx[idx] = mexx; a.m.exy[idx] = mexy;
             a.m.sxx[idx] = msxx; a.m.sxy[idx] = msxy; a.m.p[idx] = mp;
             a.m.vx[idx] = mvx; a.m.vy[idx] = mvy; a.m.e[idx] = me;
-            a.m.tk[idx] = tk; a.m.flags[idx] = flags;
+            a.m.tk[idx] = tk;
           }
         }
         if (!backscatter) continue;
@@ -438,8 +325,8 @@ __global__ void __launch_bounds__(NTH, 5) k_n2m_move(N2MArgs a) {
       N.f(V2C_NF_PHISUM)[m3] = ph; N.f(V2C_NF_SXYSUM)[m3] = sy;
       N.f(V2C_NF_EXYSUM)[m3] = ey; N.f(V2C_NF_ESUM)[m3] = es; N.f(V2C_NF_WTPHISUM)[m3] = w;
       if (w != 0.f && ci >= 1 && j >= 1 && ci < g.xn - 1 && j < g.yn - 1) {
-        N.f(V2C_NF_PHIE)[m3] = ph / w; N.f(V2C_NF_SXYEE)[m3] = sy / w;
-        N.f(V2C_NF_EXYEE)[m3] = ey / w; N.f(V2C_NF_PEE)[m3] = es / w;
+        N.f(V2C_NF_PHIE)[m3] = __fdividef(ph, w); N.f(V2C_NF_SXYEE)[m3] = __fdividef(sy, w);
+        N.f(V2C_NF_EXYEE)[m3] = __fdividef(ey, w); N.f(V2C_NF_PEE)[m3] = __fdividef(es, w);
       }
     } else if (role == 1) {
       if (ci < g.ncx && j < ncy) {
@@ -449,8 +336,8 @@ __global__ void __launch_bounds__(NTH, 5) k_n2m_move(N2MArgs a) {
         N.f(V2C_NF_PSUM)[mc] = ps; N.f(V2C_NF_SXXSUM)[mc] = sx;
         N.f(V2C_NF_EXXSUM)[mc] = ex; N.f(V2C_NF_WTSXXSUM)[mc] = w;
         if (w != 0.f) {
-          N.f(V2C_NF_SPPEE)[mc] = ps / w; N.f(V2C_NF_SXXEE)[mc] = sx / w;
-          N.f(V2C_NF_EXXEE)[mc] = ex / w;
+          N.f(V2C_NF_SPPEE)[mc] = __fdividef(ps, w); N.f(V2C_NF_SXXEE)[mc] = __fdividef(sx, w);
+          N.f(V2C_NF_EXXEE)[mc] = __fdividef(ex, w);
         }
       }
       if (ci == 0 || j == 0) {
@@ -460,20 +347,168 @@ __global__ void __launch_bounds__(NTH, 5) k_n2m_move(N2MArgs a) {
     } else if (role == 2) {
       const float w = cur[2].value(), vs = cur[0].value(), mr = cur[1].value();
       N.f(V2C_NF_VXSUM)[m3] = vs; N.f(V2C_NF_MRX0)[m3] = mr; N.f(V2C_NF_WTVXSUM)[m3] = w;
-      if (w != 0.f) N.f(V2C_NF_MVXE)[m3] = vs / mr;
+      if (w != 0.f) N.f(V2C_NF_MVXE)[m3] = __fdividef(vs, mr);
     } else {
       const float w = cur[2].value(), vs = cur[0].value(), mr = cur[1].value();
       N.f(V2C_NF_VYSUM)[m3] = vs; N.f(V2C_NF_MRY0)[m3] = mr; N.f(V2C_NF_WTVYSUM)[m3] = w;
-      if (w != 0.f) N.f(V2C_NF_MVYE)[m3] = vs / mr;
+      if (w != 0.f) N.f(V2C_NF_MVYE)[m3] = __fdividef(vs, mr);
     }
+  }
+}
+
+// ----------------------------------------------------------- the move
+// Velocities averaged to the pressure node m (allinteri's pairs,
+// interpolation.c:1730-1745): VXP[m] = (vx[m-1] + vx[m-yn-1])/2,
+// VYP[m] = (vy[m-yn] + vy[m-yn-1])/2; nodes of the first row or column have
+// no pressure node and get 0 (the pressure stencil never reaches them).
+__global__ void k_vel_pnodes(Grid g, const float *vx, const float *vy, float *vxp, float *vyp) {
+  const long m = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (m >= g.nn) return;
+  const long yn = g.yn;
+  const long ix = m / yn, iy = m - ix * yn;
+  if (ix < 1 || iy < 1) {
+    vxp[m] = 0.f;
+    vyp[m] = 0.f;
+    return;
+  }
+  vxp[m] = 0.5f * (__ldg(vx + m - 1) + __ldg(vx + m - yn - 1));
+  vyp[m] = 0.5f * (__ldg(vy + m - yn) + __ldg(vy + m - yn - 1));
+}
+
+// moveandrotatemarkers (moveandrotatemarkers.c:1-178), one thread per
+// marker in cell order: Euler or RK4 through allinteri, stress rotation,
+// markers from depth, out-of-grid reset.  New positions go to the second
+// position buffer.
+__global__ void __launch_bounds__(256) k_move(N2MArgs a) {
+  const Grid &g = a.g;
+  const Nodes &N = a.N;
+  const v2c_params &P = a.S.p;
+  const int ncy = g.ncy;
+  const float dt = a.S.dt;
+  for (long s = blockIdx.x * (long)blockDim.x + threadIdx.x; s < a.n;
+       s += (long)gridDim.x * blockDim.x) {
+    const int idx = __ldg(a.perm + s);
+    const int c = a.m.cell_in[idx];
+    const int ix = c / ncy, iy = c - ix * ncy;
+    const float u = a.m.u_in[idx], v = a.m.v_in[idx];
+    const int t = a.m.type[idx];
+    const bool in_grid = (ix > 0 || u >= 0.f) && (ix < g.ncx - 1 || u <= 1.f) &&
+                         (iy > 0 || v >= 0.f) && (iy < g.ncy - 1 || v <= 1.f);
+    int nix = ix, niy = iy;
+    float nu_ = u, nv_ = v;
+    if (!a.R(RK_IM, t) && (in_grid || P.outgrid != 1)) {
+      const float wxc = __ldg(g.wx + ix), wyc = __ldg(g.wy + iy);
+      const Pos p0{ix, iy, u * wxc, v * wyc};
+      float vx0, vy0, sp0, vx1, vy1, sp1;
+      allinteri(g, N, a.vxp, a.vyp, p0, vx1, vy1, sp1);
+      if (P.markmod == 1) {
+        vx0 = vx1; vy0 = vy1; sp0 = sp1;
+      } else {
+        float vx2, vy2, sp2, vx3, vy3, sp3, vx4, vy4, sp4;
+        Pos p = p0;
+        p.X += vx1 * dt / 2.f; p.Y += vy1 * dt / 2.f;
+        settle(g, p, a.stat);
+        allinteri(g, N, a.vxp, a.vyp, p, vx2, vy2, sp2);
+        p = p0;
+        p.X += vx2 * dt / 2.f; p.Y += vy2 * dt / 2.f;
+        settle(g, p, a.stat);
+        allinteri(g, N, a.vxp, a.vyp, p, vx3, vy3, sp3);
+        p = p0;
+        p.X += vx3 * dt; p.Y += vy3 * dt;
+        settle(g, p, a.stat);
+        allinteri(g, N, a.vxp, a.vyp, p, vx4, vy4, sp4);
+        vx0 = (vx1 + 2.f * vx2 + 2.f * vx3 + vx4) / 6.f;
+        vy0 = (vy1 + 2.f * vy2 + 2.f * vy3 + vy4) / 6.f;
+        sp0 = (P.markmod == 2) ? (sp1 + 2.f * sp2 + 2.f * sp3 + sp4) / 6.f : sp1;
+      }
+      if (P.outgrid == 2) {
+        if ((ix == 0 && u < 0.f) || (ix == g.ncx - 1 && u > 1.f)) vy0 = 0.f;
+        if ((iy == 0 && v < 0.f) || (iy == g.ncy - 1 && v > 1.f)) vx0 = 0.f;
+      }
+      // new position: in offset space while the marker stays in its cell
+      // (one FP32 rounding of u), else walked in metres
+      nu_ = u + dt * vx0 / wxc;
+      nv_ = v + dt * vy0 / wyc;
+      const bool interior_x = ix > 0 && ix < g.ncx - 1, interior_y = iy > 0 && iy < g.ncy - 1;
+      if (!(nu_ >= 0.f && nu_ < 1.f && (interior_x || (u >= 0.f && u <= 1.f)))) {
+        Pos p{ix, 0, nu_ * wxc, 0.f};
+        settle(g, p, a.stat);
+        nix = p.ix;
+        const float nwx = __ldg(g.wx + nix);
+        nu_ = p.X / nwx;
+        if (p.X < nwx && nu_ >= 1.f) nu_ = nextafterf(1.f, 0.f);
+        if (p.X < 0.5f * nwx && nu_ >= 0.5f) nu_ = nextafterf(0.5f, 0.f);
+        if (p.X > 0.5f * nwx && nu_ <= 0.5f) nu_ = nextafterf(0.5f, 1.f);
+        if (p.X > nwx && nu_ <= 1.f) nu_ = nextafterf(1.f, 2.f);
+      }
+      if (!(nv_ >= 0.f && nv_ < 1.f && (interior_y || (v >= 0.f && v <= 1.f)))) {
+        Pos p{0, iy, 0.f, nv_ * wyc};
+        settle(g, p, a.stat);
+        niy = p.iy;
+        const float nwy = __ldg(g.wy + niy);
+        nv_ = p.Y / nwy;
+        if (p.Y < nwy && nv_ >= 1.f) nv_ = nextafterf(1.f, 0.f);
+        if (p.Y < 0.5f * nwy && nv_ >= 0.5f) nv_ = nextafterf(0.5f, 0.f);
+        if (p.Y > 0.5f * nwy && nv_ <= 0.5f) nv_ = nextafterf(0.5f, 1.f);
+        if (p.Y > nwy && nv_ <= 1.f) nv_ = nextafterf(1.f, 2.f);
+      }
+      // stress rotation, moveandrotatemarkers.c:58-76
+      float msxx = a.m.sxx[idx], msxy = a.m.sxy[idx];
+      sp0 *= dt;
+      if (P.stoksmod == 1) {
+        float sn, cs;
+        sincosf(sp0, &sn, &cs);
+        const float s2 = 2.f * sn * cs, c2 = cs * cs - sn * sn;  // sin, cos of 2 sp0
+        const float r1 = msxx * cs * cs - msxx * sn * sn + msxy * s2;
+        const float r3 = 0.5f * (-msxx - msxx) * s2 + msxy * c2;
+        msxx = r1; msxy = r3;
+      } else if (P.stoksmod == 2) {
+        const float r1 = msxx + msxy * 2.f * sp0;
+        const float r3 = msxy + 0.5f * (-msxx - msxx) * 2.f * sp0;
+        msxx = r1; msxy = r3;
+      }
+      a.m.sxx[idx] = msxx;
+      a.m.sxy[idx] = msxy;
+      // markers coming from depth, out-of-grid reset (:79-87); the FP64
+      // position only when the FP32 one is within 1 m of zdeep
+      float tk = a.m.tk[idx];
+      const float tk0 = tk;
+      if (vy0 < 0.f && tk < (float)P.tdeep &&
+          __ldg(a.gyf + niy) + nv_ * __ldg(g.wy + niy) >
+              (float)P.zdeep - 1.f - 1e-6f * fabsf((float)P.zdeep)) {
+        const double ynew = g.gy[niy] + (double)nv_ * (g.gy[niy + 1] - g.gy[niy]);
+        if (ynew > P.zdeep) tk = (float)P.tdeep;
+      }
+      const bool out = (nix == 0 && nu_ < 0.f) || (nix == g.ncx - 1 && nu_ > 1.f) ||
+                       (niy == 0 && nv_ < 0.f) || (niy == g.ncy - 1 && nv_ > 1.f);
+      if (out) {
+        tk = 0.f;
+        a.m.e[idx] = 0.f;
+        a.m.flags[idx] |= MFLAG_RESET;
+        atomicAdd(a.stat + ST_OUT_OF_GRID, 1ull);
+      }
+      if (tk != tk0) a.m.tk[idx] = tk;
+    }
+    a.m.cell_out[idx] = nix * ncy + niy;
+    a.m.u_out[idx] = nu_;
+    a.m.v_out[idx] = nv_;
   }
 }
 
 }  // namespace
 
-void launch_n2m_move(const N2MArgs &a, cudaStream_t st) {
+void launch_n2m(const N2MArgs &a, cudaStream_t st) {
   dim3 grid((a.g.xn + a.TX - 1) / a.TX, (a.g.yn + TY - 1) / TY);
-  k_n2m_move<<<grid, NTH, 0, st>>>(a);
+  k_n2m<<<grid, NTH, 0, st>>>(a);
+}
+
+void launch_move(const N2MArgs &a, cudaStream_t st) {
+  k_vel_pnodes<<<(unsigned)((a.g.nn + 255) / 256), 256, 0, st>>>(
+      a.g, a.N.f(V2C_NF_VX), a.N.f(V2C_NF_VY), a.vxp, a.vyp);
+  if (a.n <= 0) return;
+  long blocks = (a.n + 255) / 256;
+  if (blocks > 152 * 8 * 4) blocks = 152 * 8 * 4;
+  k_move<<<(unsigned)blocks, 256, 0, st>>>(a);
 }
 
 }  // namespace v2c

@@ -95,7 +95,9 @@ __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, in
 struct Fric {
   float a, b, L, V0, mu0;
 };
-__device__ __forceinline__ float friction_marker(const v2c_params &p, int phi_reset0,
+// Out of line: the marker physics calls it only near the frictional band
+// (FP64 position test) and for sticky air.
+static __device__ __noinline__ float friction_marker(const v2c_params &p, int phi_reset0,
                                                  double x, double y, int t, float phi,
                                                  Fric &f) {
   double d = y - (p.fault_y + p.fault_slope * x);

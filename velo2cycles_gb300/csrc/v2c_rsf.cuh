@@ -98,8 +98,10 @@ struct RsfResult {
 // Safeguarded FP64 Newton from u (the oracle's v2c_oracle_rsf_newton1
 // rules).  `snap_floor`: an iterate handed over from the FP32 phase at the
 // floor is taken as the floor itself.
-__device__ __forceinline__ void rsf_newton64(const RsfState &q, double u, double rtol, int maxit,
-                                             bool snap_floor, RsfResult &r) {
+// Kept out of line: the split form reaches it only as a rare fallback, and
+// its FP64 library code would otherwise crowd the hot loop's instructions.
+static __device__ __noinline__ void rsf_newton64(const RsfState &q, double u, double rtol, int maxit,
+                                          bool snap_floor, RsfResult &r) {
   r.it64 = 0;
   r.ok = false;
   double ulo = RSF_LOG_FLOOR, uhi = log(q.Ts / q.klin);
@@ -129,8 +131,21 @@ __device__ __forceinline__ void rsf_newton64(const RsfState &q, double u, double
 }
 
 // Degenerate loads: T* <= 0, or the floor already above the load.
-__device__ __forceinline__ bool rsf_degenerate(double Ts, double klin) {
+static __device__ __noinline__ bool rsf_degenerate(double Ts, double klin) {
   return !(Ts > 0) || !(log(Ts / klin) > RSF_LOG_FLOOR);
+}
+
+// Out-of-line FP64 pieces of the split form (rarely taken).
+static __device__ __noinline__ bool rsf_degenerate_in(const RsfIn &in) {
+  RsfState s;
+  rsf_setup64(s, in);
+  return rsf_degenerate(s.Ts, s.klin);
+}
+static __device__ __noinline__ void rsf_finish64(const RsfIn &in, double u, double rtol, int maxit,
+                                          RsfResult &r) {
+  RsfState s;
+  rsf_setup64(s, in);
+  rsf_newton64(s, u, rtol, maxit, true, r);
 }
 
 // Whole FP64 solve from the start u0.
@@ -328,9 +343,7 @@ __device__ __forceinline__ RsfResult rsf_solve_split(const RsfIn &in, const Rsf3
   const float floor32 = (float)RSF_LOG_FLOOR;
   if (!(q32.Ts > 0.f) || !(q32.uhi > floor32)) {
     // degenerate in FP32: decided in FP64 as the FP64 form does
-    RsfState s;
-    rsf_setup64(s, in);
-    if (rsf_degenerate(s.Ts, s.klin)) { r.V = 1e-40; r.Vf = 1e-40f; r.ok = true; return r; }
+    if (rsf_degenerate_in(in)) { r.V = 1e-40; r.Vf = 1e-40f; r.ok = true; return r; }
   }
   float dF32;
   const float u32 = rsf_newton32(q32, u0, floor32, q32.uhi, maxit, r.it32, dF32);
@@ -365,9 +378,7 @@ __device__ __forceinline__ RsfResult rsf_solve_split(const RsfIn &in, const Rsf3
     u = ff_add_f(u, -F.hi / dF32);
   }
   // the FP64 Newton finishes
-  RsfState s;
-  rsf_setup64(s, in);
-  rsf_newton64(s, ff_to_double(u), rtol, maxit, true, r);
+  rsf_finish64(in, ff_to_double(u), rtol, maxit, r);
   return r;
 }
 
