@@ -222,6 +222,8 @@ MODES = [("learned_split", "GUESS_LEARNED", "NEWTON_SPLIT"),
          ("plain_split", "GUESS_PLAIN", "NEWTON_SPLIT"),
          ("plain_fp64", "GUESS_PLAIN", "NEWTON_FP64"),
          ("learned_fp64", "GUESS_LEARNED", "NEWTON_FP64")]
+# not timed by default: the step with the per-marker Newton switched off
+EXTRA_FORMS = [("no_newton", "GUESS_OFF", "NEWTON_SPLIT")]
 
 
 def dt_sequence(k: int, seed: int) -> np.ndarray:
@@ -314,7 +316,7 @@ def run_gpu(args, rank: int, world: int) -> None:
     m.synchronize()
     n = case.n
     log(f"[bench] uploaded in {time.time() - t0:.1f}s")
-    forms = [f for f in MODES if f[0] in args.forms.split(",")]
+    forms = [f for f in MODES + EXTRA_FORMS if f[0] in args.forms.split(",")]
     if not forms or forms[0][0] != "learned_split":
         raise SystemExit("--forms must start with learned_split (the headline form)")
     training = None
