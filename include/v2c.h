@@ -40,7 +40,9 @@ enum {
   V2C_ERR_UNSUPPORTED = 4,  /* configuration outside what the kernels implement  */
   V2C_ERR_NAN = 5,          /* NaN / non-positive viscosity detected (errcheck)  */
   V2C_ERR_NOCONV = 6,       /* per-marker Newton did not converge for some marker */
-  V2C_ERR_STATE = 7         /* call order violated (e.g. no markers uploaded)     */
+  V2C_ERR_STATE = 7,        /* call order violated (e.g. no markers uploaded)     */
+  V2C_ERR_TIMESTEP = 8      /* chi == 0 in the adaptive time step (the reference
+                               stops there, calc_RSF.c:477-481)                */
 };
 
 #define V2C_MAXTMR 200 /* rock types, src/headevps.c:15 */
@@ -163,6 +165,8 @@ enum {
   V2C_NF_PHISUM, V2C_NF_WTPHISUM, V2C_NF_SXYSUM, V2C_NF_EXYSUM, V2C_NF_ESUM,
   V2C_NF_PSUM, V2C_NF_SXXSUM, V2C_NF_EXXSUM, V2C_NF_WTSXXSUM, V2C_NF_VXSUM,
   V2C_NF_VYSUM, V2C_NF_WTVXSUM, V2C_NF_WTVYSUM, V2C_NF_MRX0, V2C_NF_MRY0,
+  /* read by the adaptive time step (calc_RSF.c:455) */
+  V2C_NF_PRS,
   V2C_NF_N
 };
 
@@ -235,6 +239,34 @@ int v2c_moveandrotatemarkers(v2c_ctx *ctx);         /* [moveandrotatemarkers.c:1
 /* nodes2markers followed by moveandrotatemarkers in one marker pass. */
 int v2c_nodes2markers_move(v2c_ctx *ctx);
 
+/* ============================================== adaptive time step
+ * calc_timestep (calc_RSF.c:352-572): the next time step from the node
+ * fields, limited by the visco-plastic Maxwell time (tcnvp), the
+ * displacement per step (tcd), the state evolution (tcphih) and the
+ * Lapusta et al. (2000) slip length (lambda L / V), and the maximum slip
+ * rate; oldornew = 0 before the Stokes solve (mvx/mvy, RK_sliprs_final,
+ * phis, sppes), 1 inside the Picard loop (vx/vy, RK_sliprs_solved, phis_it,
+ * prs).  Also returns the reference's diagnostic statistics of stress and
+ * viscosity over sticky01 == 1 and == 2 nodes.  Synchronises the stream. */
+typedef struct v2c_timestep_ctl {
+  double maxtmstep;         /* maximum time step, s     headevps.c:339     */
+  double dtfactor;          /* [1.0]                    input_RSF.c:17     */
+  double tcnvp;             /* [0.2]                    input_RSF.c:18     */
+  double tcd;               /* [1e-3]                   input_RSF.c:19     */
+  double tcphih;            /* [0.2]                    input_RSF.c:20     */
+} v2c_timestep_ctl;
+typedef struct v2c_timestep_info {
+  double dt_f, maxvel, maxVx, dtnvp, dtd, dtphi, dtL;
+  long nr_0, nr_1;
+  double max_sigin_0, min_sigin_0, sum_sigin_0, sum2_sigin_0;
+  double max_visc_0, min_visc_0, sum_visc_0, sum2_visc_0;
+  double max_sigin_1, min_sigin_1, sum_sigin_1, sum2_sigin_1;
+  double max_visc_1, min_visc_1, sum_visc_1, sum2_visc_1;
+  double sigin_P1, sigin_P2, visco_P1, visco_P2;
+} v2c_timestep_info;
+int v2c_calc_timestep(v2c_ctx *ctx, int oldornew, const v2c_timestep_ctl *ctl,
+                      v2c_timestep_info *info);            /* [calc_RSF.c:352] */
+
 int v2c_synchronize(v2c_ctx *ctx);
 int v2c_get_status(v2c_ctx *ctx, v2c_status *st);
 
@@ -253,6 +285,7 @@ enum {
   V2C_PROF_NEWTON,      /* marker physics with the per-marker Newton    */
   V2C_PROF_PHYS,        /* marker physics without the Newton            */
   V2C_PROF_MOVE,        /* moveandrotatemarkers                        */
+  V2C_PROF_TIMESTEP,    /* calc_timestep                                */
   V2C_PROF_N
 };
 int v2c_set_profiling(v2c_ctx *ctx, int on);

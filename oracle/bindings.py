@@ -86,6 +86,9 @@ def _lib():
             getattr(lib, fn).argtypes = [P(_State)]
         lib.v2c_oracle_compute_before_solve.restype = ctypes.c_int
         lib.v2c_oracle_compute_before_solve.argtypes = [P(_State), ctypes.c_double, ctypes.c_int]
+        lib.v2c_oracle_calc_timestep.restype = ctypes.c_int
+        lib.v2c_oracle_calc_timestep.argtypes = [P(_State), ctypes.c_int, P(abi.TimestepCtl),
+                                                 P(abi.TimestepInfo)]
         lib.v2c_oracle_compute_after_solve.restype = ctypes.c_double
         lib.v2c_oracle_compute_after_solve.argtypes = [P(_State), ctypes.c_double, ctypes.c_int]
         lib.v2c_oracle_rsf_newton.restype = ctypes.c_long
@@ -159,6 +162,14 @@ class Restatement:
 
     def compute_after_solve(self, dt, rk=0):
         return self.lib.v2c_oracle_compute_after_solve(ctypes.byref(self.st), dt, rk)
+
+    def calc_timestep(self, oldornew=0, **ctl):
+        """(status, info dict) of calc_timestep (calc_RSF.c:352-572)."""
+        c = abi.TimestepCtl(**dict(abi.TIMESTEP_DEFAULTS, **ctl))
+        info = abi.TimestepInfo()
+        rc = self.lib.v2c_oracle_calc_timestep(ctypes.byref(self.st), oldornew, ctypes.byref(c),
+                                               ctypes.byref(info))
+        return rc, info.to_dict()
 
     def nodes2markers(self):
         return self.lib.v2c_oracle_nodes2markers(ctypes.byref(self.st))
@@ -248,9 +259,13 @@ def mlp_forward(params: np.ndarray, X: np.ndarray) -> np.ndarray:
 
 STAGE_M2N, STAGE_C2B, STAGE_BEFORE, STAGE_AFTER, STAGE_N2M, STAGE_MOVE = range(6)
 ALL_STAGES = 0b111111
+TIMESTEP_STAGE = 1 << 6
 
 
-def write_case(path: str, case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0) -> None:
+def write_case(path: str, case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0,
+               timestep=None, oldornew=0) -> None:
+    """timestep: v2c_timestep_ctl values as a dict (abi.TIMESTEP_DEFAULTS when
+    None); oldornew: the argument of calc_timestep (stage bit 6)."""
     c = case
     nn = c.nodenum
     with open(path, "wb") as f:
@@ -269,6 +284,9 @@ def write_case(path: str, case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=
         np.ascontiguousarray(c.bondm, dtype=np.int64).tofile(f)
         np.ascontiguousarray(c.bondn, dtype=np.int64).tofile(f)
         np.ascontiguousarray(c.bondv, dtype=np.float64).tofile(f)
+        ts = dict(abi.TIMESTEP_DEFAULTS, **(timestep or {}))
+        np.array([ts["maxtmstep"], ts["dtfactor"], ts["tcnvp"], ts["tcd"], ts["tcphih"],
+                  float(oldornew)], dtype=np.float64).tofile(f)
 
 
 def read_result(path: str, nodenum: int):
@@ -280,10 +298,14 @@ def read_result(path: str, nodenum: int):
         markt = np.fromfile(f, dtype=np.int8, count=n)
         secs = np.fromfile(f, dtype=np.float64, count=8)
         deltas = float(np.fromfile(f, dtype=np.float64, count=1)[0])
-    return dict(nodes=nodes, marks=marks, markt=markt, seconds=secs, deltas=deltas, n=n)
+        ts_rc = int(np.fromfile(f, dtype=np.int64, count=1)[0])
+        info = abi.TimestepInfo.from_buffer_copy(f.read(ctypes.sizeof(abi.TimestepInfo)))
+    return dict(nodes=nodes, marks=marks, markt=markt, seconds=secs, deltas=deltas, n=n,
+                timestep_rc=ts_rc, timestep=info.to_dict())
 
 
-def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeout=3600):
+def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeout=3600,
+                  timestep=None, oldornew=0):
     """Run the reference routines on `case`; returns the arrays after the
     stages plus per-stage seconds summed over the timed steps."""
     if not reference_available():
@@ -292,7 +314,7 @@ def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeo
         raise RuntimeError("reference oracle not built (reference sources unavailable)")
     with tempfile.TemporaryDirectory() as d:
         cp, rp = os.path.join(d, "case.bin"), os.path.join(d, "res.bin")
-        write_case(cp, case, stages, nthreads, nsteps, warmup)
+        write_case(cp, case, stages, nthreads, nsteps, warmup, timestep, oldornew)
         env = dict(os.environ, OMP_NUM_THREADS=str(max(1, nthreads)))
         r = subprocess.run([reference_path(), cp, rp], env=env, capture_output=True,
                            timeout=timeout)

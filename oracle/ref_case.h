@@ -42,6 +42,9 @@ typedef struct {
   long xn, yn, n, nb, nn;
   int nthreads, stages, nsteps, warmup;
   double *scratch;
+  double ts[6];            /* maxtmstep, dtfactor, tcnvp, tcd, tcphih, oldornew */
+  v2c_timestep_info info;  /* calc_timestep results (stage bit 6) */
+  long ts_rc;              /* 0, or 1 when chi == 0 stopped it */
 } ref_case;
 
 /* returns 0, or the process exit code on failure */
@@ -102,6 +105,9 @@ static int ref_load_case(const char *path, ref_case *C) {
   for (long i = 0; i < nb; i++)
     for (int k = 0; k < 4; k++) bondv[i][k] = bv[i * 4 + k];
   bondnum = nb;
+  rd(C->ts, sizeof(double), 6, f);
+  memset(&C->info, 0, sizeof(C->info));
+  C->ts_rc = 0;
   fclose(f);
   marknum = n;
   return 0;
@@ -134,6 +140,8 @@ static int ref_write_result(const char *path, const ref_case *C, const double *s
   }
   wr(secs, sizeof(double), 8, o);
   wr(&deltas, sizeof(double), 1, o);
+  wr(&C->ts_rc, sizeof(long), 1, o);
+  wr(&C->info, sizeof(C->info), 1, o);
   fclose(o);
   return 0;
 }

@@ -59,6 +59,26 @@
 
 #include "ref_case.h"
 
+/* the reference's calc_timestep and the globals it leaves behind */
+static void ref_timestep(ref_case *C, int oldornew) {
+  v2c_timestep_info *o = &C->info;
+  o->dt_f = calc_timestep(oldornew);
+  o->maxvel = maxvel;
+  o->maxVx = NAN; /* a local of calc_timestep */
+  o->dtnvp = dtnvp; o->dtd = dtd; o->dtphi = dtphi; o->dtL = dtL;
+  o->nr_0 = nr_0; o->nr_1 = nr_1;
+  o->max_sigin_0 = max_sigin_0; o->min_sigin_0 = min_sigin_0;
+  o->sum_sigin_0 = sum_sigin_0; o->sum2_sigin_0 = sum2_sigin_0;
+  o->max_visc_0 = max_visc_0; o->min_visc_0 = min_visc_0;
+  o->sum_visc_0 = sum_visc_0; o->sum2_visc_0 = sum2_visc_0;
+  o->max_sigin_1 = max_sigin_1; o->min_sigin_1 = min_sigin_1;
+  o->sum_sigin_1 = sum_sigin_1; o->sum2_sigin_1 = sum2_sigin_1;
+  o->max_visc_1 = max_visc_1; o->min_visc_1 = min_visc_1;
+  o->sum_visc_1 = sum_visc_1; o->sum2_visc_1 = sum2_visc_1;
+  o->sigin_P1 = sigin_P1; o->sigin_P2 = sigin_P2;
+  o->visco_P1 = visco_P1; o->visco_P2 = visco_P2;
+}
+
 int main(int argc, char **argv) {
   if (argc < 3) { fprintf(stderr, "usage: v2c_ref case.bin result.bin\n"); return 2; }
   ref_case C;
@@ -85,6 +105,14 @@ int main(int argc, char **argv) {
     STAGE(3, 3, deltas = compute_after_solve(timestep, 0));
     STAGE(4, 4, nodes2markers());
     STAGE(5, 5, moveandrotatemarkers());
+    if (stages & (1 << 6)) {
+      /* calc_timestep (calc_RSF.c:352): its controls are globals */
+      maxtmstep = C.ts[0]; dtfactor = C.ts[1]; tcnvp = C.ts[2]; tcd = C.ts[3];
+      tcphih = C.ts[4];
+      t0 = omp_get_wtime();
+      ref_timestep(&C, (int)C.ts[5]);
+      if (timed) secs[6] += omp_get_wtime() - t0;
+    }
 #undef STAGE
   }
 

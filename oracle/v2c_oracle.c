@@ -1269,6 +1269,121 @@ int v2c_oracle_move(v2c_oracle_state *s) {
 }
 
 /* =========================================================================
+ * calc_timestep, calc_RSF.c:352-572, in the reference's loop order.  Nodes
+ * with b <= 0 reset the state and slip-length limits to maxtmstep
+ * (calc_RSF.c:497-501), so those two minima run over the nodes after the
+ * last such node; lambda keeps its previous value where chi is NaN
+ * (calc_RSF.c:466-481, no branch taken), starting here from 1/5.
+ * ========================================================================= */
+/* min/max/abs with the reference's comparison order (headevps.c:3-5), which
+ * decides what a NaN candidate does to the running extremum */
+#define MINV(a, b) ((a) <= (b) ? (a) : (b))
+#define MAXV(a, b) ((a) >= (b) ? (a) : (b))
+#define ABSV(a) ((a) >= 0 ? (a) : -(a))
+
+int v2c_oracle_calc_timestep(const v2c_oracle_state *s, int oldornew,
+                             const v2c_timestep_ctl *c, v2c_timestep_info *o) {
+  const v2c_params *p = &s->p;
+  const long xn = p->xnumx, yn = p->ynumy, nodenum = xn * yn;
+  double *const *N = s->N;
+  memset(o, 0, sizeof(*o));
+  double maxvel = 0, maxVx = 0;
+  o->min_sigin_1 = o->min_sigin_0 = 1e30;
+  o->min_visc_1 = o->min_visc_0 = 1e30;
+  double dt_f = c->maxtmstep;
+  double dtnvp = 1e30, dtd = 1e30, dtphi = 1e30, dtL = 1e30;
+  double lambda = 1.0 / 5.0;
+  for (long m3 = 0; m3 < nodenum; m3++) {
+    long m2 = m3 % yn, m1 = (m3 - m2) / yn;
+    if (!(m1 >= 1 && m2 >= 1 && m1 < xn - 1 && m2 < yn - 1)) continue;
+    double dx = s->gx[m1 + 1] - s->gx[m1];
+    double dy = s->gy[m2 + 1] - s->gy[m2];
+    double faultwidth = 2 * 0.5 * (dx + dy);
+    double NUVP;
+    if (oldornew == 0) {
+      if (N[V2C_NF_NU_M2C][m3] > 1.00e+26) {
+        double sigin = pow(N[V2C_NF_SXXES][m3] * N[V2C_NF_SXXES][m3] +
+                           N[V2C_NF_SXYE][m3] * N[V2C_NF_SXYE][m3], 0.5);
+        double V = N[V2C_NF_RK_SLIPRS_FINAL][m3], nu = N[V2C_NF_NU_M2C][m3];
+        if (sigin > 0 && V > 0) NUVP = nu * sigin / (2 * nu * V / faultwidth + sigin);
+        else NUVP = nu;
+      } else {
+        NUVP = 5.00e+26;
+      }
+    } else {
+      if (N[V2C_NF_NU_M2C][m3] > 1.00e+26) NUVP = N[V2C_NF_NU][m3];
+      else NUVP = 5.00e+26;
+    }
+    dtnvp = MINV(dtnvp, c->tcnvp * NUVP / N[V2C_NF_GG][m3]);
+    /* displacement time step */
+    double VXn = oldornew == 1 ? N[V2C_NF_VX][m3] : N[V2C_NF_MVX][m3];
+    double VYn = oldornew == 1 ? N[V2C_NF_VY][m3] : N[V2C_NF_MVY][m3];
+    if (VXn != 0 && VYn != 0) {
+      maxVx = MAXV(maxVx, MAXV(ABSV(VXn), ABSV(VYn)));
+      double maxdr = MAXV(ABSV(VXn / dx), ABSV(VYn / dy));
+      dtd = MINV(dtd, c->tcd * 1.0 / maxdr);
+    }
+    /* seismic-cycle time step */
+    if (p->RSFmode == 1) {
+      double nps = 0;
+      if (p->pmode == 0) nps = p->nstress;
+      else if (p->pmode == 1) nps = oldornew == 0 ? N[V2C_NF_SPPES][m3] : N[V2C_NF_PRS][m3];
+      double bm = N[V2C_NF_BM][m3], gg = N[V2C_NF_GG][m3];
+      double as = N[V2C_NF_AS][m3], bs = N[V2C_NF_BS][m3], Ls = N[V2C_NF_LS][m3];
+      double v = (3 * bm - 2 * gg) / (2 * (3 * bm + gg));
+      double k = 2.0 / 3.14 * (gg / (1 - v)) / p->xstpx;
+      double chi = 1.0 / 4.0 * pow(k * Ls / (as * nps) - (bs - as) / as, 2) - k * Ls / (as * nps);
+      if (chi > 0) lambda = as * nps / (k * Ls - (bs - as) * nps);
+      else if (chi < 0) lambda = 1 - (bs - as) * nps / (k * Ls);
+      else if (chi == 0) return V2C_ERR_TIMESTEP;
+      lambda = MINV(lambda, 1.0 / 5.0);
+      if (bs > 0) {
+        if (oldornew == 0 && N[V2C_NF_RK_SLIPRS_FINAL][m3] > 0) {
+          double phisc = N[V2C_NF_V0S][m3] / Ls * exp(-N[V2C_NF_PHIS][m3]);
+          dtphi = MINV(dtphi, c->tcphih * 1.0 / phisc);
+          dtL = MINV(dtL, lambda * Ls / (N[V2C_NF_RK_SLIPRS_FINAL][m3]));
+        } else if (oldornew == 1 && N[V2C_NF_RK_SLIPRS_SOLVED][m3] > 0) {
+          double phisc = N[V2C_NF_V0S][m3] / Ls * exp(-N[V2C_NF_PHIS_IT][m3]);
+          dtphi = MINV(dtphi, c->tcphih * 1.0 / phisc);
+          dtL = MINV(dtL, lambda * Ls / (N[V2C_NF_RK_SLIPRS_SOLVED][m3]));
+        }
+      } else {
+        dtphi = c->maxtmstep;
+        dtL = c->maxtmstep;
+      }
+    }
+    /* stress and viscosity statistics over sticky-air flags */
+    double sigin = pow(N[V2C_NF_SXXS][m3] * N[V2C_NF_SXXS][m3] +
+                       N[V2C_NF_SXY][m3] * N[V2C_NF_SXY][m3], 0.5);
+    double st = N[V2C_NF_STICKY01][m3], nu = N[V2C_NF_NU][m3];
+    if (st == 1 && m1 == 50 && m2 == 50) { o->sigin_P1 = sigin; o->visco_P1 = nu; }
+    if (st == 1 && m1 == 500 && m2 == 50) { o->sigin_P2 = sigin; o->visco_P2 = nu; }
+    if (st == 2) {
+      o->nr_1++;
+      o->max_sigin_1 = MAXV(o->max_sigin_1, sigin); o->min_sigin_1 = MINV(o->min_sigin_1, sigin);
+      o->sum_sigin_1 += sigin; o->sum2_sigin_1 += pow(sigin, 2);
+      o->max_visc_1 = MAXV(o->max_visc_1, nu); o->min_visc_1 = MINV(o->min_visc_1, nu);
+      o->sum_visc_1 += log10(nu); o->sum2_visc_1 += pow(log10(nu), 2);
+    }
+    if (st == 1) {
+      o->nr_0++;
+      o->max_sigin_0 = MAXV(o->max_sigin_0, sigin); o->min_sigin_0 = MINV(o->min_sigin_0, sigin);
+      o->sum_sigin_0 += sigin; o->sum2_sigin_0 += pow(sigin, 2);
+      o->max_visc_0 = MAXV(o->max_visc_0, nu); o->min_visc_0 = MINV(o->min_visc_0, nu);
+      o->sum_visc_0 += log10(nu); o->sum2_visc_0 += pow(log10(nu), 2);
+    }
+    if (oldornew == 0 && N[V2C_NF_RK_SLIPRS_FINAL][m3] > 0)
+      maxvel = MAXV(maxvel, N[V2C_NF_RK_SLIPRS_FINAL][m3]);
+    if (oldornew == 1 && N[V2C_NF_RK_SLIPRS_SOLVED][m3] > 0)
+      maxvel = MAXV(maxvel, N[V2C_NF_RK_SLIPRS_SOLVED][m3]);
+  }
+  dt_f = c->dtfactor * MINV(dt_f, MINV(dtphi, MINV(MINV(dtL, dtnvp), dtd)));
+  o->dt_f = dt_f; o->maxvel = maxvel; o->maxVx = maxVx;
+  o->dtnvp = dtnvp; o->dtd = dtd; o->dtphi = dtphi; o->dtL = dtL;
+  return V2C_OK;
+}
+
+/* =========================================================================
  * Per-marker visco-elasto-plastic + RSF Newton (no counterpart in the
  * reference, which couples stress and slip rate only through its global
  * Picard loop).  With T* = tau_old + 2 G dt edot, c1 = 1 + G dt/eta and

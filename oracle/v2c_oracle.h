@@ -48,6 +48,11 @@ double v2c_oracle_compute_after_solve(v2c_oracle_state *s, double dt, int rk);
 int v2c_oracle_nodes2markers(v2c_oracle_state *s);
 int v2c_oracle_move(v2c_oracle_state *s);
 
+/* adaptive time step, calc_RSF.c:352-572; returns V2C_OK or
+ * V2C_ERR_TIMESTEP where the reference would stop (chi == 0) */
+int v2c_oracle_calc_timestep(const v2c_oracle_state *s, int oldornew,
+                             const v2c_timestep_ctl *c, v2c_timestep_info *info);
+
 /* per-marker ductile viscosity, density_ductilevisc_calc.c:29-223 */
 double v2c_oracle_ductilevisc(const v2c_oracle_state *s, int mm2, double SXY,
                               double SXX, double EXY, double EXX, double mtk,

@@ -166,3 +166,24 @@ def test_interpolationmod1_reported_unsupported(built_lib):
     with pytest.raises(V2CError) as e:
         mic.from_case(c)
     assert e.value.code == abi.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("oldornew", [0, 1])
+@pytest.mark.parametrize("variant", [{}, dict(pmode=1), dict(RSFmode=0)])
+def test_calc_timestep(oldornew, variant, built_lib, oracle_built):
+    """calc_timestep on the device node fields against the oracle: the time
+    step and its limits to 1e-5 (FP32 node fields), counts exactly."""
+    c = synth.make_case("small", seed=21, **variant)
+    ctl = dict(maxtmstep=3e9, tcd=2e-3)
+    m = mic.from_case(c)
+    got = m.calc_timestep(oldornew, **ctl)
+    m.close()
+    rc, ref = oracle.Restatement(c.copy()).calc_timestep(oldornew, **ctl)
+    assert rc == 0
+    for k in ("nr_0", "nr_1"):
+        assert got[k] == ref[k], k
+    for k in ("dt_f", "maxvel", "maxVx", "dtnvp", "dtd", "dtphi", "dtL", "max_sigin_0",
+              "min_sigin_0", "max_sigin_1", "min_sigin_1", "max_visc_0", "min_visc_0",
+              "max_visc_1", "min_visc_1", "sum_sigin_0", "sum_sigin_1", "sum_visc_0",
+              "sum_visc_1", "sum2_sigin_0", "sum2_visc_1"):
+        assert abs(got[k] - ref[k]) <= 1e-5 * max(abs(ref[k]), 1e-30), (k, got[k], ref[k])

@@ -95,3 +95,41 @@ def test_nxsearch_ties_and_clamps():
     assert B.nxsearch(g, 8.0) == 3          # last line clamps to n-2
     assert B.nxsearch(g, 100.0) == 3
     assert B.nxsearch(g, 3.999) == 2
+
+
+@needs_ref
+@pytest.mark.parametrize("oldornew", [0, 1])
+@pytest.mark.parametrize("variant", [{}, dict(pmode=1), dict(RSFmode=0)])
+def test_calc_timestep_bit_exact_vs_reference(oldornew, variant):
+    """calc_timestep (calc_RSF.c:352-572) alone on seeded node fields: every
+    output the reference leaves in its globals, bit for bit."""
+    c = synth.make_case("small", 6, **variant)
+    ctl = dict(maxtmstep=3e9, tcd=2e-3)
+    ref = B.run_reference(c, stages=B.TIMESTEP_STAGE, timestep=ctl, oldornew=oldornew)
+    assert ref["timestep_rc"] == 0
+    rc, info = oracle.Restatement(c.copy()).calc_timestep(oldornew, **ctl)
+    assert rc == 0
+    bad = {k: (info[k], ref["timestep"][k]) for k in info
+           if k != "maxVx" and info[k] != ref["timestep"][k]}
+    assert not bad, bad
+    assert 0 < info["dt_f"] <= 3e9 or variant.get("pmode") == 1
+
+
+def test_calc_timestep_resets_and_golden():
+    """A node with b <= 0 resets the state and slip-length limits
+    (calc_RSF.c:497-501): only nodes after the last reset count."""
+    c = synth.make_case("tiny", 2)
+    yn = c.gy.size
+    bs = c.nodes[abi.NF_BS]
+    m_reset = 5 * yn + 5
+    bs[m_reset] = 0.0
+    r = oracle.Restatement(c.copy())
+    rc, info = r.calc_timestep(0, maxtmstep=1e12)
+    # recompute the state limit over interior nodes after the reset
+    N = c.nodes
+    m = np.arange(c.nodenum)
+    m2, m1 = m % yn, m // yn
+    inter = (m1 >= 1) & (m2 >= 1) & (m1 < c.gx.size - 1) & (m2 < yn - 1)
+    after = inter & (m > m_reset) & (N[abi.NF_BS] > 0) & (N[abi.NF_RK_SLIPRS_FINAL] > 0)
+    phisc = N[abi.NF_V0S][after] / N[abi.NF_LS][after] * np.exp(-N[abi.NF_PHIS][after])
+    assert info["dtphi"] == min(1e12, (0.2 / phisc).min())

@@ -60,6 +60,7 @@ _SIGS = {
                       ctypes.c_int, ctypes.c_float, ctypes.c_uint64, c_fp],
     "v2c_mlp_grad": [c_ctx, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_long, c_fp, c_fp],
     "v2c_mlp_infer": [c_ctx, ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p],
+    "v2c_calc_timestep": [c_ctx, ctypes.c_int, P(abi.TimestepCtl), P(abi.TimestepInfo)],
     "v2c_sort_cells_static": [ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p, ctypes.c_long,
                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p,
                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],

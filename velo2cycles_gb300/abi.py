@@ -41,17 +41,26 @@ for _body in re.findall(r"enum\s*\{(.*?)\}\s*;", _SRC, flags=re.S):
 for _k, _v in _CONST.items():
     globals()[_k[4:] if _k.startswith("V2C_") else _k] = _v
 
-# v2c_params
-_m = re.search(r"typedef\s+struct\s+v2c_params\s*\{(.*?)\}\s*v2c_params\s*;", _SRC, flags=re.S)
 _CT = {"long": ctypes.c_long, "double": ctypes.c_double, "int": ctypes.c_int}
-_FIELDS = []
-for _decl in _m.group(1).split(";"):
-    _decl = _decl.strip()
-    if not _decl:
-        continue
-    _typ, _names = _decl.split(None, 1)
-    for _nm in _names.split(","):
-        _FIELDS.append((_nm.strip(), _CT[_typ]))
+
+
+def _struct_fields(name: str) -> list:
+    """(field, ctype) list of `typedef struct name { ... } name;`"""
+    m = re.search(r"typedef\s+struct\s+" + name + r"\s*\{(.*?)\}\s*" + name + r"\s*;", _SRC,
+                  flags=re.S)
+    out = []
+    for decl in m.group(1).split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        typ, names = decl.split(None, 1)
+        for nm in names.split(","):
+            out.append((nm.strip(), _CT[typ]))
+    return out
+
+
+# v2c_params
+_FIELDS = _struct_fields("v2c_params")
 
 
 class Params(ctypes.Structure):
@@ -101,3 +110,18 @@ def declared_functions() -> list[str]:
                 src = _strip_comments(f.read())
             names += re.findall(r"^\s*(?:int|double|void|long)\s+\**\s*(\w+)\s*\(", src, flags=re.M)
     return names
+
+
+class TimestepCtl(ctypes.Structure):
+    _fields_ = _struct_fields("v2c_timestep_ctl")
+
+
+class TimestepInfo(ctypes.Structure):
+    _fields_ = _struct_fields("v2c_timestep_info")
+
+    def to_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+# reference defaults (input_RSF.c:17-20); maxtmstep comes from the model file
+TIMESTEP_DEFAULTS = dict(maxtmstep=1e10, dtfactor=1.0, tcnvp=0.2, tcd=1e-3, tcphih=0.2)

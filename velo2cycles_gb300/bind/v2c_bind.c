@@ -200,6 +200,32 @@ void v2c_bind_moveandrotatemarkers(void) {
   if (v2c_bind_sync_markers) v2c_bind_markers_to_host();
 }
 
+double v2c_bind_calc_timestep(int oldornew) {
+  if (!v2c_bind_setup() || !v2c_bind_nodes_up()) return 0;
+  v2c_timestep_ctl c = {maxtmstep, dtfactor, tcnvp, tcd, tcphih};
+  v2c_timestep_info o;
+  int rc = v2c_calc_timestep(v2c_bind_ctx, oldornew, &c, &o);
+  if (rc == V2C_ERR_TIMESTEP) {  /* the reference stops here */
+    printf("\n Chi is zero in the adaptive time stepping loop \n");
+    exit(0);
+  }
+  if (!v2c_bind_ok(rc, "v2c_calc_timestep")) return 0;
+  /* the globals calc_timestep leaves behind (calc_RSF.c:352-572) */
+  maxvel = o.maxvel;
+  dtnvp = o.dtnvp; dtd = o.dtd; dtphi = o.dtphi; dtL = o.dtL;
+  nr_0 = (int)o.nr_0; nr_1 = (int)o.nr_1;
+  max_sigin_0 = o.max_sigin_0; min_sigin_0 = o.min_sigin_0;
+  sum_sigin_0 = o.sum_sigin_0; sum2_sigin_0 = o.sum2_sigin_0;
+  max_visc_0 = o.max_visc_0; min_visc_0 = o.min_visc_0;
+  sum_visc_0 = o.sum_visc_0; sum2_visc_0 = o.sum2_visc_0;
+  max_sigin_1 = o.max_sigin_1; min_sigin_1 = o.min_sigin_1;
+  sum_sigin_1 = o.sum_sigin_1; sum2_sigin_1 = o.sum2_sigin_1;
+  max_visc_1 = o.max_visc_1; min_visc_1 = o.min_visc_1;
+  sum_visc_1 = o.sum_visc_1; sum2_visc_1 = o.sum2_visc_1;
+  sigin_P1 = o.sigin_P1; sigin_P2 = o.sigin_P2; visco_P1 = o.visco_P1; visco_P2 = o.visco_P2;
+  return o.dt_f;
+}
+
 void v2c_bind_close(void) {
   if (v2c_bind_ctx) v2c_destroy(v2c_bind_ctx);
   v2c_bind_ctx = NULL;

@@ -14,6 +14,8 @@
  *   compute_after_solve(dt, rk)          -> v2c_bind_compute_after_solve(dt, rk)
  *   nodes2markers()                      -> v2c_bind_nodes2markers()
  *   moveandrotatemarkers()               -> v2c_bind_moveandrotatemarkers()
+ *   calc_timestep(oldornew)              -> v2c_bind_calc_timestep(oldornew)
+ *                                           (momentum_continuity_iterate.c:44,92)
  *
  * Data movement.  The host arrays stay the truth for everything the host
  * solvers read and write.  Every call uploads the node arrays and brings
@@ -42,6 +44,7 @@ void v2c_bind_compute_before_solve(double dt, int rk);
 double v2c_bind_compute_after_solve(double dt, int rk);
 double v2c_bind_nodes2markers(void);
 void v2c_bind_moveandrotatemarkers(void);
+double v2c_bind_calc_timestep(int oldornew);
 
 /* the host changed marker arrays (temperature solve, loading a file) */
 void v2c_bind_markers_changed(void);

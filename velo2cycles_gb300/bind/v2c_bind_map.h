@@ -105,6 +105,7 @@ static double *v2c_bind_node_array(int f) {
     case V2C_NF_WTVYSUM: return wtvysum;
     case V2C_NF_MRX0: return mrx0;
     case V2C_NF_MRY0: return mry0;
+    case V2C_NF_PRS: return prs;
   }
   return NULL;
 }

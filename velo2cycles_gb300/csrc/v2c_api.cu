@@ -45,6 +45,8 @@ struct v2c_ctx {
   double *d_node64 = nullptr;  // boundary staging, one FP64 node field
   uint32_t *d_sticky = nullptr;
   float *d_vxp = nullptr, *d_vyp = nullptr;  // move: velocities at pressure nodes
+  unsigned *d_list_n = nullptr;              // count of listed Newton problems
+  double *d_ts = nullptr;                    // calc_timestep scratch
   // markers
   Markers m{};
   void *marker_mem[32] = {};
@@ -220,6 +222,8 @@ extern "C" int v2c_create(const v2c_params *p, long max_markers, void *cuda_stre
   AL(ctx->d_node64, ctx->nn);
   AL(ctx->d_sticky, ctx->nn);
   AL(ctx->d_vxp, ctx->nn); AL(ctx->d_vyp, ctx->nn);
+  AL(ctx->d_list_n, 1);
+  AL(ctx->d_ts, TIMESTEP_SCRATCH);
   AL(ctx->d_stat, ST_N);
   ctx->red_cap = 2 + 2 * ((ctx->nn + 255) / 256);
   AL(ctx->d_red, ctx->red_cap);
@@ -257,7 +261,7 @@ extern "C" int v2c_destroy(v2c_ctx *ctx) {
   if (!ctx) return V2C_ERR_ARG;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   void *ptrs[] = {ctx->d_gx, ctx->d_gy, ctx->d_wx, ctx->d_wy, ctx->d_gxf, ctx->d_gyf,
-                  ctx->d_rock, ctx->d_node, ctx->d_node64, ctx->d_sticky, ctx->d_vxp, ctx->d_vyp,
+                  ctx->d_rock, ctx->d_node, ctx->d_node64, ctx->d_sticky, ctx->d_vxp, ctx->d_vyp, ctx->d_list_n, ctx->d_ts,
                   ctx->d_stat, ctx->d_red,
                   ctx->sb.counts, ctx->sb.start, ctx->sb.slot, ctx->sb.tmp, ctx->sb.perm,
                   ctx->sb.blocksum, ctx->d_stage64, ctx->d_stage64b, ctx->bc_mem,
@@ -676,9 +680,14 @@ extern "C" int v2c_marker2nodes(v2c_ctx *ctx) {
     ph.g = a.g; ph.N = a.N; ph.m = a.m; ph.R = a.R; ph.S = a.S; ph.n = ctx->n;
     ph.sticky_key = ctx->d_sticky; ph.stat = ctx->d_stat; ph.gxf = ctx->d_gxf; ph.gyf = ctx->d_gyf;
     ph.mlp = ctx->nw.have_mlp ? ctx->nw.d_mlp : nullptr;
+    // the problem list borrows the sort's slot buffer, which holds nothing
+    // between sorts (capacity: one entry per marker)
+    ph.list = ctx->sb.slot;
+    ph.list_n = ctx->d_list_n;
+    ph.guess = reinterpret_cast<float *>(ctx->sb.tmp);  // likewise free between sorts
     Prof pr(ctx, ctx->p.newton_guess == V2C_GUESS_OFF ? V2C_PROF_PHYS : V2C_PROF_NEWTON);
     launch_phys(ph, st);
-    ctx->launches += 1;
+    ctx->launches += ctx->p.newton_guess == V2C_GUESS_OFF ? 1 : (ph.mlp && ctx->p.newton_guess == V2C_GUESS_LEARNED ? 3 : 2);
   }
   {
     Prof pr(ctx, V2C_PROF_M2N);
@@ -807,6 +816,22 @@ static int n2m_move(v2c_ctx *ctx, int do_n2m, int do_move) {
 extern "C" int v2c_nodes2markers(v2c_ctx *ctx) { return n2m_move(ctx, 1, 0); }
 extern "C" int v2c_moveandrotatemarkers(v2c_ctx *ctx) { return n2m_move(ctx, 0, 1); }
 extern "C" int v2c_nodes2markers_move(v2c_ctx *ctx) { return n2m_move(ctx, 1, 1); }
+
+extern "C" int v2c_calc_timestep(v2c_ctx *ctx, int oldornew, const v2c_timestep_ctl *ctl,
+                                 v2c_timestep_info *info) {
+  if (!ctx || !ctl || !info || (oldornew != 0 && oldornew != 1)) return V2C_ERR_ARG;
+  if (!ctx->have_grid) return fail(ctx, V2C_ERR_STATE);
+  memset(info, 0, sizeof(*info));
+  int rc;
+  {
+    Prof pr(ctx, V2C_PROF_TIMESTEP);
+    rc = calc_timestep_device(make_grid(ctx), make_nodes(ctx), make_scal(ctx->p, ctx->h_rt), *ctl,
+                              oldornew, ctx->d_ts, TIMESTEP_SCRATCH, info, ctx->stream);
+  }
+  ctx->launches += 2;
+  if (rc) return fail(ctx, rc);
+  return V2C_OK;
+}
 
 extern "C" int v2c_synchronize(v2c_ctx *ctx) {
   if (!ctx) return V2C_ERR_ARG;

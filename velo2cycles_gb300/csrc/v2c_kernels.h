@@ -53,6 +53,11 @@ struct PhysArgs {
   // xs[V2C_RS_N][xs_cap] and changes nothing else
   double *xs = nullptr;
   long xs_stride = 1, xs_cap = 0;
+  // the Newton problems the physics pass leaves for the Newton kernel:
+  // marker indices (capacity n) and their count (device)
+  int32_t *list = nullptr;
+  unsigned *list_n = nullptr;
+  float *guess = nullptr;  // the network's start per listed problem (capacity n)
 };
 void launch_phys(const PhysArgs &a, cudaStream_t st);
 void launch_sticky(const Nodes &N, const uint32_t *key, long nn, cudaStream_t st);
@@ -100,6 +105,13 @@ struct N2MArgs {
 void launch_n2m(const N2MArgs &a, cudaStream_t st);
 // moveandrotatemarkers: one thread per marker, new positions to *_out
 void launch_move(const N2MArgs &a, cudaStream_t st);
+
+// calc_timestep over the device node fields (synchronises the stream);
+// scratch: TIMESTEP_SCRATCH doubles
+constexpr long TIMESTEP_SCRATCH = (152 * 4 * 8 + 1) * 32 + 64;
+int calc_timestep_device(const Grid &g, const Nodes &N, const Scal &S, const v2c_timestep_ctl &c,
+                         int oldornew, double *scratch, long scratch_doubles,
+                         v2c_timestep_info *info, cudaStream_t st);
 
 // upload / download helpers
 void launch_assign(const Grid &g, const double *x, const double *y, long n, Markers m,

@@ -33,7 +33,10 @@ cudaError_t newton_init(NewtonState &s, long cap) {
 
 void newton_free(NewtonState &s) {
   if (s.d_mlp) cudaFree(s.d_mlp);
+  if (s.d_guess) cudaFree(s.d_guess);
   s.d_mlp = nullptr;
+  s.d_guess = nullptr;
+  s.guess_cap = 0;
 }
 
 namespace {
@@ -81,19 +84,16 @@ __device__ __forceinline__ void state_of(const double *S, long n, long i, double
 }
 
 // ---------------------------------------------------------- solve states
-// one instantiation per (arithmetic, start) pair
+// one instantiation per (arithmetic, start) pair; the learned start comes
+// from the network's outputs guess[i] (k_infer), so this kernel keeps the
+// plain start's occupancy
 template <bool FP64, bool LEARNED>
 __global__ void __launch_bounds__(NT, 4) k_solve_states(const double *S, long n, double W,
-                                                        const float *mlp, double rtol, int maxit,
+                                                        const float *guess, double rtol, int maxit,
                                                         double *out, int32_t *iters,
                                                         unsigned long long *stat) {
-  __shared__ MlpSmem M;
   const bool learned = LEARNED;
   const bool fp64 = FP64;
-  if (learned) {
-    mlp_load_smem(M, mlp);
-    __syncthreads();
-  }
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const long nwarps = (long)gridDim.x * (NT / 32);
   for (long base = ((long)blockIdx.x * (NT / 32) + wl) * 32; base < n; base += nwarps * 32) {
@@ -104,22 +104,11 @@ __global__ void __launch_bounds__(NT, 4) k_solve_states(const double *S, long n,
     if (valid) state_of(S, n, i, W, in, vold);
     const float u_plain = (vold > 0) ? logf((float)vold) : -30.f;
     // split form: states whose load is certainly below the floor's yield
-    // are done with one FP32 evaluation; a warp with no other state skips
-    // the network
+    // are done with one FP32 evaluation
     bool at_floor = false;
     float A_floor = 0.f;
     if (valid && !fp64) at_floor = rsf_floor_certain(rsf32_of(in), A_floor);
-    float u0 = u_plain;
-    if (learned && __any_sync(V2C_FULL, valid && !at_floor)) {
-      float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      if (valid && !at_floor) rsf_features(in, f);
-#pragma unroll
-      for (int k = 0; k < 8; k++) M.xin[wl][lane][k] = f[k];
-      __syncwarp();
-      mlp_warp_forward(M, wl);
-      u0 = M.yout[wl][lane][0];
-      __syncwarp();
-    }
+    const float u0 = (learned && valid) ? guess[i] : u_plain;
     unsigned long long it = 0, fb = 0, nc = 0, resbits = 0;
     if (valid) {
       // the FP64 form starts from the FP64 log of the previous slip rate
@@ -518,10 +507,21 @@ extern "C" int v2c_rsf_newton(v2c_ctx *ctx, const double *states_dev, long n, in
   v2c_ctx_prof_begin(ctx, V2C_PROF_NEWTON, &ev);
   const bool fp64 = p->newton_precision == V2C_NEWTON_FP64;
   const bool learned = guess == V2C_GUESS_LEARNED;
-  const float *mlp = v2c_ctx_newton(ctx)->d_mlp;
+  NewtonState *ns = v2c_ctx_newton(ctx);
+  if (learned) {
+    if (ns->guess_cap < n) {
+      if (ns->d_guess) cudaFree(ns->d_guess);
+      ns->d_guess = nullptr;
+      ns->guess_cap = 0;
+      CKR(cudaMalloc((void **)&ns->d_guess, sizeof(float) * 2 * n));
+      ns->guess_cap = n;
+    }
+    k_infer<<<(unsigned)blocks, NT, 0, st>>>(states_dev, n, p->faultwidth, ns->d_mlp, ns->d_guess);
+    v2c_ctx_count_launches(ctx, 1);
+  }
   auto kern = fp64 ? (learned ? k_solve_states<true, true> : k_solve_states<true, false>)
                    : (learned ? k_solve_states<false, true> : k_solve_states<false, false>);
-  kern<<<(unsigned)blocks, NT, 0, st>>>(states_dev, n, p->faultwidth, mlp, p->newton_rtol,
+  kern<<<(unsigned)blocks, NT, 0, st>>>(states_dev, n, p->faultwidth, ns->d_guess, p->newton_rtol,
                                         p->newton_maxit, out_dev, iters_dev, v2c_ctx_stat(ctx));
   v2c_ctx_prof_end(ctx, V2C_PROF_NEWTON, ev);
   v2c_ctx_count_launches(ctx, 1);

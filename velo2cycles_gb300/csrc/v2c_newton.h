@@ -10,6 +10,8 @@ struct NewtonState {
   float *d_mlp = nullptr;  // packed network parameters (V2C_MLP_NPARAM)
   int have_mlp = 0;
   long cap = 0;
+  float *d_guess = nullptr;  // network outputs [2][guess_cap] for v2c_rsf_newton
+  long guess_cap = 0;
 };
 
 cudaError_t newton_init(NewtonState &s, long cap);

@@ -60,6 +60,9 @@ __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, in
     const float p2fac = 2.f * s0 * invS;
     // |log10(m_k / m_k-1)| < 1e-6  <=>  10^-1e-6 < m_k / m_k-1 < 10^1e-6
     const float RLO = 0.99999769741f, RHI = 1.00000230259f;
+    // the extra derivative term p2 (below) is at most invS e^max(p2fac,0)
+    // (dold >= 0); under half an ulp of gm it cannot change gm + p2 in FP32
+    const float p2max = invS * __expf(fmaxf(p2fac, 0.f));
     float dnew = d0, m_prev = 1.f;
     for (int counter = 1; counter <= 50; counter++) {
       const float dold = dnew;
@@ -70,11 +73,12 @@ __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, in
       const float f2 = dold - c0 * f1;
       // pow(eta_diff, 2/(eta_diff+eta_disl_old)) / eta_diff, the reference's
       // extra term of the derivative (density_ductilevisc_calc.c:190-191)
-      const float p2 = (invS > 1e-30f) ? __expf(__fdividef(p2fac, 1.f + dold)) * invS : 0.f;
+      const float p2 = (invS > 1e-30f && !(p2max < gm * 0x1p-25f))
+                           ? __expf(__fdividef(p2fac, 1.f + dold)) * invS : 0.f;
       const float df = 1.f - emc0 * __fdividef(f1, base) * (gm + p2);  // base^(-1/mm) = f1/base
       dnew = dold - __fdividef(f2, df);
-      const float r = __fdividef(m, m_prev);
-      if (counter > 3 && r > RLO && r < RHI) break;
+      // m / m_prev within (RLO, RHI), m and m_prev positive
+      if (counter > 3 && m > RLO * m_prev && m < RHI * m_prev) break;
       m_prev = m;
     }
     lnv = s0 - log1pf(1.f / dnew);

@@ -163,6 +163,15 @@ class MarkerInCell:
     def synchronize(self):
         call("v2c_synchronize", self.h)
 
+    def calc_timestep(self, oldornew: int = 0, **ctl) -> dict:
+        """calc_timestep (calc_RSF.c:352): dt_f, the maximum slip rate, the
+        individual limits and the sticky-air statistics.  ctl overrides
+        abi.TIMESTEP_DEFAULTS (maxtmstep, dtfactor, tcnvp, tcd, tcphih)."""
+        c = abi.TimestepCtl(**dict(abi.TIMESTEP_DEFAULTS, **ctl))
+        info = abi.TimestepInfo()
+        call("v2c_calc_timestep", self.h, int(oldornew), ctypes.byref(c), ctypes.byref(info))
+        return info.to_dict()
+
     def status(self) -> dict:
         s = abi.Status()
         call("v2c_get_status", self.h, ctypes.byref(s))

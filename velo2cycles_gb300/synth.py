@@ -410,5 +410,19 @@ def make_case(name: str = "small", seed: int = 0, n_markers: int | None = None,
     nodes[abi.NF_NU] = nodes[abi.NF_NU_M2C].copy()
     nodes[abi.NF_GG] = np.full(nn, 3.0e10)
     nodes[abi.NF_TK] = _temperature(yb + oy, YS)
+    # fields the adaptive time step reads (calc_RSF.c:352-572): pressure at
+    # basic nodes, bulk modulus, nodal friction parameters with the
+    # velocity-weakening band, sticky-air flags, some very stiff nodes
+    nodes[abi.NF_PRS] = 3000.0 * 9.81 * (yb + oy) + 10e6 + rng.normal(0, 1e4, nn)
+    nodes[abi.NF_BM] = 5.0e10 * (1 + 0.1 * rng.uniform(size=nn))
+    band = np.abs(yb + oy - 10e3) <= 100.0
+    nodes[abi.NF_AS] = np.where(band, p["a_vw"], p["a_hr"]) * (1 + 0.01 * rng.uniform(size=nn))
+    nodes[abi.NF_BS] = np.where(band, p["b_vw"], p["b_hr"]) * (1 + 0.01 * rng.uniform(size=nn))
+    nodes[abi.NF_LS] = np.where(band, p["L_vw"], p["L_hr"]) * (1 + 0.01 * rng.uniform(size=nn))
+    nodes[abi.NF_V0S] = np.where(band, p["V0_vw"], p["V0_hr"])
+    nodes[abi.NF_STICKY01] = rng.choice([0.0, 1.0, 2.0], size=nn, p=[0.6, 0.3, 0.1])
+    stiff = rng.uniform(size=nn) < 0.2
+    nodes[abi.NF_NU_M2C][stiff] = 10.0 ** rng.uniform(26, 27, int(stiff.sum()))
+    nodes[abi.NF_NU][stiff] = nodes[abi.NF_NU_M2C][stiff] * 0.5
     bondm, bondn, bondv = _bonds(xn, yn)
     return Case(name, p, gx, gy, rt, nodes, marks, t, bondm, bondn, bondv)
