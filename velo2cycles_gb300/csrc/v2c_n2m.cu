@@ -23,7 +23,7 @@ namespace {
 
 constexpr int TY = 32;
 constexpr int NTH = 4 * TY;
-constexpr int CHUNK = 512;
+constexpr int CHUNK = 384;
 
 enum { Q_U = 0, Q_V, Q_PHIS, Q_SXY, Q_EXY, Q_ES, Q_PR, Q_SXX, Q_EXX, Q_VX, Q_VY, Q_MRO, Q_N };
 
@@ -113,7 +113,7 @@ __device__ __forceinline__ void allinteri(const Grid &g, const Nodes &N, const f
     A[4].add(w);                                                        \
   } while (0)
 
-__global__ void __launch_bounds__(NTH, 6) k_n2m(N2MArgs a) {
+__global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
   __shared__ Smem sm;
   const Grid &g = a.g;
   const Nodes &N = a.N;
