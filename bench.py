@@ -60,10 +60,10 @@ UNIT = "markers/s"
 #   n2m:  reads cell, u, v, type, T 17 B; writes the 9 updated fields 36 B;
 #         19 node fields read, 15 back-scatter sums written
 #   move: reads cell, u, v, type, T, sxx, sxy 25 B; writes cell, u, v, sxx,
-#         sxy 20 B; 5 node fields read (vx, vy, esp and the two pressure-node
-#         velocity averages)
+#         sxy 20 B; 3 node fields read (vx, vy, esp; the per-quarter
+#         velocity forms built from them are an intermediate, not counted)
 ALG_BYTES = {"m2n": 57 + 4, "n2m": 17 + 36, "move": 25 + 20}
-NODE_FIELDS = {"m2n": 18 + 39, "n2m": 19 + 15, "move": 5}
+NODE_FIELDS = {"m2n": 18 + 39, "n2m": 19 + 15, "move": 3}
 STEP_MARKER_BYTES = 57 + 48
 STEP_NODE_FIELDS = 94
 
@@ -391,17 +391,19 @@ def run_gpu(args, rank: int, world: int) -> None:
     from velo2cycles_gb300._lib import call
 
     dp = ctypes.POINTER(ctypes.c_double)
+    down_f = (ctypes.c_int * len(down))(*down.keys())
+    down_p = (dp * len(down))(*[a.ctypes.data_as(dp) for a in down.values()])
+    up_f = (ctypes.c_int * len(up))(*up.keys())
+    up_p = (dp * len(up))(*[a.ctypes.data_as(dp) for a in up.values()])
 
     def e2e_step(dt):
         m.set_params(timestep=float(dt))
         m.marker2nodes()
-        for f, a in down.items():
-            call("v2c_download_node_field", m.h, f, a.ctypes.data_as(dp))
+        call("v2c_download_node_fields", m.h, len(down), down_f, down_p)
         m.interpolate_center2basic_old()
         m.compute_before_solve(dt, 0)
         m.compute_after_solve(dt, 0)
-        for f, a in up.items():
-            call("v2c_upload_node_field", m.h, f, a.ctypes.data_as(dp))
+        call("v2c_upload_node_fields", m.h, len(up), up_f, up_p)
         m.nodes2markers_move()
 
     ms_e2e = None

@@ -189,8 +189,11 @@ typedef struct v2c_ctx v2c_ctx;
 
 /* ================================================================ life cycle
  * Replaces the static allocation of headevps.c:8-21 (MAXXLN/MAXYLN/MAXMRK):
- * capacities are fixed per context.  stream may be NULL (the per-thread
- * default stream is then not used; the context creates its own). */
+ * capacities are fixed per context, max_markers below 2^30 (else
+ * V2C_ERR_CAPACITY).  stream may be NULL (the per-thread default stream is
+ * then not used; the context creates its own).  The context keeps its
+ * markers sorted by cell and, within a cell, by quarter (u > 1/2, v > 1/2)
+ * and array index; markers keep the reference numbering at the boundary. */
 int v2c_create(const v2c_params *p, long max_markers, void *cuda_stream,
                v2c_ctx **out);
 int v2c_destroy(v2c_ctx *ctx);
@@ -222,9 +225,24 @@ int v2c_download_markers(v2c_ctx *ctx, double *const *fields,
  * ix*(ynumy-1)+iy with ix = nxsearch(x), iy = nysearch(y). */
 int v2c_download_cells(v2c_ctx *ctx, int32_t *cell, long n);
 
-/* ============================================================= node arrays */
+/* ============================================================= node arrays
+ * One node field (V2C_NF_*) of nodenum doubles, converted to / from the
+ * device's FP32.  The download returns when dst is filled.  The upload is
+ * asynchronous on the context stream: from pinned host memory the copy runs
+ * later, so src must stay unchanged until a call that synchronises the
+ * stream (any download, v2c_synchronize). */
 int v2c_upload_node_field(v2c_ctx *ctx, int field, const double *src);
 int v2c_download_node_field(v2c_ctx *ctx, int field, double *dst);
+/* count fields at once (fields[k] a V2C_NF_* id, src[k] / dst[k] nodenum
+ * doubles each, count <= V2C_NF_N): one conversion kernel over all of them
+ * and one copy per field back to back, one synchronisation at the end of
+ * the download; the upload is asynchronous as above.  The first call with
+ * more fields than any earlier one allocates a device staging area of
+ * count x nodenum doubles (synchronising the stream).  No counterpart in
+ * the reference, whose node arrays are host memory. */
+int v2c_upload_node_fields(v2c_ctx *ctx, int count, const int *fields,
+                           const double *const *src);
+int v2c_download_node_fields(v2c_ctx *ctx, int count, const int *fields, double *const *dst);
 
 /* ======================================================= the MIC step calls
  * Reference equivalents in brackets.  All are asynchronous on the context
@@ -356,8 +374,8 @@ int v2c_mlp_infer(v2c_ctx *ctx, const double *states_dev, long n, float *out_dev
  * No counterpart in the reference (its marker loops never sort).  Computes,
  * for n markers at device positions x_dev[n], y_dev[n] on the device grid
  * lines gx_dev[xnumx], gy_dev[ynumy], the same cell index as the context
- * path (cell_dev[i] = nxsearch(x)*(ynumy-1) + nysearch(y), bit-exact) and the
- * same stable counting sort by cell: perm_dev[start_dev[c] ..
+ * path (cell_dev[i] = nxsearch(x)*(ynumy-1) + nysearch(y), bit-exact) and a
+ * stable counting sort by cell: perm_dev[start_dev[c] ..
  * start_dev[c+1]) lists the markers of cell c in ascending index, and
  * start_dev has (xnumx-1)*(ynumy-1)+1 entries.  All pointers are device
  * pointers; the work is queued on cuda_stream (a cudaStream_t, NULL for the

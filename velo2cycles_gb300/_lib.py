@@ -39,6 +39,8 @@ _SIGS = {
     "v2c_download_cells": [c_ctx, P(ctypes.c_int32), ctypes.c_long],
     "v2c_upload_node_field": [c_ctx, ctypes.c_int, c_dp],
     "v2c_download_node_field": [c_ctx, ctypes.c_int, c_dp],
+    "v2c_upload_node_fields": [c_ctx, ctypes.c_int, P(ctypes.c_int), P(c_dp)],
+    "v2c_download_node_fields": [c_ctx, ctypes.c_int, P(ctypes.c_int), P(c_dp)],
     "v2c_marker2nodes": [c_ctx],
     "v2c_center2basic_old": [c_ctx],
     "v2c_compute_before_solve": [c_ctx, ctypes.c_double, ctypes.c_int],

@@ -122,19 +122,20 @@ static int v2c_bind_setup(void) {
 }
 
 static int v2c_bind_nodes_up(void) {
-  for (int k = 0; k < V2C_NF_N; k++)
-    if (!v2c_bind_ok(v2c_upload_node_field(v2c_bind_ctx, k, v2c_bind_node_array(k)),
-                     "v2c_upload_node_field"))
-      return 0;
-  return 1;
+  int fields[V2C_NF_N];
+  const double *src[V2C_NF_N];
+  for (int k = 0; k < V2C_NF_N; k++) {
+    fields[k] = k;
+    src[k] = v2c_bind_node_array(k);
+  }
+  return v2c_bind_ok(v2c_upload_node_fields(v2c_bind_ctx, V2C_NF_N, fields, src),
+                     "v2c_upload_node_fields");
 }
 
 static void v2c_bind_nodes_down(const int *fields, int nf) {
-  for (int k = 0; k < nf; k++)
-    if (!v2c_bind_ok(v2c_download_node_field(v2c_bind_ctx, fields[k],
-                                             v2c_bind_node_array(fields[k])),
-                     "v2c_download_node_field"))
-      return;
+  double *dst[V2C_NF_N];
+  for (int k = 0; k < nf; k++) dst[k] = v2c_bind_node_array(fields[k]);
+  v2c_bind_ok(v2c_download_node_fields(v2c_bind_ctx, nf, fields, dst), "v2c_download_node_fields");
 }
 
 void v2c_bind_markers_to_host(void) {

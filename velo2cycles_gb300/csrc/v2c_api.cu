@@ -43,8 +43,10 @@ struct v2c_ctx {
   // nodes
   float *d_node = nullptr;
   double *d_node64 = nullptr;  // boundary staging, one FP64 node field
+  double *d_nstage = nullptr;  // boundary staging of several node fields
+  int nstage_cap = 0;          // fields d_nstage holds
   uint32_t *d_sticky = nullptr;
-  float *d_vxp = nullptr, *d_vyp = nullptr;  // move: velocities at pressure nodes
+  float4 *d_quad = nullptr;                  // move: velocity forms per cell quarter
   unsigned *d_list_n = nullptr;              // count of listed Newton problems
   double *d_ts = nullptr;                    // calc_timestep scratch
   // markers
@@ -156,6 +158,29 @@ Scal make_scal(const v2c_params &p, const std::vector<double> &rt) {
   s.sticky_nu = (float)(gg2 * p.timestep / 100);
   s.ln_nubeg = (float)log(p.nubeg);
   s.ln_nuend = (float)log(p.nuend);
+  s.fault_y_f = (float)p.fault_y;
+  s.fault_slope_f = (float)p.fault_slope;
+  s.fault_hw1_f = (float)p.fault_hw + 1.0f;
+  s.a_hr_f = (float)p.a_hr; s.b_hr_f = (float)p.b_hr;
+  s.L_hr_f = (float)p.L_hr; s.V0_hr_f = (float)p.V0_hr;
+  s.tdeep_f = (float)p.tdeep;
+  s.zdeep_f = (float)p.zdeep;
+  s.zdeep_lo_f = s.zdeep_f - 1.f - 1e-6f * fabsf(s.zdeep_f);
+  s.eps2_f = (float)p.eps2;
+  s.nstress_f = (float)p.nstress;
+  s.nubeg_f = (float)p.nubeg;
+  s.nuend_f = (float)p.nuend;
+  s.faultwidth_f = (float)p.faultwidth;
+  auto split = [](double d, float &hi, float &lo) {
+    hi = (float)d;
+    lo = (float)(d - (double)hi);
+  };
+  split(p.timestep, s.dt_hi, s.dt_lo);
+  split(p.faultwidth, s.W_hi, s.W_lo);
+  split(p.nstress, s.sn_hi, s.sn_lo);
+  s.sppe_nstress = (p.timesum == 0 && p.reloadfromDP == 0 && p.compressiblemode == 1);
+  s.timesum_pos = p.timesum > 0;
+  s.timesum_zero = p.timesum == 0;
   return s;
 }
 
@@ -192,6 +217,7 @@ int pick_tx(const v2c_ctx *c) {
 extern "C" int v2c_create(const v2c_params *p, long max_markers, void *cuda_stream,
                           v2c_ctx **out) {
   if (!p || !out || max_markers < 0) return V2C_ERR_ARG;
+  if (max_markers >= SORT_MAX_MARKERS) return V2C_ERR_CAPACITY;
   int rc = check_params(p);
   if (rc) return rc;
   int dev = 0;
@@ -221,7 +247,7 @@ extern "C" int v2c_create(const v2c_params *p, long max_markers, void *cuda_stre
   AL(ctx->d_node, (size_t)V2C_NF_N * ctx->nn);
   AL(ctx->d_node64, ctx->nn);
   AL(ctx->d_sticky, ctx->nn);
-  AL(ctx->d_vxp, ctx->nn); AL(ctx->d_vyp, ctx->nn);
+  AL(ctx->d_quad, (size_t)ctx->ncell * QUAD_FLOAT4);
   AL(ctx->d_list_n, 1);
   AL(ctx->d_ts, TIMESTEP_SCRATCH);
   AL(ctx->d_stat, ST_N);
@@ -246,6 +272,7 @@ extern "C" int v2c_create(const v2c_params *p, long max_markers, void *cuda_stre
   ctx->n_marker_mem = k;
   // sort
   AL(ctx->sb.counts, ctx->ncell); AL(ctx->sb.start, ctx->ncell + 1);
+  AL(ctx->sb.qstart, ctx->ncell + 1);
   AL(ctx->sb.slot, cap); AL(ctx->sb.tmp, cap); AL(ctx->sb.perm, cap);
   ctx->sb.blocksum_cap = (ctx->ncell + 4095) / 4096 + 1;
   AL(ctx->sb.blocksum, ctx->sb.blocksum_cap);
@@ -261,9 +288,9 @@ extern "C" int v2c_destroy(v2c_ctx *ctx) {
   if (!ctx) return V2C_ERR_ARG;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   void *ptrs[] = {ctx->d_gx, ctx->d_gy, ctx->d_wx, ctx->d_wy, ctx->d_gxf, ctx->d_gyf,
-                  ctx->d_rock, ctx->d_node, ctx->d_node64, ctx->d_sticky, ctx->d_vxp, ctx->d_vyp, ctx->d_list_n, ctx->d_ts,
-                  ctx->d_stat, ctx->d_red,
-                  ctx->sb.counts, ctx->sb.start, ctx->sb.slot, ctx->sb.tmp, ctx->sb.perm,
+                  ctx->d_rock, ctx->d_node, ctx->d_node64, ctx->d_sticky, ctx->d_quad, ctx->d_list_n, ctx->d_ts,
+                  ctx->d_stat, ctx->d_red, ctx->d_nstage,
+                  ctx->sb.counts, ctx->sb.start, ctx->sb.qstart, ctx->sb.slot, ctx->sb.tmp, ctx->sb.perm,
                   ctx->sb.blocksum, ctx->d_stage64, ctx->d_stage64b, ctx->bc_mem,
                   ctx->d_bc_scratch};
   for (void *q : ptrs)
@@ -533,7 +560,7 @@ extern "C" int v2c_upload_markers(v2c_ctx *ctx, const double *const *fields,
   CK(cudaMemsetAsync(m.mkt, 0, sizeof(float) * n, st));
   CK(cudaMemsetAsync(m.mro, 0, sizeof(float) * n, st));
   // sort once and store the markers physically in cell order
-  launch_sort(m.cell_in, n, ctx->ncell, ctx->sb, ctx->d_stat, st);
+  launch_sort(m.cell_in, m.u_in, m.v_in, n, ctx->ncell, ctx->sb, ctx->d_stat, st);
   const int32_t *perm = ctx->sb.perm;
   float *tmpf = (float *)ctx->d_stage64;
   int32_t *tmpi = (int32_t *)ctx->d_stage64;
@@ -551,7 +578,7 @@ extern "C" int v2c_upload_markers(v2c_ctx *ctx, const double *const *fields,
   launch_gather_i8(m.type, perm, (int8_t *)tmpi, n, st);
   CK(cudaMemcpyAsync(m.type, tmpi, n, cudaMemcpyDeviceToDevice, st));
   // the physical order is now sorted: sort again to get the identity perm
-  launch_sort(m.cell_in, n, ctx->ncell, ctx->sb, ctx->d_stat, st);
+  launch_sort(m.cell_in, m.u_in, m.v_in, n, ctx->ncell, ctx->sb, ctx->d_stat, st);
   CK(cudaStreamSynchronize(st));
   CK(cudaGetLastError());
   ctx->have_markers = true;
@@ -634,6 +661,57 @@ extern "C" int v2c_download_node_field(v2c_ctx *ctx, int field, double *dst) {
   return V2C_OK;
 }
 
+static int node_field_list_ok(int count, const int *fields, const void *const *ptrs) {
+  if (count < 0 || count > V2C_NF_N || (count > 0 && (!fields || !ptrs))) return 0;
+  for (int k = 0; k < count; k++)
+    if (fields[k] < 0 || fields[k] >= V2C_NF_N || !ptrs[k]) return 0;
+  return 1;
+}
+
+static int grow_node_stage(v2c_ctx *ctx, int count) {
+  if (count <= ctx->nstage_cap) return V2C_OK;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->d_nstage) cudaFree(ctx->d_nstage);
+  ctx->d_nstage = nullptr;
+  ctx->nstage_cap = 0;
+  CK(cudaMalloc(&ctx->d_nstage, sizeof(double) * ctx->nn * count));
+  ctx->nstage_cap = count;
+  return V2C_OK;
+}
+
+extern "C" int v2c_upload_node_fields(v2c_ctx *ctx, int count, const int *fields,
+                                      const double *const *src) {
+  if (!ctx) return V2C_ERR_ARG;
+  if (!node_field_list_ok(count, fields, (const void *const *)src)) return fail(ctx, V2C_ERR_ARG);
+  if (count == 0) return V2C_OK;
+  int rc = grow_node_stage(ctx, count);
+  if (rc) return fail(ctx, rc);
+  for (int k = 0; k < count; k++)
+    CK(cudaMemcpyAsync(ctx->d_nstage + (long)k * ctx->nn, src[k], sizeof(double) * ctx->nn,
+                       cudaMemcpyHostToDevice, ctx->stream));
+  launch_fields_to_f32(ctx->d_nstage, ctx->nn, fields, count, ctx->d_node, ctx->stream);
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  return V2C_OK;
+}
+
+extern "C" int v2c_download_node_fields(v2c_ctx *ctx, int count, const int *fields,
+                                        double *const *dst) {
+  if (!ctx) return V2C_ERR_ARG;
+  if (!node_field_list_ok(count, fields, (const void *const *)dst)) return fail(ctx, V2C_ERR_ARG);
+  if (count == 0) return V2C_OK;
+  int rc = grow_node_stage(ctx, count);
+  if (rc) return fail(ctx, rc);
+  launch_fields_to_f64(ctx->d_node, ctx->nn, fields, count, ctx->d_nstage, ctx->stream);
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  for (int k = 0; k < count; k++)
+    CK(cudaMemcpyAsync(dst[k], ctx->d_nstage + (long)k * ctx->nn, sizeof(double) * ctx->nn,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return V2C_OK;
+}
+
 // ============================================================ the MIC step
 static int ready(v2c_ctx *ctx) {
   if (!ctx) return V2C_ERR_ARG;
@@ -653,7 +731,8 @@ extern "C" int v2c_marker2nodes(v2c_ctx *ctx) {
   cudaStream_t st = ctx->stream;
   if (!ctx->sorted) {
     Prof pr(ctx, V2C_PROF_SORT);
-    launch_sort(ctx->m.cell_in, ctx->n, ctx->ncell, ctx->sb, ctx->d_stat, st);
+    launch_sort(ctx->m.cell_in, ctx->m.u_in, ctx->m.v_in, ctx->n, ctx->ncell, ctx->sb,
+                ctx->d_stat, st);
     ctx->launches += ctx->n > 0 ? 6 : 3;
     ctx->sorted = true;
   }
@@ -669,6 +748,7 @@ extern "C" int v2c_marker2nodes(v2c_ctx *ctx) {
   a.S = make_scal(ctx->p, ctx->h_rt);
   a.perm = ctx->sb.perm;
   a.start = ctx->sb.start;
+  a.qstart = ctx->sb.qstart;
   a.sticky_key = ctx->d_sticky;
   a.stat = ctx->d_stat;
   a.gxf = ctx->d_gxf;
@@ -772,7 +852,8 @@ static int n2m_move(v2c_ctx *ctx, int do_n2m, int do_move) {
   cudaStream_t st = ctx->stream;
   if (!ctx->sorted) {
     Prof pr(ctx, V2C_PROF_SORT);
-    launch_sort(ctx->m.cell_in, ctx->n, ctx->ncell, ctx->sb, ctx->d_stat, st);
+    launch_sort(ctx->m.cell_in, ctx->m.u_in, ctx->m.v_in, ctx->n, ctx->ncell, ctx->sb,
+                ctx->d_stat, st);
     ctx->launches += ctx->n > 0 ? 6 : 3;
     ctx->sorted = true;
   }
@@ -784,10 +865,10 @@ static int n2m_move(v2c_ctx *ctx, int do_n2m, int do_move) {
   a.S = make_scal(ctx->p, ctx->h_rt);
   a.perm = ctx->sb.perm;
   a.start = ctx->sb.start;
+  a.qstart = ctx->sb.qstart;
   a.stat = ctx->d_stat;
   a.gyf = ctx->d_gyf;
-  a.vxp = ctx->d_vxp;
-  a.vyp = ctx->d_vyp;
+  a.quad = ctx->d_quad;
   a.n = ctx->n;
   a.TX = pick_tx(ctx);
   a.do_n2m = 1;
@@ -806,7 +887,8 @@ static int n2m_move(v2c_ctx *ctx, int do_n2m, int do_move) {
     swap_positions(ctx);
     // next step's order: counting sort of the new cells
     Prof pr(ctx, V2C_PROF_SORT);
-    launch_sort(ctx->m.cell_in, ctx->n, ctx->ncell, ctx->sb, ctx->d_stat, st);
+    launch_sort(ctx->m.cell_in, ctx->m.u_in, ctx->m.v_in, ctx->n, ctx->ncell, ctx->sb,
+                ctx->d_stat, st);
     ctx->launches += ctx->n > 0 ? 6 : 3;
   }
   CK(cudaGetLastError());

@@ -77,6 +77,19 @@ struct Scal {
   float dt;
   float sticky_nu;  // markgg[2]*timestep/100
   float ln_nubeg, ln_nuend;
+  // FP32 copies of the double parameters that per-marker and per-node code
+  // reads, rounded once here: in a kernel every double->float conversion or
+  // double compare issues on the FP64 pipe, 1/64 of the FP32 rate on this GPU
+  float fault_y_f, fault_slope_f;
+  float fault_hw1_f;  // (float)fault_hw + 1: far-field test margin
+  float a_hr_f, b_hr_f, L_hr_f, V0_hr_f;
+  float tdeep_f, zdeep_f;
+  float zdeep_lo_f;   // (float)zdeep - 1 - 1e-6 |zdeep|: coarse depth test
+  float eps2_f, nstress_f, nubeg_f, nuend_f, faultwidth_f;
+  float dt_hi, dt_lo, W_hi, W_lo, sn_hi, sn_lo;  // float-float timestep, faultwidth, nstress
+  int sppe_nstress;   // timesum == 0 && reloadfromDP == 0 && compressiblemode == 1
+  int timesum_pos;    // timesum > 0
+  int timesum_zero;   // timesum == 0
 };
 
 // ----------------------------------------------------- compensated sums

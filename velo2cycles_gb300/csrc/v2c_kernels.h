@@ -9,6 +9,7 @@ namespace v2c {
 struct SortBufs {
   int32_t *counts;   // [ncell]
   int32_t *start;    // [ncell+1]
+  int4 *qstart;      // [ncell+1]: start of each quarter class of a cell (see launch_sort)
   int32_t *slot;     // [cap]
   int32_t *tmp;      // [cap]
   int32_t *perm;     // [cap]
@@ -16,9 +17,13 @@ struct SortBufs {
   long blocksum_cap;
 };
 
-// sort markers by cell (stable by array index): perm and start
-void launch_sort(const int32_t *cell, long n, long ncell, SortBufs &b,
-                 unsigned long long *stat, cudaStream_t st);
+// Sort markers by cell, within a cell by quarter class
+// q = 2 (v > 1/2) + (u > 1/2), within a class by array index: perm, start
+// and qstart (x, y, z, w = first sorted position of class 0, 1, 2, 3 of
+// the cell; qstart[ncell].x = n).  Array indices must be below 2^30.
+constexpr long SORT_MAX_MARKERS = 1L << 30;
+void launch_sort(const int32_t *cell, const float *u, const float *v, long n, long ncell,
+                 SortBufs &b, unsigned long long *stat, cudaStream_t st);
 
 // marker2nodes sweep (scatter + node tail) and its follow-ups
 struct M2NArgs {
@@ -29,6 +34,7 @@ struct M2NArgs {
   Scal S;
   const int32_t *perm;
   const int32_t *start;
+  const int4 *qstart;
   uint32_t *sticky_key;
   unsigned long long *stat;
   const float *gxf, *gyf;  // FP32 line positions (coarse band test)
@@ -78,6 +84,12 @@ struct BcRows {
 void launch_bc(const BcRows &rows, const Nodes &N, float *scratch, cudaStream_t st);
 void launch_node_to_f32(const double *src, float *dst, long n, cudaStream_t st);
 void launch_node_to_f64(const float *src, double *dst, long n, cudaStream_t st);
+// count node fields (ids in fields[], count <= V2C_NF_N) to / from a staging
+// area of count x nn doubles in list order
+void launch_fields_to_f64(const float *base, long nn, const int *fields, int count, double *stage,
+                          cudaStream_t st);
+void launch_fields_to_f32(const double *stage, long nn, const int *fields, int count, float *base,
+                          cudaStream_t st);
 
 void launch_c2b_old(const Grid &g, const Nodes &N, cudaStream_t st);
 void launch_before_solve(const Grid &g, const Nodes &N, const Scal &S, double dt, int rk,
@@ -94,13 +106,16 @@ struct N2MArgs {
   Scal S;
   const int32_t *perm;
   const int32_t *start;
+  const int4 *qstart;
   unsigned long long *stat;
   const float *gyf;  // FP32 line positions (coarse depth test)
-  float *vxp, *vyp;  // velocities averaged to pressure nodes [nn] (scratch)
+  float4 *quad;      // allinteri's bilinear forms per cell quarter [ncell * QUAD_FLOAT4]
   long n;            // markers
   int TX;
   int do_n2m;
 };
+// float4 coefficient sets per cell: 4 quarters x (VX, VY, ESP)
+constexpr int QUAD_FLOAT4 = 12;
 // nodes2markers: gather, marker update, back-scatter (cell-column tiles)
 void launch_n2m(const N2MArgs &a, cudaStream_t st);
 // moveandrotatemarkers: one thread per marker, new positions to *_out

@@ -128,10 +128,11 @@ __device__ __noinline__ void friction_node(const v2c_params &p, double x, double
 __device__ __forceinline__ void node_friction(const M2NArgs &a, int ci, int j, float &mu,
                                               float &fa, float &fb, float &fL, float &fV0) {
   const v2c_params &p = a.S.p;
+  const Scal &S = a.S;
   const float xf = __ldg(a.gxf + ci), yf = __ldg(a.gyf + j);
-  const float rad = fabsf(yf - ((float)p.fault_y + (float)p.fault_slope * xf));
-  if (rad > (float)p.fault_hw + 1.0f) {
-    mu = 0.6f; fa = (float)p.a_hr; fb = (float)p.b_hr; fL = (float)p.L_hr; fV0 = (float)p.V0_hr;
+  const float rad = fabsf(yf - (S.fault_y_f + S.fault_slope_f * xf));
+  if (rad > S.fault_hw1_f) {
+    mu = 0.6f; fa = S.a_hr_f; fb = S.b_hr_f; fL = S.L_hr_f; fV0 = S.V0_hr_f;
     return;
   }
   double dmu, da, db, dL, dV0;
@@ -187,16 +188,18 @@ __global__ void __launch_bounds__(NTH, 6) k_m2n(M2NArgs a) {
       const int jlo = max(j0 - 1, 0), jhi = min(j0 + TY - 1, ncy - 1);
       const long cb = (long)ci * ncy;
       const int seg_b = __ldg(a.start + cb + jlo), seg_e = __ldg(a.start + cb + jhi + 1);
-      int lo_b = 0, lo_e = 0, up_b = 0, up_e = 0;
+      // quarter class starts of cell (ci, j-1) (lower) and (ci, j) (upper)
+      int4 ql = make_int4(0, 0, 0, 0), qu = make_int4(0, 0, 0, 0);
+      int lo_e = 0, up_e = 0;
       float s1lo = 0.f, s1up = 0.f;
       const float iwx = 1.f / __ldg(g.wx + ci);
       if (jvalid && j - 1 >= 0 && j - 1 <= ncy - 1) {
-        lo_b = __ldg(a.start + cb + j - 1);
+        ql = __ldg(a.qstart + cb + j - 1);
         lo_e = __ldg(a.start + cb + j);
         s1lo = iwx / __ldg(g.wy + j - 1);
       }
       if (jvalid && j <= ncy - 1) {
-        up_b = __ldg(a.start + cb + j);
+        qu = __ldg(a.qstart + cb + j);
         up_e = __ldg(a.start + cb + j + 1);
         s1up = iwx / __ldg(g.wy + j);
       }
@@ -205,62 +208,97 @@ __global__ void __launch_bounds__(NTH, 6) k_m2n(M2NArgs a) {
         __syncthreads();
         for (int k = tid; k < ce - cs; k += NTH) stage(a, sm, cs + k, k);
         __syncthreads();
-        // cell (ci, j-1): bottom halves (v > 0.5) reach node row j
-        for (int s = max(lo_b, cs); s < min(lo_e, ce); ++s) {
-          const int q = s - cs;
-          if (!sm.act[q]) continue;
-          const float u = sm.p[P_U][q], v = sm.p[P_V][q];
-          if (role <= 1) {
-            if (!(v > 0.5f)) continue;
+// the staged markers of sorted positions [b, e) (one quarter class run)
+#define CLASS_RUN(b, e) \
+  for (int s = max((b), cs), s_e = min((e), ce), q = s - cs; s < s_e; ++s, q = s - cs) \
+    if (sm.act[q])
+        if (role <= 1) {
+          // cell (ci, j-1), bottom halves (v > 1/2): class 2 left, class 3 right
+          CLASS_RUN(ql.z, ql.w) {
+            const float u = sm.p[P_U][q], v = sm.p[P_V][q];
             if (u < 0.5f) {
               const float w = s1lo * (1.f - 2.f * u) * (2.f * v - 1.f);
               if (role == 0) ADD_BASIC_A(cur, q, w); else ADD_BASIC_B(cur, q, w);
-            } else if (u > 0.5f) {
-              const float w = s1lo * (2.f * u - 1.f) * (2.f * v - 1.f);
-              if (role == 0) ADD_BASIC_A(car, q, w); else ADD_BASIC_B(car, q, w);
-            }
-          } else if (role == 3) {
-            if (v > 0.5f) {
-              const float w = s1lo * (1.f - fabsf(u - 0.5f)) * v;
-              const float ro = sm.p[P_RO][q];
-              vy3[0].add(sm.p[P_VY][q] * ro * w); vy3[1].add(ro * w); vy3[2].add(w);
             }
           }
-        }
-        // cell (ci, j): top halves reach node row j, the whole cell its centre
-        for (int s = max(up_b, cs); s < min(up_e, ce); ++s) {
-          const int q = s - cs;
-          if (!sm.act[q]) continue;
-          const float u = sm.p[P_U][q], v = sm.p[P_V][q];
-          if (role <= 1) {
-            if (!(v < 0.5f)) continue;
-            if (u < 0.5f) {
+          CLASS_RUN(ql.w, lo_e) {
+            const float u = sm.p[P_U][q], v = sm.p[P_V][q];
+            const float w = s1lo * (2.f * u - 1.f) * (2.f * v - 1.f);
+            if (role == 0) ADD_BASIC_A(car, q, w); else ADD_BASIC_B(car, q, w);
+          }
+          // cell (ci, j), top halves (v < 1/2): class 0 left, class 1 right
+          CLASS_RUN(qu.x, qu.y) {
+            const float u = sm.p[P_U][q], v = sm.p[P_V][q];
+            if (u < 0.5f && v < 0.5f) {
               const float w = s1up * (1.f - 2.f * u) * (1.f - 2.f * v);
               if (role == 0) ADD_BASIC_A(cur, q, w); else ADD_BASIC_B(cur, q, w);
-            } else if (u > 0.5f) {
+            }
+          }
+          CLASS_RUN(qu.y, qu.z) {
+            const float u = sm.p[P_U][q], v = sm.p[P_V][q];
+            if (v < 0.5f) {
               const float w = s1up * (2.f * u - 1.f) * (1.f - 2.f * v);
               if (role == 0) ADD_BASIC_A(car, q, w); else ADD_BASIC_B(car, q, w);
             }
-          } else if (role == 2) {
+          }
+        } else if (role == 2) {
+          // the whole cell (ci, j) to its centre node
+          CLASS_RUN(qu.x, up_e) {
+            const float u = sm.p[P_U][q], v = sm.p[P_V][q];
             const float w = s1up * (1.f - 2.f * fabsf(u - 0.5f)) * (1.f - 2.f * fabsf(v - 0.5f));
             cur[0].add(sm.p[P_NU][q] * w); cur[1].add(sm.p[P_NUG][q] * w);
             cur[2].add(sm.p[P_SXX][q] * w); cur[3].add(sm.p[P_EXX][q] * w);
             cur[4].add(sm.p[P_P][q] * w); cur[5].add(w);
-          } else {
+          }
+        } else {
+          // vy node (ci, j) from the bottom halves of cell (ci, j-1)
+          CLASS_RUN(ql.z, lo_e) {
+            const float u = sm.p[P_U][q], v = sm.p[P_V][q];
+            const float w = s1lo * (1.f - fabsf(u - 0.5f)) * v;
+            const float ro = sm.p[P_RO][q];
+            vy3[0].add(sm.p[P_VY][q] * ro * w); vy3[1].add(ro * w); vy3[2].add(w);
+          }
+          // cell (ci, j): vx node (ci, j) from u < 1/2 (classes 0, 2), vx node
+          // (ci+1, j) from u > 1/2 (classes 1, 3), vy node (ci, j) from v < 1/2
+          // (classes 0, 1)
+          CLASS_RUN(qu.x, qu.y) {
+            const float u = sm.p[P_U][q], v = sm.p[P_V][q];
             const float ro = sm.p[P_RO][q];
             if (u < 0.5f) {
               const float w = s1up * (1.f - u) * (1.f - fabsf(v - 0.5f));
               cur[0].add(sm.p[P_VX][q] * ro * w); cur[1].add(ro * w); cur[2].add(w);
-            } else if (u > 0.5f) {
-              const float w = s1up * u * (1.f - fabsf(v - 0.5f));
-              car[0].add(sm.p[P_VX][q] * ro * w); car[1].add(ro * w); car[2].add(w);
             }
             if (v < 0.5f) {
               const float w = s1up * (1.f - fabsf(u - 0.5f)) * (1.f - v);
               vy3[0].add(sm.p[P_VY][q] * ro * w); vy3[1].add(ro * w); vy3[2].add(w);
             }
           }
+          CLASS_RUN(qu.y, qu.z) {
+            const float u = sm.p[P_U][q], v = sm.p[P_V][q];
+            const float ro = sm.p[P_RO][q];
+            const float wx = s1up * u * (1.f - fabsf(v - 0.5f));
+            car[0].add(sm.p[P_VX][q] * ro * wx); car[1].add(ro * wx); car[2].add(wx);
+            if (v < 0.5f) {
+              const float w = s1up * (1.f - fabsf(u - 0.5f)) * (1.f - v);
+              vy3[0].add(sm.p[P_VY][q] * ro * w); vy3[1].add(ro * w); vy3[2].add(w);
+            }
+          }
+          CLASS_RUN(qu.z, qu.w) {
+            const float u = sm.p[P_U][q], v = sm.p[P_V][q];
+            if (u < 0.5f) {
+              const float ro = sm.p[P_RO][q];
+              const float w = s1up * (1.f - u) * (1.f - fabsf(v - 0.5f));
+              cur[0].add(sm.p[P_VX][q] * ro * w); cur[1].add(ro * w); cur[2].add(w);
+            }
+          }
+          CLASS_RUN(qu.w, up_e) {
+            const float u = sm.p[P_U][q], v = sm.p[P_V][q];
+            const float ro = sm.p[P_RO][q];
+            const float w = s1up * u * (1.f - fabsf(v - 0.5f));
+            car[0].add(sm.p[P_VX][q] * ro * w); car[1].add(ro * w); car[2].add(w);
+          }
         }
+#undef CLASS_RUN
       }
     }
 
@@ -342,8 +380,7 @@ __global__ void __launch_bounds__(NTH, 6) k_m2n(M2NArgs a) {
           } else {
             sxxe = sxxen; sppe = sppen; exxe = exxen;
           }
-          if (a.S.p.timesum == 0 && a.S.p.reloadfromDP == 0 && a.S.p.compressiblemode == 1)
-            sppe = (float)a.S.p.nstress;
+          if (a.S.sppe_nstress) sppe = a.S.nstress_f;
           float nd = __fdividef(cur[0].value(), s1);
           N.f(V2C_NF_SXXEN)[mc] = sxxen; N.f(V2C_NF_SPPEN)[mc] = sppen;
           N.f(V2C_NF_EXXEN)[mc] = exxen; N.f(V2C_NF_SXXE)[mc] = sxxe;

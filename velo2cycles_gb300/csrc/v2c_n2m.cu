@@ -1,17 +1,19 @@
-// v2c_n2m.cu -- nodes2markers (interpolation.c:929-1490) fused with
-// moveandrotatemarkers (moveandrotatemarkers.c:1-178) in one marker pass.
+// v2c_n2m.cu -- nodes2markers (interpolation.c:929-1490) and
+// moveandrotatemarkers (moveandrotatemarkers.c:1-178).
 //
-// Same tiling as the marker2nodes sweep (see v2c_m2n.cu).  Staging a marker
-// gathers the 19 node fields of interpolate_mechanical from the four
-// staggered stencils in cell-local FP32 coordinates and keeps the quantities
-// the antidiffusion correction scatters back (PHIS, SXY, EXY, ES to basic
-// nodes, PR, SXX, EXX to the centre node, VX*MRO, VY*MRO and MRO to vx/vy
-// nodes).  The tile that owns the marker also applies the marker update and
-// then moves it (Euler or RK4 through four allinteri evaluations,
-// interpolation.c:1688-1758) and rotates its stress; new positions go to
-// the second position buffer so neighbouring tiles still see the old one.
+// nodes2markers: same tiling as the marker2nodes sweep (see v2c_m2n.cu).
+// Staging a marker gathers the 19 node fields of interpolate_mechanical from
+// the four staggered stencils in cell-local FP32 coordinates and keeps the
+// quantities the antidiffusion correction scatters back (PHIS, SXY, EXY, ES
+// to basic nodes, PR, SXX, EXX to the centre node, VX*MRO, VY*MRO and MRO to
+// vx/vy nodes); the tile that owns the marker applies the marker update.
 // The back-scatter sums are formed per node by one thread each, in sorted
 // marker order with two-sum compensation, exactly as in marker2nodes.
+//
+// moveandrotatemarkers: one thread per marker, Euler or RK4 through four
+// allinteri evaluations (interpolation.c:1688-1758) from per-quarter
+// bilinear forms, stress rotation; new positions go to the second position
+// buffer.
 #include <math.h>
 
 #include "v2c_kernels.h"
@@ -55,54 +57,130 @@ __device__ __forceinline__ void settle(const Grid &g, Pos &p, unsigned long long
   }
 }
 
-// allinteri's arithmetic (interpolation.c:1688-1758) from precomputed
-// stencils: spin at basic nodes (mb), the velocities averaged to pressure
-// nodes (vxp, vyp, see k_vel_pnodes) at the pressure stencil (mc), blended
-// with the staggered velocities VXs, VYs by xrat
-__device__ __forceinline__ void allinteri_from(const Nodes &N, const float *vxp, const float *vyp,
-                                               long yn, long mb, float eb, float nb, long mc,
-                                               float ec, float nc, float VXs, float VYs,
-                                               float xrat, float &VX, float &VY, float &ESP) {
-  ESP = bil(N.f(V2C_NF_ESP), mb, yn, eb, nb);
-  VX = bil(vxp, mc, yn, ec, nc) * (1.f - xrat) + VXs * xrat;
-  VY = bil(vyp, mc, yn, ec, nc) * (1.f - xrat) + VYs * xrat;
+// allinteri (interpolation.c:1688-1758) inside one quarter of a cell is a
+// bilinear function of the position: each stencil it reads (basic nodes for
+// the spin, pressure nodes for the velocities averaged in pairs, vx and vy
+// nodes for the staggered velocities) keeps its nodes across the quarter,
+// its weights are affine in X and Y, and the blend weight xrat is constant
+// there.  k_vel_quads writes, per quarter and per quantity (VX, VY, ESP),
+// the coefficients of f = c0 + c1 dX + c2 dY + c3 dX dY, with dX, dY in
+// metres from the quarter's lower corner; vel_at evaluates them.  Quarter
+// qx = 1 holds X >= wx/2 (allinteri: xrat and the vy stencil switch at
+// X < wx/2, the pressure stencil at X > wx/2, where it is continuous).
+
+// affine weight w = (X - A) / B of one stencil axis at the quarter's corner
+// X0: w = e0 + s (X - X0)
+struct Lin {
+  float e0, s;
+};
+__device__ __forceinline__ Lin lin_w(float X0, float A, float B) {
+  return Lin{__fdividef(X0 - A, B), __fdividef(1.f, B)};
 }
 
-// allinteri's weight of the staggered velocities: 2/3, or 1 in the outer
-// half of a boundary cell.  X, Y: clamped position in metres from the cell's
-// lines; wx, wy: the cell's widths.
-__device__ __forceinline__ float allinteri_xrat(const Grid &g, int ix, int iy, float X, float Y,
-                                                float wx, float wy) {
+// bilinear interpolation of f over nodes m3, m3+1, m3+yn, m3+yn+1 as
+// c0 + c1 dX + c2 dY + c3 dX dY
+__device__ __forceinline__ float4 bil_form(const float *f, long m3, long yn, Lin ex, Lin ny) {
+  const float f0 = __ldg(f + m3), f1 = __ldg(f + m3 + 1), f2 = __ldg(f + m3 + yn),
+              f3 = __ldg(f + m3 + yn + 1);
+  const float d20 = f2 - f0, d10 = f1 - f0, D = (f3 - f2) - d10;
+  float4 c;
+  c.x = f0 + ex.e0 * d20 + ny.e0 * (d10 + ex.e0 * D);
+  c.y = (d20 + ny.e0 * D) * ex.s;
+  c.z = (d10 + ex.e0 * D) * ny.s;
+  c.w = D * ex.s * ny.s;
+  return c;
+}
+
+// the pair sums of allinteri (interpolation.c:1730-1745) at pressure node
+// m (m has ix >= 1 and iy >= 1 on every pressure stencil)
+__device__ __forceinline__ float4 bil_form_pairs(const float *v, long o1, long o2, long m3,
+                                                 long yn, Lin ex, Lin ny) {
+  auto P = [&](long m) { return 0.5f * (__ldg(v + m - o1) + __ldg(v + m - o2)); };
+  const float f0 = P(m3), f1 = P(m3 + 1), f2 = P(m3 + yn), f3 = P(m3 + yn + 1);
+  const float d20 = f2 - f0, d10 = f1 - f0, D = (f3 - f2) - d10;
+  float4 c;
+  c.x = f0 + ex.e0 * d20 + ny.e0 * (d10 + ex.e0 * D);
+  c.y = (d20 + ny.e0 * D) * ex.s;
+  c.z = (d10 + ex.e0 * D) * ny.s;
+  c.w = D * ex.s * ny.s;
+  return c;
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__device__ __forceinline__ float4 blend(float4 p, float4 s, float xrat) {
+  const float r = 1.f - xrat;
+  return make_float4(p.x * r + s.x * xrat, p.y * r + s.y * xrat, p.z * r + s.z * xrat,
+                     p.w * r + s.w * xrat);
+}
+
+// one thread per cell quarter t = 4 cell + 2 qy + qx; stencils as in
+// stencil_basic / stencil_centre / stencil_vx / stencil_vy
+__global__ void k_vel_quads(Grid g, Nodes N, float4 *Q) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= (long)g.ncx * g.ncy * 4) return;
+  const long c = t >> 2;
+  const int qx = (int)(t & 1), qy = (int)((t >> 1) & 1);
+  const int ix = (int)(c / g.ncy), iy = (int)(c - (long)ix * g.ncy);
+  const Axis ax = make_axis(g.wx, g.ncx, ix, 0.f), ay = make_axis(g.wy, g.ncy, iy, 0.f);
+  const float X0 = qx ? 0.5f * ax.w : 0.f, Y0 = qy ? 0.5f * ay.w : 0.f;
+  const long yn = g.yn;
+  // spin at basic nodes
+  int mx = clampi(ix, 1, g.xn - 3), my = clampi(iy, 1, g.yn - 3);
+  int kx = mx - ix, ky = my - iy;
+  const float4 cE = bil_form(N.f(V2C_NF_ESP), (long)mx * yn + my, yn,
+                             lin_w(X0, ax.G(kx), ax.G(kx + 1) - ax.G(kx)),
+                             lin_w(Y0, ay.G(ky), ay.G(ky + 1) - ay.G(ky)));
+  // velocities averaged to pressure nodes
+  mx = clampi(ix + qx, 1, g.xn - 2); my = clampi(iy + qy, 1, g.yn - 2);
+  kx = mx - ix; ky = my - iy;
+  Lin ex = lin_w(X0, (ax.G(kx - 1) + ax.G(kx)) * 0.5f, (ax.G(kx + 1) - ax.G(kx - 1)) * 0.5f);
+  Lin ny = lin_w(Y0, (ay.G(ky - 1) + ay.G(ky)) * 0.5f, (ay.G(ky + 1) - ay.G(ky - 1)) * 0.5f);
+  const long mc = (long)mx * yn + my;
+  const float4 cPX = bil_form_pairs(N.f(V2C_NF_VX), 1, yn + 1, mc, yn, ex, ny);
+  const float4 cPY = bil_form_pairs(N.f(V2C_NF_VY), yn, yn + 1, mc, yn, ex, ny);
+  // vx nodes
+  mx = clampi(ix, 0, g.xn - 2); my = clampi(iy - (qy ? 0 : 1), 0, g.yn - 3);
+  kx = mx - ix; ky = my - iy;
+  const float4 cVX = bil_form(N.f(V2C_NF_VX), (long)mx * yn + my, yn,
+                              lin_w(X0, ax.G(kx), ax.G(kx + 1) - ax.G(kx)),
+                              lin_w(Y0, (ay.G(ky) + ay.G(ky + 1)) * 0.5f,
+                                    (ay.G(ky + 2) - ay.G(ky)) * 0.5f));
+  // vy nodes
+  mx = clampi(ix - (qx ? 0 : 1), 0, g.xn - 3); my = clampi(iy, 0, g.yn - 2);
+  kx = mx - ix; ky = my - iy;
+  const float4 cVY = bil_form(N.f(V2C_NF_VY), (long)mx * yn + my, yn,
+                              lin_w(X0, (ax.G(kx) + ax.G(kx + 1)) * 0.5f,
+                                    (ax.G(kx + 2) - ax.G(kx)) * 0.5f),
+                              lin_w(Y0, ay.G(ky), ay.G(ky + 1) - ay.G(ky)));
+  // staggered weight: 2/3, or 1 in the outer half of a boundary cell
   float xrat = 2.f / 3.f;
-  if (ix == 0 && X < 0.5f * wx) xrat = 1.f;
-  if (ix == g.ncx - 1 && X > 0.5f * wx) xrat = 1.f;
-  if (iy == 0 && Y < 0.5f * wy) xrat = 1.f;
-  if (iy == g.ncy - 1 && Y > 0.5f * wy) xrat = 1.f;
-  return xrat;
+  if ((ix == 0 && !qx) || (ix == g.ncx - 1 && qx) || (iy == 0 && !qy) ||
+      (iy == g.ncy - 1 && qy))
+    xrat = 1.f;
+  float4 *o = Q + t * 3;
+  o[0] = blend(cPX, cVX, xrat);
+  o[1] = blend(cPY, cVY, xrat);
+  o[2] = cE;
 }
 
-// allinteri (interpolation.c:1688-1758): velocity and spin at a point
-__device__ __forceinline__ void allinteri(const Grid &g, const Nodes &N, const float *vxp,
-                                          const float *vyp, Pos p, float &VX, float &VY,
-                                          float &ESP) {
-  // clamp into the model
+// allinteri at a cell-local position: velocity and spin from the quarter's
+// forms (positions outside the model are clamped onto its boundary first)
+__device__ __forceinline__ void vel_at(const Grid &g, const float4 *Q, Pos p, float &VX,
+                                       float &VY, float &ESP) {
   const float wx = __ldg(g.wx + p.ix), wy = __ldg(g.wy + p.iy);
   if (p.ix == 0 && p.X < 0.f) p.X = 0.f;
   if (p.ix == g.ncx - 1 && p.X > wx) p.X = wx;
   if (p.iy == 0 && p.Y < 0.f) p.Y = 0.f;
   if (p.iy == g.ncy - 1 && p.Y > wy) p.Y = wy;
-  const float xrat = allinteri_xrat(g, p.ix, p.iy, p.X, p.Y, wx, wy);
-  const Axis ax = make_axis(g.wx, g.ncx, p.ix, p.X);
-  const Axis ay = make_axis(g.wy, g.ncy, p.iy, p.Y);
-  const long yn = g.yn;
-  float eb, nb, ec, nc, e, n;
-  const long mb = stencil_basic(g, ax, ay, eb, nb);
-  const long mc = stencil_centre(g, ax, ay, p.X > 0.5f * wx, p.Y > 0.5f * wy, ec, nc);
-  long m3 = stencil_vx(g, ax, ay, p.Y < 0.5f * wy, g.xn - 2, e, n);
-  const float VXs = bil(N.f(V2C_NF_VX), m3, yn, e, n);
-  m3 = stencil_vy(g, ax, ay, p.X < 0.5f * wx, g.yn - 2, e, n);
-  const float VYs = bil(N.f(V2C_NF_VY), m3, yn, e, n);
-  allinteri_from(N, vxp, vyp, yn, mb, eb, nb, mc, ec, nc, VXs, VYs, xrat, VX, VY, ESP);
+  const float hx = 0.5f * wx, hy = 0.5f * wy;
+  const int qx = p.X >= hx, qy = p.Y >= hy;
+  const float dX = qx ? p.X - hx : p.X, dY = qy ? p.Y - hy : p.Y;
+  const float4 *c = Q + (((long)p.ix * g.ncy + p.iy) * 4 + qy * 2 + qx) * 3;
+  const float4 a = __ldg(c), b = __ldg(c + 1), e = __ldg(c + 2);
+  VX = fmaf(dY, fmaf(a.w, dX, a.z), fmaf(a.y, dX, a.x));
+  VY = fmaf(dY, fmaf(b.w, dX, b.z), fmaf(b.y, dX, b.x));
+  ESP = fmaf(dY, fmaf(e.w, dX, e.z), fmaf(e.y, dX, e.x));
 }
 
 // basic-node back-scatter into a named register array
@@ -144,17 +222,7 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
       const int jlo = max(j0 - 1, 0), jhi = min(j0 + TY - 1, ncy - 1);
       const long cb = (long)ci * ncy;
       const int seg_b = __ldg(a.start + cb + jlo), seg_e = __ldg(a.start + cb + jhi + 1);
-      int lo_b = 0, lo_e = 0, up_b = 0, up_e = 0;
-      float s1lo = 0.f, s1up = 0.f;
-      const float iwx = 1.f / __ldg(g.wx + ci);
-      if (jvalid && j - 1 >= 0 && j - 1 <= ncy - 1) {
-        lo_b = __ldg(a.start + cb + j - 1); lo_e = __ldg(a.start + cb + j);
-        s1lo = iwx / __ldg(g.wy + j - 1);
-      }
-      if (jvalid && j <= ncy - 1) {
-        up_b = __ldg(a.start + cb + j); up_e = __ldg(a.start + cb + j + 1);
-        s1up = iwx / __ldg(g.wy + j);
-      }
+
       const bool owned_col = ci >= i0;
       for (int cs = seg_b; cs < seg_e; cs += CHUNK) {
         const int ce = min(cs + CHUNK, seg_e);
@@ -233,7 +301,7 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
                 msxx = SXXE; msxy = SXYE; mp = SPPE; mexx = EXXE; mexy = EXYE;
                 mvx = MVX; mvy = MVY; phi = PHISE; me = ESE;
               }
-              if (!P.tempmod) tk = (float)P.eps2;
+              if (!P.tempmod) tk = a.S.eps2_f;
               changed = true;
             }
             if (in_grid && t < 50 && tk > 0.f) {
@@ -259,60 +327,108 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
         if (!backscatter) continue;
         __syncthreads();
         if (!jvalid) continue;
+        // quarter class starts of cell (ci, j-1) (lower) and (ci, j) (upper),
+        // read here rather than held through the staging
+        int4 ql = make_int4(0, 0, 0, 0), qu = make_int4(0, 0, 0, 0);
+        int lo_e = 0, up_e = 0;
+        float s1lo = 0.f, s1up = 0.f;
+        const float iwx = 1.f / __ldg(g.wx + ci);
+        if (j - 1 >= 0 && j - 1 <= ncy - 1) {
+          ql = __ldg(a.qstart + cb + j - 1); lo_e = __ldg(a.start + cb + j);
+          s1lo = iwx / __ldg(g.wy + j - 1);
+        }
+        if (j <= ncy - 1) {
+          qu = __ldg(a.qstart + cb + j); up_e = __ldg(a.start + cb + j + 1);
+          s1up = iwx / __ldg(g.wy + j);
+        }
         // ---------------------------------------------- back-scatter
-        for (int s = max(lo_b, cs); s < min(lo_e, ce); ++s) {  // cell (ci, j-1)
-          const int q = s - cs;
-          const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
-          if (role == 0) {
-            if (!(v > 0.5f)) continue;
+        // over the quarter class runs of cell (ci, j-1) and (ci, j); the
+        // conditions inside hold for the whole run except at exact halves
+#define CLASS_RUN(b, e) \
+  for (int s = max((b), cs), s_e = min((e), ce), q = s - cs; s < s_e; ++s, q = s - cs)
+        if (role == 0) {
+          CLASS_RUN(ql.z, ql.w) {  // cell (ci, j-1), v > 1/2, u <= 1/2
+            const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
             if (u < 0.5f) {
               const float w = s1lo * (1.f - 2.f * u) * (2.f * v - 1.f);
               ADD_BS(cur, q, w);
-            } else if (u > 0.5f) {
-              const float w = s1lo * (2.f * u - 1.f) * (2.f * v - 1.f);
-              ADD_BS(car, q, w);
-            }
-          } else if (role == 3) {
-            if (v > 0.5f) {
-              const float w = s1lo * (1.f - fabsf(u - 0.5f)) * v;
-              const float mro = sm.q[Q_MRO][q];
-              cur[0].add(sm.q[Q_VY][q] * mro * w); cur[1].add(mro * w); cur[2].add(w);
             }
           }
-        }
-        for (int s = max(up_b, cs); s < min(up_e, ce); ++s) {  // cell (ci, j)
-          const int q = s - cs;
-          const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
-          if (role == 0) {
-            if (!(v < 0.5f)) continue;
-            if (u < 0.5f) {
+          CLASS_RUN(ql.w, lo_e) {  // cell (ci, j-1), v > 1/2, u > 1/2
+            const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
+            const float w = s1lo * (2.f * u - 1.f) * (2.f * v - 1.f);
+            ADD_BS(car, q, w);
+          }
+          CLASS_RUN(qu.x, qu.y) {  // cell (ci, j), v <= 1/2, u <= 1/2
+            const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
+            if (u < 0.5f && v < 0.5f) {
               const float w = s1up * (1.f - 2.f * u) * (1.f - 2.f * v);
               ADD_BS(cur, q, w);
-            } else if (u > 0.5f) {
+            }
+          }
+          CLASS_RUN(qu.y, qu.z) {  // cell (ci, j), v <= 1/2, u > 1/2
+            const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
+            if (v < 0.5f) {
               const float w = s1up * (2.f * u - 1.f) * (1.f - 2.f * v);
               ADD_BS(car, q, w);
             }
-          } else if (role == 1) {
+          }
+        } else if (role == 1) {
+          CLASS_RUN(qu.x, up_e) {  // the whole cell (ci, j) to its centre node
+            const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
             const float w = s1up * (1.f - 2.f * fabsf(u - 0.5f)) * (1.f - 2.f * fabsf(v - 0.5f));
             cur[0].add(sm.q[Q_PR][q] * w); cur[1].add(sm.q[Q_SXX][q] * w);
             cur[2].add(sm.q[Q_EXX][q] * w); cur[3].add(w);
-          } else if (role == 2) {
-            const float mro = sm.q[Q_MRO][q];
+          }
+        } else if (role == 2) {
+          // vx node (ci, j) from u < 1/2 (classes 0, 2), (ci+1, j) from u > 1/2
+          CLASS_RUN(qu.x, qu.y) {
+            const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
             if (u < 0.5f) {
+              const float mro = sm.q[Q_MRO][q];
               const float w = s1up * (1.f - u) * (1.f - fabsf(v - 0.5f));
               cur[0].add(sm.q[Q_VX][q] * mro * w); cur[1].add(mro * w); cur[2].add(w);
-            } else if (u > 0.5f) {
-              const float w = s1up * u * (1.f - fabsf(v - 0.5f));
-              car[0].add(sm.q[Q_VX][q] * mro * w); car[1].add(mro * w); car[2].add(w);
             }
-          } else {
-            if (v < 0.5f) {
-              const float w = s1up * (1.f - fabsf(u - 0.5f)) * (1.f - v);
+          }
+          CLASS_RUN(qu.y, qu.z) {
+            const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
+            const float mro = sm.q[Q_MRO][q];
+            const float w = s1up * u * (1.f - fabsf(v - 0.5f));
+            car[0].add(sm.q[Q_VX][q] * mro * w); car[1].add(mro * w); car[2].add(w);
+          }
+          CLASS_RUN(qu.z, qu.w) {
+            const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
+            if (u < 0.5f) {
               const float mro = sm.q[Q_MRO][q];
+              const float w = s1up * (1.f - u) * (1.f - fabsf(v - 0.5f));
+              cur[0].add(sm.q[Q_VX][q] * mro * w); cur[1].add(mro * w); cur[2].add(w);
+            }
+          }
+          CLASS_RUN(qu.w, up_e) {
+            const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
+            const float mro = sm.q[Q_MRO][q];
+            const float w = s1up * u * (1.f - fabsf(v - 0.5f));
+            car[0].add(sm.q[Q_VX][q] * mro * w); car[1].add(mro * w); car[2].add(w);
+          }
+        } else {
+          // vy node (ci, j) from v > 1/2 of cell (ci, j-1) (classes 2, 3) and
+          // v < 1/2 of cell (ci, j) (classes 0, 1)
+          CLASS_RUN(ql.z, lo_e) {
+            const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
+            const float mro = sm.q[Q_MRO][q];
+            const float w = s1lo * (1.f - fabsf(u - 0.5f)) * v;
+            cur[0].add(sm.q[Q_VY][q] * mro * w); cur[1].add(mro * w); cur[2].add(w);
+          }
+          CLASS_RUN(qu.x, qu.z) {
+            const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
+            if (v < 0.5f) {
+              const float mro = sm.q[Q_MRO][q];
+              const float w = s1up * (1.f - fabsf(u - 0.5f)) * (1.f - v);
               cur[0].add(sm.q[Q_VY][q] * mro * w); cur[1].add(mro * w); cur[2].add(w);
             }
           }
         }
+#undef CLASS_RUN
       }
     }
 
@@ -357,31 +473,12 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
 }
 
 // ----------------------------------------------------------- the move
-// Velocities averaged to the pressure node m (allinteri's pairs,
-// interpolation.c:1730-1745): VXP[m] = (vx[m-1] + vx[m-yn-1])/2,
-// VYP[m] = (vy[m-yn] + vy[m-yn-1])/2; nodes of the first row or column have
-// no pressure node and get 0 (the pressure stencil never reaches them).
-__global__ void k_vel_pnodes(Grid g, const float *vx, const float *vy, float *vxp, float *vyp) {
-  const long m = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (m >= g.nn) return;
-  const long yn = g.yn;
-  const long ix = m / yn, iy = m - ix * yn;
-  if (ix < 1 || iy < 1) {
-    vxp[m] = 0.f;
-    vyp[m] = 0.f;
-    return;
-  }
-  vxp[m] = 0.5f * (__ldg(vx + m - 1) + __ldg(vx + m - yn - 1));
-  vyp[m] = 0.5f * (__ldg(vy + m - yn) + __ldg(vy + m - yn - 1));
-}
-
 // moveandrotatemarkers (moveandrotatemarkers.c:1-178), one thread per
 // marker in cell order: Euler or RK4 through allinteri, stress rotation,
 // markers from depth, out-of-grid reset.  New positions go to the second
 // position buffer.
 __global__ void __launch_bounds__(256) k_move(N2MArgs a) {
   const Grid &g = a.g;
-  const Nodes &N = a.N;
   const v2c_params &P = a.S.p;
   const int ncy = g.ncy;
   const float dt = a.S.dt;
@@ -400,7 +497,7 @@ __global__ void __launch_bounds__(256) k_move(N2MArgs a) {
       const float wxc = __ldg(g.wx + ix), wyc = __ldg(g.wy + iy);
       const Pos p0{ix, iy, u * wxc, v * wyc};
       float vx0, vy0, sp0, vx1, vy1, sp1;
-      allinteri(g, N, a.vxp, a.vyp, p0, vx1, vy1, sp1);
+      vel_at(g, a.quad, p0, vx1, vy1, sp1);
       if (P.markmod == 1) {
         vx0 = vx1; vy0 = vy1; sp0 = sp1;
       } else {
@@ -408,15 +505,15 @@ __global__ void __launch_bounds__(256) k_move(N2MArgs a) {
         Pos p = p0;
         p.X += vx1 * dt / 2.f; p.Y += vy1 * dt / 2.f;
         settle(g, p, a.stat);
-        allinteri(g, N, a.vxp, a.vyp, p, vx2, vy2, sp2);
+        vel_at(g, a.quad, p, vx2, vy2, sp2);
         p = p0;
         p.X += vx2 * dt / 2.f; p.Y += vy2 * dt / 2.f;
         settle(g, p, a.stat);
-        allinteri(g, N, a.vxp, a.vyp, p, vx3, vy3, sp3);
+        vel_at(g, a.quad, p, vx3, vy3, sp3);
         p = p0;
         p.X += vx3 * dt; p.Y += vy3 * dt;
         settle(g, p, a.stat);
-        allinteri(g, N, a.vxp, a.vyp, p, vx4, vy4, sp4);
+        vel_at(g, a.quad, p, vx4, vy4, sp4);
         vx0 = (vx1 + 2.f * vx2 + 2.f * vx3 + vx4) / 6.f;
         vy0 = (vy1 + 2.f * vy2 + 2.f * vy3 + vy4) / 6.f;
         sp0 = (P.markmod == 2) ? (sp1 + 2.f * sp2 + 2.f * sp3 + sp4) / 6.f : sp1;
@@ -473,11 +570,10 @@ __global__ void __launch_bounds__(256) k_move(N2MArgs a) {
       // position only when the FP32 one is within 1 m of zdeep
       float tk = a.m.tk[idx];
       const float tk0 = tk;
-      if (vy0 < 0.f && tk < (float)P.tdeep &&
-          __ldg(a.gyf + niy) + nv_ * __ldg(g.wy + niy) >
-              (float)P.zdeep - 1.f - 1e-6f * fabsf((float)P.zdeep)) {
+      if (vy0 < 0.f && tk < a.S.tdeep_f &&
+          __ldg(a.gyf + niy) + nv_ * __ldg(g.wy + niy) > a.S.zdeep_lo_f) {
         const double ynew = g.gy[niy] + (double)nv_ * (g.gy[niy + 1] - g.gy[niy]);
-        if (ynew > P.zdeep) tk = (float)P.tdeep;
+        if (ynew > P.zdeep) tk = a.S.tdeep_f;
       }
       const bool out = (nix == 0 && nu_ < 0.f) || (nix == g.ncx - 1 && nu_ > 1.f) ||
                        (niy == 0 && nv_ < 0.f) || (niy == g.ncy - 1 && nv_ > 1.f);
@@ -503,8 +599,8 @@ void launch_n2m(const N2MArgs &a, cudaStream_t st) {
 }
 
 void launch_move(const N2MArgs &a, cudaStream_t st) {
-  k_vel_pnodes<<<(unsigned)((a.g.nn + 255) / 256), 256, 0, st>>>(
-      a.g, a.N.f(V2C_NF_VX), a.N.f(V2C_NF_VY), a.vxp, a.vyp);
+  const long quarters = (long)a.g.ncx * a.g.ncy * 4;
+  k_vel_quads<<<(unsigned)((quarters + 255) / 256), 256, 0, st>>>(a.g, a.N, a.quad);
   if (a.n <= 0) return;
   long blocks = (a.n + 255) / 256;
   if (blocks > 152 * 8 * 4) blocks = 152 * 8 * 4;

@@ -235,6 +235,30 @@ __global__ void k_to_f64(const float *src, double *dst, long n) {
   if (i < n) dst[i] = (double)src[i];
 }
 
+// several node fields at once: blockIdx.y picks the field, stage holds
+// them one after another (field list order)
+struct FieldList {
+  int f[V2C_NF_N];
+};
+__global__ void k_fields_to_f64(const float *base, long nn, FieldList L, double *stage) {
+  const float *src = base + (long)L.f[blockIdx.y] * nn;
+  double *dst = stage + (long)blockIdx.y * nn;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nn; i += (long)gridDim.x * blockDim.x)
+    dst[i] = (double)src[i];
+}
+__global__ void k_fields_to_f32(const double *stage, long nn, FieldList L, float *base) {
+  const double *src = stage + (long)blockIdx.y * nn;
+  float *dst = base + (long)L.f[blockIdx.y] * nn;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nn; i += (long)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
+}
+
+FieldList field_list(const int *fields, int count) {
+  FieldList L;
+  for (int k = 0; k < V2C_NF_N; k++) L.f[k] = k < count ? fields[k] : 0;
+  return L;
+}
+
 }  // namespace
 
 void launch_c2b_old(const Grid &g, const Nodes &N, cudaStream_t st) {
@@ -267,6 +291,20 @@ void launch_node_to_f32(const double *src, float *dst, long n, cudaStream_t st) 
 }
 void launch_node_to_f64(const float *src, double *dst, long n, cudaStream_t st) {
   if (n > 0) k_to_f64<<<nblk(n, 256), 256, 0, st>>>(src, dst, n);
+}
+void launch_fields_to_f64(const float *base, long nn, const int *fields, int count, double *stage,
+                          cudaStream_t st) {
+  if (nn <= 0 || count <= 0) return;
+  const unsigned bx = nblk(nn, 256) < 152 * 8 ? nblk(nn, 256) : 152 * 8;
+  k_fields_to_f64<<<dim3(bx, (unsigned)count), 256, 0, st>>>(base, nn, field_list(fields, count),
+                                                             stage);
+}
+void launch_fields_to_f32(const double *stage, long nn, const int *fields, int count, float *base,
+                          cudaStream_t st) {
+  if (nn <= 0 || count <= 0) return;
+  const unsigned bx = nblk(nn, 256) < 152 * 8 ? nblk(nn, 256) : 152 * 8;
+  k_fields_to_f32<<<dim3(bx, (unsigned)count), 256, 0, st>>>(stage, nn, field_list(fields, count),
+                                                             base);
 }
 
 }  // namespace v2c

@@ -52,11 +52,11 @@ __device__ __forceinline__ float marker_friction(const PhysArgs &a, int ix, int 
                                                  Fric &fr) {
   const Grid &g = a.g;
   const v2c_params &P = a.S.p;
+  const Scal &S = a.S;
   const float xf = __ldg(a.gxf + ix) + Xc, yf = __ldg(a.gyf + iy) + Yc;
-  const float rad = fabsf(yf - ((float)P.fault_y + (float)P.fault_slope * xf));
-  if (t > 0 && rad > (float)P.fault_hw + 1.0f) {
-    fr.a = (float)P.a_hr; fr.b = (float)P.b_hr; fr.L = (float)P.L_hr;
-    fr.V0 = (float)P.V0_hr; fr.mu0 = 0.6f;
+  const float rad = fabsf(yf - (S.fault_y_f + S.fault_slope_f * xf));
+  if (t > 0 && rad > S.fault_hw1_f) {
+    fr.a = S.a_hr_f; fr.b = S.b_hr_f; fr.L = S.L_hr_f; fr.V0 = S.V0_hr_f; fr.mu0 = 0.6f;
     return 50.f;
   }
   const double x = g.gx[ix] + (double)u * (g.gx[ix + 1] - g.gx[ix]);
@@ -102,8 +102,7 @@ __global__ void __launch_bounds__(PT, 5) k_phys(PhysArgs a) {
   const long nwarps = (long)gridDim.x * (PT / 32);
   const long n = a.n;
   const v2c_params &P = a.S.p;
-  const ff dt_ff = ff_from_double(P.timestep), W_ff = ff_from_double(P.faultwidth),
-           sn_ff = ff_from_double(P.nstress);
+  const ff dt_ff{a.S.dt_hi, a.S.dt_lo}, W_ff{a.S.W_hi, a.S.W_lo}, sn_ff{a.S.sn_hi, a.S.sn_lo};
   unsigned long long it = 0;
   for (long base = ((long)blockIdx.x * (PT / 32) + wl) * 32; base < n; base += nwarps * 32) {
     const long i = base + lane;
@@ -225,8 +224,7 @@ __global__ void __launch_bounds__(PT, 4) k_guess(PhysArgs a, float *guess) {
   const long nwarps = (long)gridDim.x * (PT / 32);
   const long cnt = *a.list_n;
   const v2c_params &P = a.S.p;
-  const ff dt_ff = ff_from_double(P.timestep), W_ff = ff_from_double(P.faultwidth),
-           sn_ff = ff_from_double(P.nstress);
+  const ff dt_ff{a.S.dt_hi, a.S.dt_lo}, W_ff{a.S.W_hi, a.S.W_lo}, sn_ff{a.S.sn_hi, a.S.sn_lo};
   for (long base = ((long)blockIdx.x * (PT / 32) + wl) * 32; base < cnt; base += nwarps * 32) {
     const long e = base + lane;
     const bool valid = e < cnt;
@@ -256,8 +254,7 @@ __global__ void __launch_bounds__(PT, 5) k_newton(PhysArgs a, const float *guess
   const long nwarps = (long)gridDim.x * (PT / 32);
   const long cnt = *a.list_n;
   const v2c_params &P = a.S.p;
-  const ff dt_ff = ff_from_double(P.timestep), W_ff = ff_from_double(P.faultwidth),
-           sn_ff = ff_from_double(P.nstress);
+  const ff dt_ff{a.S.dt_hi, a.S.dt_lo}, W_ff{a.S.W_hi, a.S.W_lo}, sn_ff{a.S.sn_hi, a.S.sn_lo};
   unsigned long long it = 0, fb = 0, nc = 0, resbits = 0;
   for (long base = ((long)blockIdx.x * (PT / 32) + wl) * 32; base < cnt; base += nwarps * 32) {
     const long e = base + lane;

@@ -85,8 +85,8 @@ __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, in
   }
   // limits nubeg/nuend then the per-type limits, in that order
   float nu;
-  if (lnv < S.ln_nubeg) nu = (float)S.p.nubeg;
-  else if (lnv > S.ln_nuend) nu = (float)S.p.nuend;
+  if (lnv < S.ln_nubeg) nu = S.nubeg_f;
+  else if (lnv > S.ln_nuend) nu = S.nuend_f;
   else nu = expf(lnv);
   if (nu < R(RK_N0, t)) nu = R(RK_N0, t);
   if (nu > R(RK_N1, t)) nu = R(RK_N1, t);

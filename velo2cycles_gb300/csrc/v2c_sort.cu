@@ -2,11 +2,13 @@
 //
 // Cell assignment (upload) bisects the FP64 grid lines exactly like
 // nxsearch/nysearch (interpolation.c:1536-1573), so the integer cell of
-// every marker is bit-identical to the reference's.  The counting sort is
-// stable by array index: counts by integer atomics (order-independent),
-// exclusive scan, scatter into per-cell slots, then each cell's slots are
-// ranked by array index, which fixes the order whatever order the atomics
-// handed the slots out in.
+// every marker is bit-identical to the reference's.  The counting sort
+// orders by cell, within a cell by quarter class q = 2 (v > 1/2) + (u > 1/2)
+// and within a class by array index: counts by integer atomics
+// (order-independent), exclusive scan, scatter of (q, index) keys into
+// per-cell slots, then each cell's keys are ranked, which fixes the order
+// whatever order the atomics handed the slots out in.  The sweeps that
+// scatter to nodes read each quarter class as one contiguous run.
 #include <climits>
 
 #include "v2c_kernels.h"
@@ -105,40 +107,52 @@ __global__ void k_scan_add(int32_t *out, long m, const int32_t *bsum) {
   if (i < m) out[i] += bsum[i / (SB * SE)];
 }
 
-__global__ void k_slots(const int32_t *cell, long n, const int32_t *start, const int32_t *slot,
-                        int32_t *tmp) {
+// key of marker i: quarter class in bits 30-31, array index below
+__global__ void k_slots(const int32_t *cell, const float *u, const float *v, long n,
+                        const int32_t *start, const int32_t *slot, uint32_t *tmp) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i < n) tmp[start[cell[i]] + slot[i]] = (int32_t)i;
+  if (i < n) {
+    const uint32_t q = (v[i] > 0.5f ? 2u : 0u) + (u[i] > 0.5f ? 1u : 0u);
+    tmp[start[cell[i]] + slot[i]] = (q << 30) | (uint32_t)i;
+  }
 }
 
-// One warp ranks the L distinct entries of a cell's slots (any order) and
-// writes them in ascending order.
-__device__ __forceinline__ void rank_segment(const int32_t *tmp, int32_t *perm, int L, int lane) {
-  if (L <= 32) {
-    const int val = (lane < L) ? tmp[lane] : INT_MAX;
-    int rank = 0;
-#pragma unroll
-    for (int k = 0; k < 32; k++) rank += (__shfl_sync(V2C_FULL, val, k) < val);
-    if (lane < L) perm[rank] = val;
-    return;
-  }
+constexpr uint32_t KEY_INDEX = (1u << 30) - 1;
+
+// One warp ranks the L distinct keys of a cell's slots (any order), writes
+// their indices in ascending key order and returns the count of quarter
+// classes 0, 1, 2 (same value in every lane).
+__device__ __forceinline__ int4 rank_segment(const uint32_t *tmp, int32_t *perm, int L, int lane) {
+  int4 cnt = make_int4(0, 0, 0, 0);
   for (int b = 0; b < L; b += 32) {
     const int jj = b + lane;
-    const int val = (jj < L) ? tmp[jj] : INT_MAX;
+    const uint32_t val = (jj < L) ? tmp[jj] : 0xffffffffu;
     int rank = 0;
-    for (int b2 = 0; b2 < L; b2 += 32) {
-      const int other = (b2 + lane < L) ? tmp[b2 + lane] : INT_MAX;
+    if (L <= 32) {
+#pragma unroll
+      for (int k = 0; k < 32; k++) rank += (__shfl_sync(V2C_FULL, val, k) < val);
+    } else {
+      for (int b2 = 0; b2 < L; b2 += 32) {
+        const uint32_t other = (b2 + lane < L) ? tmp[b2 + lane] : 0xffffffffu;
 #pragma unroll 8
-      for (int k = 0; k < 32; k++) rank += (__shfl_sync(V2C_FULL, other, k) < val);
+        for (int k = 0; k < 32; k++) rank += (__shfl_sync(V2C_FULL, other, k) < val);
+      }
     }
-    if (jj < L) perm[rank] = val;
+    const bool in = jj < L;
+    const uint32_t q = val >> 30;
+    cnt.x += __popc(__ballot_sync(V2C_FULL, in && q == 0));
+    cnt.y += __popc(__ballot_sync(V2C_FULL, in && q == 1));
+    cnt.z += __popc(__ballot_sync(V2C_FULL, in && q == 2));
+    if (in) perm[rank] = (int32_t)(val & KEY_INDEX);
   }
+  return cnt;
 }
 
-// one warp per cell: rank each entry among the cell's entries (all distinct);
-// the largest cell count goes to the status counter once per block
-__global__ void k_rank(const int32_t *start, long ncell, const int32_t *tmp, int32_t *perm,
-                       unsigned long long *stat) {
+// one warp per cell: rank each key among the cell's keys (all distinct) and
+// write the quarter class starts; the largest cell count goes to the status
+// counter once per block
+__global__ void k_rank(const int32_t *start, long ncell, const uint32_t *tmp, int32_t *perm,
+                       int4 *qstart, unsigned long long *stat) {
   __shared__ int bmax;
   if (threadIdx.x == 0) bmax = 0;
   __syncthreads();
@@ -147,10 +161,21 @@ __global__ void k_rank(const int32_t *start, long ncell, const int32_t *tmp, int
   if (c < ncell) {
     const int s = start[c], L = start[c + 1] - s;
     if (lane == 0 && L > 0) atomicMax(&bmax, L);
+    int4 cnt = make_int4(0, 0, 0, 0);
     if (L == 1) {
-      if (lane == 0) perm[s] = tmp[s];
+      const uint32_t key = tmp[s];
+      if (lane == 0) perm[s] = (int32_t)(key & KEY_INDEX);
+      const int q = (int)(key >> 30);
+      cnt = make_int4(q == 0, q == 1, q == 2, 0);
     } else if (L > 1) {
-      rank_segment(tmp + s, perm + s, L, lane);
+      cnt = rank_segment(tmp + s, perm + s, L, lane);
+    }
+    if (lane == 0) {
+      qstart[c] = make_int4(s, s + cnt.x, s + cnt.x + cnt.y, s + cnt.x + cnt.y + cnt.z);
+      if (c == ncell - 1) {
+        const int e = start[ncell];
+        qstart[ncell] = make_int4(e, e, e, e);
+      }
     }
   }
   __syncthreads();
@@ -195,18 +220,17 @@ void launch_assign(const Grid &g, const double *x, const double *y, long n, Mark
   if (n > 0) k_assign<<<nblk(n, 256), 256, 0, st>>>(g, x, y, n, m);
 }
 
-void launch_sort(const int32_t *cell, long n, long ncell, SortBufs &b,
-                 unsigned long long *stat, cudaStream_t st) {
+void launch_sort(const int32_t *cell, const float *u, const float *v, long n, long ncell,
+                 SortBufs &b, unsigned long long *stat, cudaStream_t st) {
   cudaMemsetAsync(b.counts, 0, sizeof(int32_t) * ncell, st);
   if (n > 0) k_count<<<nblk(n, 256), 256, 0, st>>>(cell, n, b.counts, b.slot);
   long nb = (ncell + SB * SE - 1) / (SB * SE);
   k_scan_block<<<(unsigned)nb, SB, 0, st>>>(b.counts, ncell, b.start, b.blocksum);
   k_scan_sums<<<1, SB, 0, st>>>(b.blocksum, nb, b.start + ncell);
   k_scan_add<<<nblk(ncell, 256), 256, 0, st>>>(b.start, ncell, b.blocksum);
-  if (n > 0) {
-    k_slots<<<nblk(n, 256), 256, 0, st>>>(cell, n, b.start, b.slot, b.tmp);
-    k_rank<<<nblk(ncell * 32, 256), 256, 0, st>>>(b.start, ncell, b.tmp, b.perm, stat);
-  }
+  uint32_t *keys = reinterpret_cast<uint32_t *>(b.tmp);
+  if (n > 0) k_slots<<<nblk(n, 256), 256, 0, st>>>(cell, u, v, n, b.start, b.slot, keys);
+  k_rank<<<nblk(ncell * 32, 256), 256, 0, st>>>(b.start, ncell, keys, b.perm, b.qstart, stat);
 }
 
 void launch_f64_to_f32(const double *src, float *dst, long n, cudaStream_t st) {

@@ -129,12 +129,26 @@ class MarkerInCell:
         return a
 
     def upload_nodes(self, nodes: dict):
-        for f, v in nodes.items():
-            self.upload_node(f, v)
+        """Several node fields in one call (one conversion kernel, one copy
+        each); the arrays must stay unchanged until the stream synchronises."""
+        arrs = {int(f): np.ascontiguousarray(v, dtype=np.float64) for f, v in nodes.items()}
+        for a in arrs.values():
+            assert a.size == self.nn
+        self._keep_up = arrs  # the copies from pinned memory run later
+        fl = (ctypes.c_int * len(arrs))(*arrs.keys())
+        pp = (ctypes.POINTER(ctypes.c_double) * len(arrs))(*[_ptr(a) for a in arrs.values()])
+        call("v2c_upload_node_fields", self.h, len(arrs), fl, pp)
 
-    def download_nodes(self, fields=None) -> dict:
-        fields = range(abi.NF_N) if fields is None else fields
-        return {f: self.download_node(f) for f in fields}
+    def download_nodes(self, fields=None, into: dict | None = None) -> dict:
+        fields = list(range(abi.NF_N) if fields is None else fields)
+        out = into if into is not None else {}
+        for f in fields:
+            if f not in out:
+                out[f] = np.zeros(self.nn)
+        fl = (ctypes.c_int * len(fields))(*fields)
+        pp = (ctypes.POINTER(ctypes.c_double) * len(fields))(*[_ptr(out[f]) for f in fields])
+        call("v2c_download_node_fields", self.h, len(fields), fl, pp)
+        return {f: out[f] for f in fields}
 
     # ----------------------------------------------------- the MIC calls
     def marker2nodes(self):
