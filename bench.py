@@ -173,7 +173,8 @@ def ncu_traffic(kernel: str):
 
 def cpu_baseline(steps: int = 3, warmup: int = 1, threads: int | None = None) -> dict:
     """Reference routines (oracle/_ref, compiled from the reference sources)
-    on a window of the same workload, all host cores."""
+    on a window of the same workload, all host cores, plus the same routines
+    on one thread (one warm-up and one timed step)."""
     import oracle
     from oracle import bindings as B
     from velo2cycles_gb300 import synth
@@ -181,10 +182,13 @@ def cpu_baseline(steps: int = 3, warmup: int = 1, threads: int | None = None) ->
     oracle.build()
     threads = threads or os.cpu_count() or 1
     case = synth.make_case("c4", seed=1, window=(1200, 0, 401, 101))
+    one = None
     if B.reference_available():
         res = B.run_reference(case, nthreads=threads, nsteps=steps, warmup=warmup)
         secs = float(res["seconds"][:6].sum()) / steps
         kind = "reference"
+        r1 = B.run_reference(case, nthreads=1, nsteps=1, warmup=1)
+        one = case.n / float(r1["seconds"][:6].sum())
     else:
         r = oracle.Restatement(case.copy())
         for _ in range(warmup):
@@ -195,6 +199,7 @@ def cpu_baseline(steps: int = 3, warmup: int = 1, threads: int | None = None) ->
         secs = (time.perf_counter() - t) / steps
         threads, kind = 1, "port"
     return {"value": case.n / secs, "unit": UNIT, "cores": threads, "kind": kind,
+            "value_1thread": one,
             "sample": f"c4 window of 401x101 grid lines at the c4 spacing, {case.n} markers, "
                       f"{warmup} warm-up + {steps} timed steps, full MIC step",
             "seconds_per_step": secs}

@@ -167,6 +167,8 @@ enum {
   V2C_NF_VYSUM, V2C_NF_WTVXSUM, V2C_NF_WTVYSUM, V2C_NF_MRX0, V2C_NF_MRY0,
   /* read by the adaptive time step (calc_RSF.c:455) */
   V2C_NF_PRS,
+  /* interpolate_center2basic outputs (with SXXS, EXXPL, PRS above) */
+  V2C_NF_EXXS, V2C_NF_EXXEL,
   V2C_NF_N
 };
 
@@ -249,6 +251,22 @@ int v2c_download_node_fields(v2c_ctx *ctx, int count, const int *fields, double 
  * stream except where a status must be read back (noted). */
 int v2c_marker2nodes(v2c_ctx *ctx);                 /* [interpolation.c:55]   */
 int v2c_center2basic_old(v2c_ctx *ctx);             /* [interpolation.c:1575] */
+/* interpolate_basic2center [interpolation.c:1639]: nd at the pressure nodes
+ * (harmonic mean of nu); the Picard loop calls it after compute_before_solve
+ * (momentum_continuity_iterate.c:71) */
+int v2c_interpolate_basic2center(v2c_ctx *ctx);
+/* interpolate_center2basic [interpolation.c:1600]: exxs, exxpl, sxxs, prs and
+ * exxel on the basic nodes from the solver's pressure-node fields; called
+ * before compute_after_solve (momentum_continuity_iterate.c:87) */
+int v2c_interpolate_center2basic(v2c_ctx *ctx, double dt);
+/* recompute_stress_strainrate [momentum_continuity_iterate.c:214]: exx, sxx
+ * (pressure nodes) and exy, esp, sxy (basic nodes) from the node velocities
+ * vx, vy with the visco-elastic update of sxxcalc / sxycalc; the reference
+ * runs it after reloading the Stokes solution (:84) */
+int v2c_recompute_stress_strainrate(v2c_ctx *ctx, double dt);
+/* copyarrays [momentum_continuity_iterate.c:265]: RK_sliprs_final, sliprs
+ * and RK_phidts_final from the solved rates, at the end of a step */
+int v2c_copyarrays(v2c_ctx *ctx);
 int v2c_compute_before_solve(v2c_ctx *ctx, double dt, int rk); /* [plastic.c:2] */
 /* returns the RMS of (syield - sigin) in *deltas, [plastic.c:61] (syncs) */
 int v2c_compute_after_solve(v2c_ctx *ctx, double dt, int rk, double *deltas);
@@ -285,6 +303,30 @@ typedef struct v2c_timestep_info {
 int v2c_calc_timestep(v2c_ctx *ctx, int oldornew, const v2c_timestep_ctl *ctl,
                       v2c_timestep_info *info);            /* [calc_RSF.c:352] */
 
+/* ========================================================= seismic cycle
+ * The seismic-cycle workload (no counterpart in the reference: it stands in
+ * for the host Stokes solve with prescribed velocities).  Regime 0
+ * (interseismic) and 1 (coseismic) each get a velocity field vx, vy
+ * (nodenum doubles each); setting regime 0 also zeroes the accumulated
+ * slip.  Synchronises. */
+int v2c_cycle_set_velocity(v2c_ctx *ctx, int regime, const double *vx, const double *vy);
+/* One step of timestep dt with regime r's velocities: marker2nodes,
+ * interpolate_center2basic_old, compute_before_solve, interpolate_basic2center,
+ * recompute_stress_strainrate, interpolate_center2basic, compute_after_solve
+ * (no readback), copyarrays, the accumulated slip of every basic node
+ * (+= dt * RK_sliprs_final), nodes2markers, moveandrotatemarkers and the next
+ * counting sort; then timesum += dt.  Asynchronous.
+ * use_graph: the step is captured once into a CUDA graph per key (regime,
+ * dt, the position buffer holding the current positions, every parameter
+ * but timesum, and timesum's classes: zero, positive, equal to dt, above
+ * 4e7 s, which are all the kernels see of it) and replayed afterwards; at
+ * most 8 graphs are kept (the oldest dropped).  The first step of a key
+ * runs the capture (no profiling events there); a capture needs no
+ * allocation, so it may run at any point after the context is set up. */
+int v2c_cycle_step(v2c_ctx *ctx, int regime, double dt, int use_graph);
+/* accumulated slip of every node (nodenum doubles).  Synchronises. */
+int v2c_cycle_slip(v2c_ctx *ctx, double *out);
+
 int v2c_synchronize(v2c_ctx *ctx);
 int v2c_get_status(v2c_ctx *ctx, v2c_status *st);
 
@@ -304,6 +346,7 @@ enum {
   V2C_PROF_PHYS,        /* marker physics without the Newton            */
   V2C_PROF_MOVE,        /* moveandrotatemarkers                        */
   V2C_PROF_TIMESTEP,    /* calc_timestep                                */
+  V2C_PROF_B2C,         /* basic2center, center2basic, recompute stress */
   V2C_PROF_N
 };
 int v2c_set_profiling(v2c_ctx *ctx, int on);

@@ -84,6 +84,14 @@ def _lib():
                    "v2c_oracle_nodes2markers", "v2c_oracle_move"):
             getattr(lib, fn).restype = ctypes.c_int
             getattr(lib, fn).argtypes = [P(_State)]
+        lib.v2c_oracle_basic2center.restype = ctypes.c_int
+        lib.v2c_oracle_basic2center.argtypes = [P(_State)]
+        lib.v2c_oracle_recompute_stress.restype = ctypes.c_int
+        lib.v2c_oracle_recompute_stress.argtypes = [P(_State), ctypes.c_double]
+        lib.v2c_oracle_copyarrays.restype = ctypes.c_int
+        lib.v2c_oracle_copyarrays.argtypes = [P(_State)]
+        lib.v2c_oracle_center2basic.restype = ctypes.c_int
+        lib.v2c_oracle_center2basic.argtypes = [P(_State), ctypes.c_double]
         lib.v2c_oracle_compute_before_solve.restype = ctypes.c_int
         lib.v2c_oracle_compute_before_solve.argtypes = [P(_State), ctypes.c_double, ctypes.c_int]
         lib.v2c_oracle_calc_timestep.restype = ctypes.c_int
@@ -156,6 +164,18 @@ class Restatement:
 
     def center2basic_old(self):
         return self.lib.v2c_oracle_center2basic_old(ctypes.byref(self.st))
+
+    def basic2center(self):
+        return self.lib.v2c_oracle_basic2center(ctypes.byref(self.st))
+
+    def center2basic(self, dt):
+        return self.lib.v2c_oracle_center2basic(ctypes.byref(self.st), dt)
+
+    def recompute_stress(self, dt):
+        return self.lib.v2c_oracle_recompute_stress(ctypes.byref(self.st), dt)
+
+    def copyarrays(self):
+        return self.lib.v2c_oracle_copyarrays(ctypes.byref(self.st))
 
     def compute_before_solve(self, dt, rk=0):
         return self.lib.v2c_oracle_compute_before_solve(ctypes.byref(self.st), dt, rk)
@@ -260,6 +280,11 @@ def mlp_forward(params: np.ndarray, X: np.ndarray) -> np.ndarray:
 STAGE_M2N, STAGE_C2B, STAGE_BEFORE, STAGE_AFTER, STAGE_N2M, STAGE_MOVE = range(6)
 ALL_STAGES = 0b111111
 TIMESTEP_STAGE = 1 << 6
+# interpolate_basic2center after compute_before_solve, interpolate_center2basic
+# before compute_after_solve (the Picard loop's order)
+B2C_STAGE, C2B_FULL_STAGE = 1 << 7, 1 << 8
+# recompute_stress_strainrate between them, copyarrays after compute_after_solve
+RECOMPUTE_STAGE, COPY_STAGE = 1 << 9, 1 << 10
 
 
 def write_case(path: str, case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0,

@@ -8,7 +8,9 @@
  * the sources are #included into one translation unit; this file only
  * loads the reference's global arrays from a case file, calls
  *   marker2nodes, interpolate_center2basic_old, compute_before_solve,
- *   compute_after_solve, nodes2markers, moveandrotatemarkers
+ *   interpolate_basic2center, recompute_stress_strainrate,
+ *   interpolate_center2basic, copyarrays (stage bits 7, 9, 8, 10),
+ *   compute_after_solve, nodes2markers, moveandrotatemarkers, calc_timestep
  * and writes the arrays back.  Stdout (the reference's progress prints) is
  * discarded.
  *
@@ -46,6 +48,7 @@
 #include "density_ductilevisc_calc.c"
 #include "moveandrotatemarkers.c"
 #include "momentum_continuity_addmatrix_checkerror.c"
+#include "momentum_continuity_iterate.c"
 #include "temperature_iterate.c"
 #include "plastic.c"
 #include "recalc_marker_properties.c"
@@ -102,7 +105,11 @@ int main(int argc, char **argv) {
     STAGE(0, 0, marker2nodes());
     STAGE(1, 1, interpolate_center2basic_old(timestep));
     STAGE(2, 2, compute_before_solve(timestep, 0));
+    STAGE(7, 7, interpolate_basic2center());
+    STAGE(9, 7, recompute_stress_strainrate(timestep, 0));
+    STAGE(8, 7, interpolate_center2basic(timestep));
     STAGE(3, 3, deltas = compute_after_solve(timestep, 0));
+    STAGE(10, 7, copyarrays(0));
     STAGE(4, 4, nodes2markers());
     STAGE(5, 5, moveandrotatemarkers());
     if (stages & (1 << 6)) {

@@ -725,6 +725,119 @@ int v2c_oracle_center2basic_old(v2c_oracle_state *s) {
   return 0;
 }
 
+/* interpolate_center2basic, interpolation.c:1600-1637: strain rate, stress,
+ * pressure, plastic and elastic strain rate averaged from the four pressure
+ * nodes around each interior basic node */
+int v2c_oracle_center2basic(v2c_oracle_state *s, double dt) {
+  long xn = s->p.xnumx, yn = s->p.ynumy, nn = nnodes(s);
+  const double *exx = s->N[V2C_NF_EXX], *sxx = s->N[V2C_NF_SXX], *sxxe = s->N[V2C_NF_SXXE];
+  const double *gd = s->N[V2C_NF_GD], *nd = s->N[V2C_NF_ND_M2C], *pr = s->N[V2C_NF_PR];
+  for (long m3 = 0; m3 < nn; m3++) {
+    long m2 = m3 % yn, m1 = (m3 - m2) / yn;
+    if (!(m1 >= 1 && m2 >= 1 && m1 < xn - 1 && m2 < yn - 1)) continue;
+    const long k[4] = {m3, m3 + 1, m3 + yn, m3 + yn + 1};
+    double epl[4], eel[4];
+    for (int q = 0; q < 4; q++) {
+      const long i = k[q];
+      epl[q] = exx[i] - (sxx[i] - sxxe[i]) / (2 * gd[i] * dt) - sxx[i] / (2 * nd[i]);
+      eel[q] = 2 * gd[i] * dt * exx[i] + sxxe[i];
+    }
+    s->N[V2C_NF_EXXS][m3] = 0.25 * (exx[k[0]] + exx[k[1]] + exx[k[2]] + exx[k[3]]);
+    s->N[V2C_NF_EXXPL][m3] = 0.25 * (epl[0] + epl[1] + epl[2] + epl[3]);
+    s->N[V2C_NF_SXXS][m3] = 0.25 * (sxx[k[0]] + sxx[k[1]] + sxx[k[2]] + sxx[k[3]]);
+    s->N[V2C_NF_PRS][m3] = 0.25 * (pr[k[0]] + pr[k[1]] + pr[k[2]] + pr[k[3]]);
+    s->N[V2C_NF_EXXEL][m3] = 0.25 * (eel[0] + eel[1] + eel[2] + eel[3]);
+  }
+  return 0;
+}
+
+/* interpolate_basic2center, interpolation.c:1639-1685: viscosity of each
+ * pressure node as the bilinear harmonic mean of the basic-node viscosity
+ * nu around the cell centre (weights clamped to the grid) */
+int v2c_oracle_basic2center(v2c_oracle_state *s) {
+  long xn = s->p.xnumx, yn = s->p.ynumy, nn = nnodes(s);
+  const double *gx = s->gx, *gy = s->gy, *nu = s->N[V2C_NF_NU];
+  for (long m3 = 0; m3 < nn; m3++) {
+    long m2 = m3 % yn, m1 = (m3 - m2) / yn;
+    if (!(m1 >= 1 && m2 >= 1)) continue;
+    double x = (gx[m1] + gx[m1 - 1]) / 2, y = (gy[m2] + gy[m2 - 1]) / 2;
+    long m10 = v2c_oracle_nxsearch(gx, xn, x), m20 = v2c_oracle_nxsearch(gy, yn, y);
+    if (m10 < 1) m10 = 1;
+    if (m10 > xn - 3) m10 = xn - 3;
+    if (m20 < 1) m20 = 1;
+    if (m20 > yn - 3) m20 = yn - 3;
+    double e = (x - gx[m10]) / (gx[m10 + 1] - gx[m10]);
+    double n = (y - gy[m20]) / (gy[m20 + 1] - gy[m20]);
+    if (e < 0) e = 0.0;
+    if (n < 0) n = 0.0;
+    if (e > 1) e = 1.0;
+    if (n > 1) n = 1.0;
+    double dm0 = (1.0 - e) * (1.0 - n), dm1 = (1.0 - e) * n, dm2 = e * (1.0 - n), dm3 = e * n;
+    long m4 = m10 * yn + m20;
+    s->N[V2C_NF_ND][m3] = 1.0 / (dm0 * 1.0 / nu[m4] + dm1 * 1.0 / nu[m4 + 1] +
+                                 dm2 * 1.0 / nu[m4 + yn] + dm3 * 1.0 / nu[m4 + yn + 1]);
+  }
+  return 0;
+}
+
+/* nueffcalc, momentum_continuity_addmatrix_checkerror.c:380-393: the
+ * visco-elastic factor Z and the computational viscosity Z*nvp (lower limit
+ * nubeg) */
+static double nueff_of(const v2c_params *p, double nvp, double ggeff, double dt, double *Z) {
+  *Z = ggeff * dt / (ggeff * dt + nvp);
+  double nueff = *Z * nvp;
+  if (nueff < p->nubeg) nueff = p->nubeg;
+  return nueff;
+}
+
+/* recompute_stress_strainrate, momentum_continuity_iterate.c:228-271 with
+ * sxxcalc and sxycalc (momentum_continuity_addmatrix_checkerror.c:446-481,
+ * 528-572): strain rates from the node velocities, visco-elastic stresses
+ * from the node viscosities and the previous elastic stresses */
+int v2c_oracle_recompute_stress(v2c_oracle_state *s, double dt) {
+  const v2c_params *p = &s->p;
+  long xn = p->xnumx, yn = p->ynumy, nn = nnodes(s);
+  double **N = s->N;
+  const double *gx = s->gx, *gy = s->gy, *vx = N[V2C_NF_VX], *vy = N[V2C_NF_VY];
+  for (long m3 = 0; m3 < nn; m3++) {
+    long m2 = m3 % yn, m1 = (m3 - m2) / yn;
+    if (!(m1 < xn && m2 < yn && m1 >= 1 && m2 >= 1)) continue;
+    long v0 = (m1 - 1) * yn + (m2 - 1), v1 = v0 + 1, v2 = v0 + yn, v3 = v2 + 1;
+    double Z, nueff;
+    nueff = nueff_of(p, N[V2C_NF_ND][v3], N[V2C_NF_GD][v3], dt, &Z);
+    double edotxx = 0.5 * ((vx[v2] - vx[v0]) / (gx[m1] - gx[m1 - 1]) -
+                           (vy[v1] - vy[v0]) / (gy[m2] - gy[m2 - 1]));
+    N[V2C_NF_EXX][m3] = edotxx;
+    N[V2C_NF_SXX][m3] = 2.0 * nueff * edotxx + N[V2C_NF_SXXE][v3] * (1.0 - Z);
+    if (m1 < xn - 1 && m2 < yn - 1) {
+      nueff = nueff_of(p, N[V2C_NF_NU][v3], N[V2C_NF_GG][v3], dt, &Z);
+      double exy1 = (vx[v3] - vx[v2]) / (gy[m2 + 1] - gy[m2 - 1]);
+      double exy2 = (vy[v3] - vy[v1]) / (gx[m1 + 1] - gx[m1 - 1]);
+      double edotxy = exy1 + exy2;
+      N[V2C_NF_EXY][m3] = edotxy;
+      N[V2C_NF_ESP][m3] = exy1 - exy2;
+      N[V2C_NF_SXY][m3] = 2.0 * nueff * edotxy + N[V2C_NF_SXYE][v3] * (1.0 - Z);
+    }
+  }
+  return 0;
+}
+
+/* copyarrays, momentum_continuity_iterate.c:265-281: the solved slip rate
+ * and state rate become the step's final ones (deltaVs, an output-only
+ * diagnostic, is not kept) */
+int v2c_oracle_copyarrays(v2c_oracle_state *s) {
+  long xn = s->p.xnumx, yn = s->p.ynumy, nn = nnodes(s);
+  double **N = s->N;
+  for (long m3 = 0; m3 < nn; m3++) {
+    long m2 = m3 % yn, m1 = (m3 - m2) / yn;
+    if (m1 >= 1 && m2 >= 1 && m1 < xn - 1 && m2 < yn - 1) {
+      N[V2C_NF_SLIPRS][m3] = N[V2C_NF_RK_SLIPRS_FINAL][m3] = N[V2C_NF_RK_SLIPRS_SOLVED][m3];
+      N[V2C_NF_RK_PHIDTS_FINAL][m3] = N[V2C_NF_RK_PHIDTS_SOLVED][m3];
+    }
+  }
+  return 0;
+}
+
 /* calc_vpvisc, calc_RSF.c:33-169 (rkmod 0 and 1) */
 static double vpvisc(v2c_oracle_state *s, int rk, double dt, long m3, double nP,
                      double W, int *err) {

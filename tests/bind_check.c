@@ -1,7 +1,9 @@
 /*
  * Test program for velo2cycles_gb300/bind/v2c_bind.c (built and run by
  * tests/test_gpu_bind.py): loads a case file into the reference's globals,
- * runs one MIC step with the reference's own routines, writes the result,
+ * runs one MIC step with the reference's own routines (interpolate_basic2center
+ * and interpolate_center2basic between the node updates, as the Picard loop
+ * calls them), writes the result,
  * restores the initial globals, runs the same step through the binding
  * (GPU) and writes that result.
  *   bind_check <case.bin> <ref_result.bin> <bind_result.bin>
@@ -73,6 +75,8 @@ int main(int argc, char **argv) {
   marker2nodes();
   interpolate_center2basic_old(timestep);
   compute_before_solve(timestep, 0);
+  interpolate_basic2center();
+  interpolate_center2basic(timestep);
   double d_ref = compute_after_solve(timestep, 0);
   nodes2markers();
   moveandrotatemarkers();
@@ -84,6 +88,8 @@ int main(int argc, char **argv) {
   v2c_bind_marker2nodes();
   v2c_bind_interpolate_center2basic_old(timestep);
   v2c_bind_compute_before_solve(timestep, 0);
+  v2c_bind_interpolate_basic2center();
+  v2c_bind_interpolate_center2basic(timestep);
   double d_bind = v2c_bind_compute_after_solve(timestep, 0);
   v2c_bind_nodes2markers();
   v2c_bind_moveandrotatemarkers();

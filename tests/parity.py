@@ -20,6 +20,9 @@ M2N_OUT = [abi.NF_PHIN, abi.NF_SXYEN, abi.NF_EXYEN, abi.NF_PEN, abi.NF_PHIS, abi
            abi.NF_MRY, abi.NF_RO, abi.NF_ET, abi.NF_HT, abi.NF_KT, abi.NF_CP, abi.NF_TK,
            abi.NF_STICKY01, abi.NF_NU, abi.NF_ND, abi.NF_MRX0, abi.NF_MRY0]
 C2B_OUT = [abi.NF_EXXES, abi.NF_SXXES, abi.NF_SPPES]
+# interpolate_basic2center, interpolate_center2basic (interpolation.c:1600-1685);
+# nd, exxpl and exxel carry the viscosity fields' error
+B2C_C2B_OUT = [abi.NF_ND, abi.NF_EXXS, abi.NF_EXXPL, abi.NF_SXXS, abi.NF_PRS, abi.NF_EXXEL]
 RSF_OUT = [abi.NF_PES, abi.NF_PHIS_IT, abi.NF_SYIELDS, abi.NF_NUVP_IT, abi.NF_SLIPRS, abi.NF_NU,
            abi.NF_RK_SLIPRS_SOLVED, abi.NF_RK_PHIDTS_SOLVED, abi.NF_RK_DELTAS]
 N2M_OUT = [abi.NF_PHISUM, abi.NF_WTPHISUM, abi.NF_SXYSUM, abi.NF_EXYSUM, abi.NF_ESUM,
@@ -36,9 +39,10 @@ MOVE_MARK = [abi.MF_X, abi.MF_Y, abi.MF_XX, abi.MF_XY, abi.MF_K, abi.MF_E]
 # exponent by ~6e-8 relative, i.e. ~2e-6 relative on exp(40).
 # The state rate RK_phidts_solved = V0/L e^-phi - V/L (calc_RSF.c:202) is a
 # difference of two terms that carries the same error through the slip rate
-# inverted from those viscosities.
+# inverted from those viscosities; nd (harmonic mean of nu) and exxpl, exxel
+# (through gd and nd_m2c, interpolation.c:1620-1632) carry it too.
 VISCOUS = {abi.NF_NU_M2C, abi.NF_GG, abi.NF_ND_M2C, abi.NF_GD, abi.NF_NUVP_IT, abi.NF_NU,
-           abi.NF_RK_PHIDTS_SOLVED}
+           abi.NF_RK_PHIDTS_SOLVED, abi.NF_ND, abi.NF_EXXPL, abi.NF_EXXEL}
 
 
 def rel_err(a: np.ndarray, b: np.ndarray) -> float:

@@ -20,7 +20,8 @@ import oracle
 from oracle import bindings as B
 from velo2cycles_gb300 import abi, build, synth
 
-from .parity import C2B_OUT, M2N_OUT, N2M_OUT, RSF_OUT, VISCOUS, nxsearch_np, rel_err
+from .parity import (B2C_C2B_OUT, C2B_OUT, M2N_OUT, N2M_OUT, RSF_OUT, VISCOUS, nxsearch_np,
+                     rel_err)
 
 pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -56,7 +57,7 @@ def test_binding_step_matches_reference(bind_check):
     got = B.read_result(r_bind, c.nodenum)
     names = abi.node_field_names()
     bad = {}
-    for f in M2N_OUT + C2B_OUT + RSF_OUT + N2M_OUT:
+    for f in M2N_OUT + C2B_OUT + B2C_C2B_OUT + RSF_OUT + N2M_OUT:
         a, b = got["nodes"][f].copy(), ref["nodes"][f].copy()
         if f in RAW_SUMS:
             a[0] = b[0] = 0.0

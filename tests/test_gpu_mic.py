@@ -14,7 +14,7 @@ import pytest
 import oracle
 from velo2cycles_gb300 import abi, mic, synth
 
-from .parity import (C2B_OUT, M2N_OUT, MOVE_MARK, N2M_MARK, N2M_OUT, RSF_OUT, VISCOUS,
+from .parity import (B2C_C2B_OUT, C2B_OUT, M2N_OUT, MOVE_MARK, N2M_MARK, N2M_OUT, RSF_OUT, VISCOUS,
                      node_errors, marker_errors, nxsearch_np)
 
 pytestmark = pytest.mark.gpu
@@ -71,6 +71,20 @@ def test_center2basic_and_node_rsf(case):
     got = m.download_nodes(C2B_OUT + RSF_OUT)
     _check_nodes(node_errors(got, ref.nodes, C2B_OUT + RSF_OUT))
     assert abs(d_gpu - d_ref) <= 1e-5 * max(abs(d_ref), 1.0)
+    m.close()
+
+
+def test_basic2center_center2basic(case):
+    """The Picard loop's node interpolations after marker2nodes and
+    compute_before_solve, on the GPU's own node fields."""
+    dt = case.params["timestep"]
+    m = mic.from_case(case)
+    ref = oracle.Restatement(case.copy())
+    m.marker2nodes(); ref.marker2nodes()
+    m.compute_before_solve(dt, 0); ref.compute_before_solve(dt, 0)
+    m.interpolate_basic2center(); ref.basic2center()
+    m.interpolate_center2basic(dt); ref.center2basic(dt)
+    _check_nodes(node_errors(m.download_nodes(B2C_C2B_OUT), ref.nodes, B2C_C2B_OUT))
     m.close()
 
 

@@ -88,6 +88,57 @@ def test_restatement_bit_exact_nonuniform_grid():
     assert not _compare(r, ref["nodes"], ref["marks"])
 
 
+@needs_ref
+@pytest.mark.parametrize("name,seed", [("small", 8), ("c2", 3)])
+def test_basic2center_center2basic_bit_exact_vs_reference(name, seed):
+    """interpolate_basic2center and interpolate_center2basic
+    (interpolation.c:1600-1685) after marker2nodes and compute_before_solve,
+    as the Picard loop calls them, on a uniform and the non-uniform C2 grid."""
+    kw = dict(n_markers=100000) if name == "c2" else {}
+    c = synth.make_case(name, seed, **kw)
+    stages = (1 << B.STAGE_M2N) | (1 << B.STAGE_BEFORE) | B.B2C_STAGE | B.C2B_FULL_STAGE
+    ref = B.run_reference(c, stages=stages, nthreads=1)
+    r = oracle.Restatement(c.copy(), phantom=True)
+    dt = c.params["timestep"]
+    r.marker2nodes()
+    r.compute_before_solve(dt, 0)
+    assert r.basic2center() == 0
+    assert r.center2basic(dt) == 0
+    assert not _compare(r, ref["nodes"], ref["marks"])
+    nd = r.nodes[abi.NF_ND]
+    assert np.isfinite(nd).sum() > 0.9 * nd.size
+
+
+@needs_ref
+@pytest.mark.parametrize("name,seed", [("small", 9), ("c2", 4)])
+def test_picard_node_sequence_bit_exact_vs_reference(name, seed):
+    """The node routines of one Picard pass in the reference's order
+    (momentum_continuity_iterate.c:69-92) with the Stokes solve replaced by
+    the given velocities: compute_before_solve, interpolate_basic2center,
+    recompute_stress_strainrate, interpolate_center2basic,
+    compute_after_solve, copyarrays."""
+    kw = dict(n_markers=100000) if name == "c2" else {}
+    c = synth.make_case(name, seed, **kw)
+    stages = ((1 << B.STAGE_M2N) | (1 << B.STAGE_BEFORE) | B.B2C_STAGE | B.RECOMPUTE_STAGE |
+              B.C2B_FULL_STAGE | (1 << B.STAGE_AFTER) | B.COPY_STAGE)
+    ref = B.run_reference(c, stages=stages, nthreads=1)
+    r = oracle.Restatement(c.copy(), phantom=True)
+    dt = c.params["timestep"]
+    r.marker2nodes()
+    r.compute_before_solve(dt, 0)
+    r.basic2center()
+    assert r.recompute_stress(dt) == 0
+    r.center2basic(dt)
+    r.compute_after_solve(dt, 0)
+    assert r.copyarrays() == 0
+    assert not _compare(r, ref["nodes"], ref["marks"])
+    yn = c.gy.size
+    m = np.arange(c.nodenum)
+    inner = (m // yn >= 1) & (m % yn >= 1) & (m // yn < c.gx.size - 1) & (m % yn < yn - 1)
+    assert np.array_equal(r.nodes[abi.NF_RK_SLIPRS_FINAL][inner],
+                          r.nodes[abi.NF_RK_SLIPRS_SOLVED][inner], equal_nan=True)
+
+
 def test_nxsearch_ties_and_clamps():
     g = np.array([0.0, 1.0, 2.0, 4.0, 8.0])
     assert B.nxsearch(g, 2.0) == 2          # on a line: ties go left of the upper limit

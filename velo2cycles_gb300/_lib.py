@@ -39,6 +39,13 @@ _SIGS = {
     "v2c_download_cells": [c_ctx, P(ctypes.c_int32), ctypes.c_long],
     "v2c_upload_node_field": [c_ctx, ctypes.c_int, c_dp],
     "v2c_download_node_field": [c_ctx, ctypes.c_int, c_dp],
+    "v2c_interpolate_basic2center": [c_ctx],
+    "v2c_interpolate_center2basic": [c_ctx, ctypes.c_double],
+    "v2c_recompute_stress_strainrate": [c_ctx, ctypes.c_double],
+    "v2c_copyarrays": [c_ctx],
+    "v2c_cycle_set_velocity": [c_ctx, ctypes.c_int, c_dp, c_dp],
+    "v2c_cycle_step": [c_ctx, ctypes.c_int, ctypes.c_double, ctypes.c_int],
+    "v2c_cycle_slip": [c_ctx, c_dp],
     "v2c_upload_node_fields": [c_ctx, ctypes.c_int, P(ctypes.c_int), P(c_dp)],
     "v2c_download_node_fields": [c_ctx, ctypes.c_int, P(ctypes.c_int), P(c_dp)],
     "v2c_marker2nodes": [c_ctx],

@@ -170,6 +170,24 @@ double v2c_bind_interpolate_center2basic_old(double dt) {
   return 0;
 }
 
+double v2c_bind_interpolate_basic2center(void) {
+  static const int out[] = {V2C_NF_ND};
+  if (!v2c_bind_setup() || !v2c_bind_nodes_up()) return 0;
+  if (!v2c_bind_ok(v2c_interpolate_basic2center(v2c_bind_ctx), "v2c_interpolate_basic2center"))
+    return 0;
+  v2c_bind_nodes_down(out, V2C_BIND_LEN(out));
+  return 0;
+}
+
+double v2c_bind_interpolate_center2basic(double dt) {
+  static const int out[] = {V2C_NF_EXXS, V2C_NF_EXXPL, V2C_NF_SXXS, V2C_NF_PRS, V2C_NF_EXXEL};
+  if (!v2c_bind_setup() || !v2c_bind_nodes_up()) return 0;
+  if (!v2c_bind_ok(v2c_interpolate_center2basic(v2c_bind_ctx, dt), "v2c_interpolate_center2basic"))
+    return 0;
+  v2c_bind_nodes_down(out, V2C_BIND_LEN(out));
+  return 0;
+}
+
 void v2c_bind_compute_before_solve(double dt, int rk) {
   if (!v2c_bind_setup() || !v2c_bind_nodes_up()) return;
   if (!v2c_bind_ok(v2c_compute_before_solve(v2c_bind_ctx, dt, rk), "v2c_compute_before_solve"))

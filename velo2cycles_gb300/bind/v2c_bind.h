@@ -16,6 +16,9 @@
  *   moveandrotatemarkers()               -> v2c_bind_moveandrotatemarkers()
  *   calc_timestep(oldornew)              -> v2c_bind_calc_timestep(oldornew)
  *                                           (momentum_continuity_iterate.c:44,92)
+ *   interpolate_basic2center()           -> v2c_bind_interpolate_basic2center()
+ *   interpolate_center2basic(dt)         -> v2c_bind_interpolate_center2basic(dt)
+ *                                           (momentum_continuity_iterate.c:71,87)
  *
  * Data movement.  The host arrays stay the truth for everything the host
  * solvers read and write.  Every call uploads the node arrays and brings
@@ -45,6 +48,8 @@ double v2c_bind_compute_after_solve(double dt, int rk);
 double v2c_bind_nodes2markers(void);
 void v2c_bind_moveandrotatemarkers(void);
 double v2c_bind_calc_timestep(int oldornew);
+double v2c_bind_interpolate_basic2center(void);
+double v2c_bind_interpolate_center2basic(double dt);
 
 /* the host changed marker arrays (temperature solve, loading a file) */
 void v2c_bind_markers_changed(void);

@@ -106,6 +106,8 @@ static double *v2c_bind_node_array(int f) {
     case V2C_NF_MRX0: return mrx0;
     case V2C_NF_MRY0: return mry0;
     case V2C_NF_PRS: return prs;
+    case V2C_NF_EXXS: return exxs;
+    case V2C_NF_EXXEL: return exxel;
   }
   return NULL;
 }

@@ -84,6 +84,20 @@ struct v2c_ctx {
   double prof_ms[V2C_PROF_N] = {};
   long prof_n[V2C_PROF_N] = {};
   std::vector<cudaEvent_t> ev_pool;
+  // seismic-cycle workload: per-regime velocity fields, accumulated slip,
+  // captured step graphs
+  float *d_cyc_v[2] = {nullptr, nullptr};  // [regime]: vx then vy, 2 nn floats
+  double *d_slip = nullptr;                 // accumulated slip per node
+  struct CycleGraph {
+    int regime;
+    double dt;
+    const void *pos;      // position buffer holding the current positions
+    v2c_params p;         // all parameters, timesum zeroed
+    int flags;            // the timesum classes the kernels see
+    cudaGraphExec_t exec;
+    long launches;        // kernels in one replay
+  };
+  std::vector<CycleGraph> graphs;
 };
 
 namespace {
@@ -287,6 +301,11 @@ extern "C" int v2c_create(const v2c_params *p, long max_markers, void *cuda_stre
 extern "C" int v2c_destroy(v2c_ctx *ctx) {
   if (!ctx) return V2C_ERR_ARG;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (auto &gr : ctx->graphs) cudaGraphExecDestroy(gr.exec);
+  ctx->graphs.clear();
+  for (float *v : ctx->d_cyc_v)
+    if (v) cudaFree(v);
+  if (ctx->d_slip) cudaFree(ctx->d_slip);
   void *ptrs[] = {ctx->d_gx, ctx->d_gy, ctx->d_wx, ctx->d_wy, ctx->d_gxf, ctx->d_gyf,
                   ctx->d_rock, ctx->d_node, ctx->d_node64, ctx->d_sticky, ctx->d_quad, ctx->d_list_n, ctx->d_ts,
                   ctx->d_stat, ctx->d_red, ctx->d_nstage,
@@ -816,6 +835,52 @@ extern "C" int v2c_center2basic_old(v2c_ctx *ctx) {
   return V2C_OK;
 }
 
+extern "C" int v2c_interpolate_basic2center(v2c_ctx *ctx) {
+  if (!ctx) return V2C_ERR_ARG;
+  if (!ctx->have_grid) return fail(ctx, V2C_ERR_STATE);
+  {
+    Prof pr(ctx, V2C_PROF_B2C);
+    launch_b2c(make_grid(ctx), make_nodes(ctx), ctx->d_stat, ctx->stream);
+  }
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  return V2C_OK;
+}
+
+extern "C" int v2c_interpolate_center2basic(v2c_ctx *ctx, double dt) {
+  if (!ctx) return V2C_ERR_ARG;
+  if (!ctx->have_grid) return fail(ctx, V2C_ERR_STATE);
+  {
+    Prof pr(ctx, V2C_PROF_B2C);
+    launch_c2b(make_grid(ctx), make_nodes(ctx), (float)dt, ctx->stream);
+  }
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  return V2C_OK;
+}
+
+extern "C" int v2c_recompute_stress_strainrate(v2c_ctx *ctx, double dt) {
+  if (!ctx) return V2C_ERR_ARG;
+  if (!ctx->have_grid) return fail(ctx, V2C_ERR_STATE);
+  {
+    Prof pr(ctx, V2C_PROF_B2C);
+    launch_recompute(make_grid(ctx), make_nodes(ctx), make_scal(ctx->p, ctx->h_rt), (float)dt,
+                     ctx->stream);
+  }
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  return V2C_OK;
+}
+
+extern "C" int v2c_copyarrays(v2c_ctx *ctx) {
+  if (!ctx) return V2C_ERR_ARG;
+  if (!ctx->have_grid) return fail(ctx, V2C_ERR_STATE);
+  launch_copyarrays(make_grid(ctx), make_nodes(ctx), ctx->stream);
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  return V2C_OK;
+}
+
 extern "C" int v2c_compute_before_solve(v2c_ctx *ctx, double dt, int rk) {
   if (!ctx) return V2C_ERR_ARG;
   {
@@ -919,6 +984,129 @@ extern "C" int v2c_synchronize(v2c_ctx *ctx) {
   if (!ctx) return V2C_ERR_ARG;
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaGetLastError());
+  return V2C_OK;
+}
+
+// ======================================================= seismic cycle
+extern "C" int v2c_cycle_set_velocity(v2c_ctx *ctx, int regime, const double *vx,
+                                      const double *vy) {
+  if (!ctx || regime < 0 || regime > 1 || !vx || !vy) return V2C_ERR_ARG;
+  if (!ctx->have_grid) return fail(ctx, V2C_ERR_STATE);
+  const long nn = ctx->nn;
+  if (!ctx->d_cyc_v[regime]) CK(cudaMalloc(&ctx->d_cyc_v[regime], sizeof(float) * 2 * nn));
+  if (!ctx->d_slip) CK(cudaMalloc(&ctx->d_slip, sizeof(double) * nn));
+  cudaStream_t st = ctx->stream;
+  const double *src[2] = {vx, vy};
+  for (int k = 0; k < 2; k++) {
+    CK(cudaMemcpyAsync(ctx->d_node64, src[k], sizeof(double) * nn, cudaMemcpyHostToDevice, st));
+    launch_node_to_f32(ctx->d_node64, ctx->d_cyc_v[regime] + k * nn, nn, st);
+  }
+  if (regime == 0) CK(cudaMemsetAsync(ctx->d_slip, 0, sizeof(double) * nn, st));
+  CK(cudaStreamSynchronize(st));
+  return V2C_OK;
+}
+
+// the launches of one cycle step (no host synchronisation: capturable)
+static int cycle_enqueue(v2c_ctx *ctx, int regime, double dt) {
+  cudaStream_t st = ctx->stream;
+  const long nn = ctx->nn;
+  CK(cudaMemcpyAsync(ctx->d_node + (long)V2C_NF_VX * nn, ctx->d_cyc_v[regime],
+                     sizeof(float) * nn, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_node + (long)V2C_NF_VY * nn, ctx->d_cyc_v[regime] + nn,
+                     sizeof(float) * nn, cudaMemcpyDeviceToDevice, st));
+  int rc;
+  if ((rc = v2c_marker2nodes(ctx))) return rc;
+  if ((rc = v2c_center2basic_old(ctx))) return rc;
+  if ((rc = v2c_compute_before_solve(ctx, dt, 0))) return rc;
+  if ((rc = v2c_interpolate_basic2center(ctx))) return rc;
+  if ((rc = v2c_recompute_stress_strainrate(ctx, dt))) return rc;
+  if ((rc = v2c_interpolate_center2basic(ctx, dt))) return rc;
+  if ((rc = v2c_compute_after_solve(ctx, dt, 0, nullptr))) return rc;
+  if ((rc = v2c_copyarrays(ctx))) return rc;
+  launch_slip_acc(make_grid(ctx), make_nodes(ctx), dt, ctx->d_slip, st);
+  ctx->launches += 1;
+  return n2m_move(ctx, 1, 1);
+}
+
+static int cycle_flags(const v2c_ctx *ctx) {
+  const Scal s = make_scal(ctx->p, ctx->h_rt);
+  return s.antid | s.phi_reset0 << 1 | s.sticky_cap << 2 | s.sppe_nstress << 3 |
+         s.timesum_pos << 4 | s.timesum_zero << 5;
+}
+
+extern "C" int v2c_cycle_step(v2c_ctx *ctx, int regime, double dt, int use_graph) {
+  int rc = ready(ctx);
+  if (rc) return rc;
+  if (regime < 0 || regime > 1 || !(dt > 0)) return fail(ctx, V2C_ERR_ARG);
+  if (!ctx->d_cyc_v[regime] || !ctx->d_slip) return fail(ctx, V2C_ERR_STATE);
+  ctx->p.timestep = dt;
+  cudaStream_t st = ctx->stream;
+  if (!use_graph) {
+    rc = cycle_enqueue(ctx, regime, dt);
+    if (rc) return rc;
+    ctx->p.timesum += dt;
+    return V2C_OK;
+  }
+  // work the capture must not contain: the first sort and the boundary rows
+  if (!ctx->sorted) {
+    launch_sort(ctx->m.cell_in, ctx->m.u_in, ctx->m.v_in, ctx->n, ctx->ncell, ctx->sb,
+                ctx->d_stat, st);
+    ctx->sorted = true;
+  }
+  if (ctx->have_bonds && (rc = build_bc(ctx))) return fail(ctx, rc);
+  v2c_params pk = ctx->p;
+  pk.timesum = 0;
+  const int flags = cycle_flags(ctx);
+  const void *pos = ctx->m.cell_in;
+  for (auto &gr : ctx->graphs) {
+    if (gr.regime == regime && gr.dt == dt && gr.pos == pos && gr.flags == flags &&
+        !memcmp(&gr.p, &pk, sizeof(pk))) {
+      CK(cudaGraphLaunch(gr.exec, st));
+      // the host side of the step the graph replays
+      swap_positions(ctx);
+      ctx->sorted = true;
+      ctx->launches += gr.launches;
+      ctx->p.timesum += dt;
+      return V2C_OK;
+    }
+  }
+  // capture: the enqueue does the step's host bookkeeping (position swap)
+  // as it records, so afterwards the host state is the one after the step
+  const Markers saved = ctx->m;
+  const long l0 = ctx->launches;
+  const bool prof = ctx->prof;
+  ctx->prof = false;
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  rc = cycle_enqueue(ctx, regime, dt);
+  const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+  ctx->prof = prof;
+  cudaGraphExec_t exec = nullptr;
+  if (!rc && ce == cudaSuccess && graph && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+    exec = nullptr;
+  if (graph) cudaGraphDestroy(graph);
+  if (rc || ce != cudaSuccess || !exec) {
+    ctx->m = saved;  // nothing ran
+    ctx->launches = l0;
+    cudaGetLastError();
+    return fail(ctx, rc ? rc : V2C_ERR_CUDA);
+  }
+  if (ctx->graphs.size() >= 8) {
+    cudaGraphExecDestroy(ctx->graphs.front().exec);
+    ctx->graphs.erase(ctx->graphs.begin());
+  }
+  ctx->graphs.push_back({regime, dt, pos, pk, flags, exec, ctx->launches - l0});
+  CK(cudaGraphLaunch(exec, st));
+  ctx->p.timesum += dt;
+  return V2C_OK;
+}
+
+extern "C" int v2c_cycle_slip(v2c_ctx *ctx, double *out) {
+  if (!ctx || !out) return V2C_ERR_ARG;
+  if (!ctx->d_slip) return fail(ctx, V2C_ERR_STATE);
+  CK(cudaMemcpyAsync(out, ctx->d_slip, sizeof(double) * ctx->nn, cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   return V2C_OK;
 }
 

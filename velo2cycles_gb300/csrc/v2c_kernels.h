@@ -92,6 +92,11 @@ void launch_fields_to_f32(const double *stage, long nn, const int *fields, int c
                           cudaStream_t st);
 
 void launch_c2b_old(const Grid &g, const Nodes &N, cudaStream_t st);
+void launch_c2b(const Grid &g, const Nodes &N, float dt, cudaStream_t st);
+void launch_b2c(const Grid &g, const Nodes &N, unsigned long long *stat, cudaStream_t st);
+void launch_recompute(const Grid &g, const Nodes &N, const Scal &S, float dt, cudaStream_t st);
+void launch_copyarrays(const Grid &g, const Nodes &N, cudaStream_t st);
+void launch_slip_acc(const Grid &g, const Nodes &N, double dt, double *acc, cudaStream_t st);
 void launch_before_solve(const Grid &g, const Nodes &N, const Scal &S, double dt, int rk,
                          unsigned long long *stat, cudaStream_t st);
 void launch_after_solve(const Grid &g, const Nodes &N, const Scal &S, double dt, int rk,

@@ -52,6 +52,131 @@ __device__ __forceinline__ float new_state(float ph, float V, float dt, float L,
   return hi + log1pf(expf(lo - hi));
 }
 
+// interpolate_center2basic (interpolation.c:1600-1637): means of the four
+// pressure nodes around each interior basic node; the plastic and elastic
+// strain rates use the reference's per-node terms (IEEE division: a node no
+// marker reached has gd = 0 and gives inf as in the reference)
+__global__ void k_c2b(Grid g, Nodes N, float dt) {
+  long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (m3 >= g.nn) return;
+  const long yn = g.yn;
+  long m2 = m3 % yn, m1 = m3 / yn;
+  if (!(m1 >= 1 && m2 >= 1 && m1 < g.xn - 1 && m2 < g.yn - 1)) return;
+  const float *exx = N.f(V2C_NF_EXX), *sxx = N.f(V2C_NF_SXX), *sxxe = N.f(V2C_NF_SXXE);
+  const float *gd = N.f(V2C_NF_GD), *nd = N.f(V2C_NF_ND_M2C), *pr = N.f(V2C_NF_PR);
+  float se = 0.f, ss = 0.f, sp = 0.f, spl = 0.f, sel = 0.f;
+  const long k[4] = {m3, m3 + 1, m3 + yn, m3 + yn + 1};
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const long i = k[q];
+    const float e = exx[i], s = sxx[i], s0 = sxxe[i], G = gd[i];
+    se += e; ss += s; sp += pr[i];
+    spl += e - (s - s0) / (2.f * G * dt) - s / (2.f * nd[i]);
+    sel += 2.f * G * dt * e + s0;
+  }
+  N.f(V2C_NF_EXXS)[m3] = 0.25f * se;
+  N.f(V2C_NF_EXXPL)[m3] = 0.25f * spl;
+  N.f(V2C_NF_SXXS)[m3] = 0.25f * ss;
+  N.f(V2C_NF_PRS)[m3] = 0.25f * sp;
+  N.f(V2C_NF_EXXEL)[m3] = 0.25f * sel;
+}
+
+// bilinear weight of the centre between lines m1-1 and m1 against the
+// clamped basic stencil [m10, m10+1] (interpolation.c:1655-1667): the
+// centre lies in cell m1-1 (nxsearch of the midpoint, checked in FP64 for
+// a midpoint that rounds onto line m1), so the weight is 1/2 inside and
+// clamps to 0 or 1 where the stencil was shifted at the edges
+__device__ __forceinline__ int centre_stencil(const double *gl, const float *w, int n, int m1,
+                                              float &e) {
+  const double x = (gl[m1] + gl[m1 - 1]) / 2;
+  int nx = (x >= gl[m1] && m1 <= n - 2) ? m1 : m1 - 1;
+  int m10 = nx < 1 ? 1 : (nx > n - 3 ? n - 3 : nx);
+  // offset of the midpoint from line m10: half the cell inside, FP64 at the
+  // shifted edge stencils (where the weight clamps to 0 or 1)
+  const float X = (m10 == nx && nx == m1 - 1) ? 0.5f * __ldg(w + m1 - 1) : (float)(x - gl[m10]);
+  e = X / __ldg(w + m10);
+  e = fminf(fmaxf(e, 0.f), 1.f);
+  return m10;
+}
+
+// interpolate_basic2center (interpolation.c:1639-1685): nd at every node
+// with m1, m2 >= 1 as the harmonic mean of nu over the basic stencil
+__global__ void k_b2c(Grid g, Nodes N, unsigned long long *stat) {
+  long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (m3 >= g.nn) return;
+  const long yn = g.yn;
+  const int m2 = (int)(m3 % yn), m1 = (int)(m3 / yn);
+  if (!(m1 >= 1 && m2 >= 1)) return;
+  float e, n;
+  const int m10 = centre_stencil(g.gx, g.wx, g.xn, m1, e);
+  const int m20 = centre_stencil(g.gy, g.wy, g.yn, m2, n);
+  const float dm0 = (1.f - e) * (1.f - n), dm1 = (1.f - e) * n, dm2 = e * (1.f - n), dm3 = e * n;
+  const float *nu = N.f(V2C_NF_NU);
+  const long m4 = (long)m10 * yn + m20;
+  const float nd = 1.f / (dm0 / nu[m4] + dm1 / nu[m4 + 1] + dm2 / nu[m4 + yn] + dm3 / nu[m4 + yn + 1]);
+  N.f(V2C_NF_ND)[m3] = nd;
+  if (!(nd > 0.f)) atomicAdd(stat + ST_NAN, 1ull);  // the reference prints these
+}
+
+// nueffcalc (momentum_continuity_addmatrix_checkerror.c:380-393)
+__device__ __forceinline__ float nueff_of(float nvp, float ggeff, float dt, float nubeg, float &Z) {
+  Z = ggeff * dt / (ggeff * dt + nvp);
+  const float nueff = Z * nvp;
+  return nueff < nubeg ? nubeg : nueff;
+}
+
+// recompute_stress_strainrate (momentum_continuity_iterate.c:214-262) with
+// sxxcalc / sxycalc (momentum_continuity_addmatrix_checkerror.c:446-572):
+// strain rates from the node velocities, visco-elastic stresses from the
+// node viscosities and the previous elastic stresses.  Line spacings are
+// sums of the FP32 cell widths.
+__global__ void k_recompute(Grid g, Nodes N, float dt, float nubeg) {
+  long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (m3 >= g.nn) return;
+  const long yn = g.yn;
+  const int m2 = (int)(m3 % yn), m1 = (int)(m3 / yn);
+  if (!(m1 >= 1 && m2 >= 1)) return;
+  const long v0 = m3 - yn - 1, v1 = v0 + 1, v2 = v0 + yn;
+  const float *vx = N.f(V2C_NF_VX), *vy = N.f(V2C_NF_VY);
+  float Z;
+  float nueff = nueff_of(N.f(V2C_NF_ND)[m3], N.f(V2C_NF_GD)[m3], dt, nubeg, Z);
+  const float edotxx = 0.5f * ((vx[v2] - vx[v0]) / __ldg(g.wx + m1 - 1) -
+                               (vy[v1] - vy[v0]) / __ldg(g.wy + m2 - 1));
+  N.f(V2C_NF_EXX)[m3] = edotxx;
+  N.f(V2C_NF_SXX)[m3] = 2.f * nueff * edotxx + N.f(V2C_NF_SXXE)[m3] * (1.f - Z);
+  if (m1 < g.xn - 1 && m2 < g.yn - 1) {
+    nueff = nueff_of(N.f(V2C_NF_NU)[m3], N.f(V2C_NF_GG)[m3], dt, nubeg, Z);
+    const float exy1 = (vx[m3] - vx[v2]) / (__ldg(g.wy + m2 - 1) + __ldg(g.wy + m2));
+    const float exy2 = (vy[m3] - vy[v1]) / (__ldg(g.wx + m1 - 1) + __ldg(g.wx + m1));
+    N.f(V2C_NF_EXY)[m3] = exy1 + exy2;
+    N.f(V2C_NF_ESP)[m3] = exy1 - exy2;
+    N.f(V2C_NF_SXY)[m3] = 2.f * nueff * (exy1 + exy2) + N.f(V2C_NF_SXYE)[m3] * (1.f - Z);
+  }
+}
+
+// copyarrays (momentum_continuity_iterate.c:265-281): the solved slip and
+// state rates become the final ones
+__global__ void k_copyarrays(Grid g, Nodes N) {
+  long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (m3 >= g.nn) return;
+  const long yn = g.yn;
+  const long m2 = m3 % yn, m1 = m3 / yn;
+  if (!(m1 >= 1 && m2 >= 1 && m1 < g.xn - 1 && m2 < g.yn - 1)) return;
+  const float v = N.f(V2C_NF_RK_SLIPRS_SOLVED)[m3];
+  N.f(V2C_NF_SLIPRS)[m3] = v;
+  N.f(V2C_NF_RK_SLIPRS_FINAL)[m3] = v;
+  N.f(V2C_NF_RK_PHIDTS_FINAL)[m3] = N.f(V2C_NF_RK_PHIDTS_SOLVED)[m3];
+}
+
+// accumulated slip of every interior basic node: acc += dt * slip rate
+__global__ void k_slip_acc(Grid g, const float *v, double dt, double *acc) {
+  long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (m3 >= g.nn) return;
+  const long yn = g.yn;
+  const long m2 = m3 % yn, m1 = m3 / yn;
+  if (m1 >= 1 && m2 >= 1 && m1 < g.xn - 1 && m2 < g.yn - 1) acc[m3] += dt * (double)v[m3];
+}
+
 __global__ void k_c2b_old(Grid g, Nodes N) {
   long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (m3 >= g.nn) return;
@@ -265,6 +390,21 @@ void launch_c2b_old(const Grid &g, const Nodes &N, cudaStream_t st) {
   k_c2b_old<<<nblk(g.nn, 256), 256, 0, st>>>(g, N);
 }
 
+void launch_c2b(const Grid &g, const Nodes &N, float dt, cudaStream_t st) {
+  k_c2b<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, dt);
+}
+void launch_recompute(const Grid &g, const Nodes &N, const Scal &S, float dt, cudaStream_t st) {
+  k_recompute<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, dt, S.nubeg_f);
+}
+void launch_copyarrays(const Grid &g, const Nodes &N, cudaStream_t st) {
+  k_copyarrays<<<nblk(g.nn, 256), 256, 0, st>>>(g, N);
+}
+void launch_slip_acc(const Grid &g, const Nodes &N, double dt, double *acc, cudaStream_t st) {
+  k_slip_acc<<<nblk(g.nn, 256), 256, 0, st>>>(g, N.f(V2C_NF_RK_SLIPRS_FINAL), dt, acc);
+}
+void launch_b2c(const Grid &g, const Nodes &N, unsigned long long *stat, cudaStream_t st) {
+  k_b2c<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, stat);
+}
 void launch_before_solve(const Grid &g, const Nodes &N, const Scal &S, double dt, int rk,
                          unsigned long long *stat, cudaStream_t st) {
   k_before<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, S, (float)dt, rk, stat);

@@ -157,6 +157,44 @@ class MarkerInCell:
     def interpolate_center2basic_old(self):
         call("v2c_center2basic_old", self.h)
 
+    def interpolate_basic2center(self):
+        """interpolate_basic2center (interpolation.c:1639): nd at the pressure
+        nodes, harmonic mean of nu."""
+        call("v2c_interpolate_basic2center", self.h)
+
+    def interpolate_center2basic(self, dt: float):
+        """interpolate_center2basic (interpolation.c:1600): exxs, exxpl, sxxs,
+        prs, exxel on the basic nodes."""
+        call("v2c_interpolate_center2basic", self.h, float(dt))
+
+    def recompute_stress_strainrate(self, dt: float):
+        """recompute_stress_strainrate (momentum_continuity_iterate.c:214):
+        node strain rates and visco-elastic stresses from vx, vy."""
+        call("v2c_recompute_stress_strainrate", self.h, float(dt))
+
+    def copyarrays(self):
+        """copyarrays (momentum_continuity_iterate.c:265)."""
+        call("v2c_copyarrays", self.h)
+
+    def cycle_set_velocity(self, regime: int, vx: np.ndarray, vy: np.ndarray):
+        """Velocity field of a seismic-cycle regime (0 interseismic, 1
+        coseismic); regime 0 also zeroes the accumulated slip."""
+        a = np.ascontiguousarray(vx, dtype=np.float64)
+        b = np.ascontiguousarray(vy, dtype=np.float64)
+        assert a.size == self.nn and b.size == self.nn
+        call("v2c_cycle_set_velocity", self.h, int(regime), _ptr(a), _ptr(b))
+
+    def cycle_step(self, regime: int, dt: float, use_graph: bool = True):
+        """One seismic-cycle step (see v2c_cycle_step); timesum advances."""
+        call("v2c_cycle_step", self.h, int(regime), float(dt), int(bool(use_graph)))
+        self.params["timestep"] = float(dt)
+        self.params["timesum"] = float(self.params["timesum"]) + float(dt)
+
+    def cycle_slip(self) -> np.ndarray:
+        a = np.zeros(self.nn)
+        call("v2c_cycle_slip", self.h, _ptr(a))
+        return a
+
     def compute_before_solve(self, dt: float, rk: int = 0):
         call("v2c_compute_before_solve", self.h, float(dt), int(rk))
 
