@@ -216,7 +216,8 @@ def run_reference_arm(args, rank: int) -> None:
         "ms_per_step": base["seconds_per_step"] * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "c4 marker-in-cell step (bounded window, see cpu_baseline.sample)"},
-        "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample",
+                                              "value_1thread")},
         "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -473,7 +474,8 @@ def run_gpu(args, rank: int, world: int) -> None:
         "step_alg_bytes_per_marker": step_alg,
         "step_roofline_frac": (value / world) * step_alg / (peaks["hbm_gbs"] * 1e9),
         "roofline": roof,
-        "cpu_baseline": ({k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        "cpu_baseline": ({k: base[k] for k in ("value", "unit", "cores", "kind", "sample",
+                                               "value_1thread")}
                          if base else None),
         "e2e": ({"value": replica_throughput(n, world, ms_e2e), "unit": UNIT,
                  "h2d_bytes_per_step": 8 * nn * len(E2E_UP),
@@ -485,6 +487,244 @@ def run_gpu(args, rank: int, world: int) -> None:
     m.close()
     if dist:
         dist.destroy_process_group()
+
+
+# ---------------------------------------------------- seismic cycle (C5)
+class _OracleCycle:
+    """The cycle step on the oracle restatement (FP64): the reference's own
+    algorithm, for the drift figures of the GPU reference form."""
+
+    def __init__(self, case, fields):
+        import oracle
+        self.r = oracle.Restatement(case.copy())
+        self.fields = fields
+        self.timesum = float(case.params["timesum"])
+        self.slip = np.zeros(case.nodenum)
+        yn = case.gy.size
+        m = np.arange(case.nodenum)
+        self.inner = ((m // yn >= 1) & (m % yn >= 1) & (m // yn < case.gx.size - 1) &
+                      (m % yn < yn - 1))
+
+    def cycle_step(self, regime, dt):
+        from velo2cycles_gb300 import abi
+        r = self.r
+        r.nodes[abi.NF_VX][:] = self.fields[regime][0]
+        r.nodes[abi.NF_VY][:] = self.fields[regime][1]
+        r.set_params(timestep=dt, timesum=self.timesum)
+        r.marker2nodes(); r.center2basic_old(); r.compute_before_solve(dt, 0); r.basic2center()
+        r.recompute_stress(dt); r.center2basic(dt); r.compute_after_solve(dt, 0); r.copyarrays()
+        self.slip[self.inner] += dt * r.nodes[abi.NF_RK_SLIPRS_FINAL][self.inner]
+        r.nodes2markers(); r.move()
+        self.timesum += dt
+        r.set_params(timesum=self.timesum)
+
+    def calc_timestep(self, oldornew):
+        return self.r.calc_timestep(oldornew)[1]
+
+
+class _GpuCycle:
+    def __init__(self, m, graph):
+        self.m, self.graph = m, graph
+
+    def cycle_step(self, regime, dt):
+        self.m.cycle_step(regime, dt, use_graph=self.graph)
+
+    def calc_timestep(self, oldornew):
+        return self.m.calc_timestep(oldornew)
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    fin = np.isfinite(b) & np.isfinite(a)
+    s = np.abs(b[fin]).max() if fin.any() else 0.0
+    return float(np.abs(a[fin] - b[fin]).max() / s) if s > 0 else 0.0
+
+
+def _drift(a, b) -> dict:
+    """|a - b| over the finite entries relative to the RMS of b: the bulk
+    (rms), the tail (p99) and the worst entry (max)."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    fin = np.isfinite(a) & np.isfinite(b)
+    d = np.abs(a[fin] - b[fin])
+    s = float(np.sqrt(np.mean(b[fin] ** 2))) if fin.any() else 0.0
+    if s == 0.0 or not d.size:
+        return {"rms": 0.0, "p99": 0.0, "max": 0.0}
+    return {"rms": float(np.sqrt(np.mean(d ** 2)) / s), "p99": float(np.quantile(d, 0.99) / s),
+            "max": float(d.max() / s)}
+
+
+def run_cycle(args) -> None:
+    """Config 5: the seismic-cycle step sequence on the C1 geometry (480 k
+    markers), per-regime CUDA graphs.  The plain FP64 form decides the regime
+    and dt sequence; the learned split form replays it (and its own decisions
+    are compared); graph and eager replays are timed; the reference form (no
+    per-marker Newton) is compared with the FP64 oracle over one compressed
+    event."""
+    import torch
+    from velo2cycles_gb300 import abi, cycle, mic, newton, synth
+    steps = args.cycle_steps
+    case = synth.make_case("c1", seed=1)
+    sched = cycle.Schedule()
+    fields = cycle.pulse_fields(case, sched)
+
+    def ctx(**kw):
+        c = case.copy()
+        c.params.update(kw)
+        m = mic.from_case(c)
+        for k in (0, 1):
+            m.cycle_set_velocity(k, *fields[k])
+        return m
+
+    out = {"metric": "seismic-cycle step sequence (config 5)", "unit": "markers/s",
+           "config": {"workload": f"c1 geometry, {case.n} markers, {steps} steps, dt "
+                                  f"{sched.dt_inter:g} s / {sched.dt_co:g} s on the slip rate, "
+                                  f"events every {sched.n_inter} interseismic steps, "
+                                  f"{sched.v_pulse:g} m/s pulse for {sched.slip_budget:g} m"},
+           "stand_in": "prescribed velocities (load field, load + slip pulse) replace the "
+                       "host Stokes solve"}
+    forms = {}
+    seq = None
+    for name, guess, prec in (("plain_fp64", abi.GUESS_PLAIN, abi.NEWTON_FP64),
+                              ("learned_split", abi.GUESS_LEARNED, abi.NEWTON_SPLIT)):
+        m = ctx(newton_guess=guess, newton_precision=prec)
+        if guess == abi.GUESS_LEARNED:
+            train_start_network(m, newton, abi, 1_000_000, seed=3)
+            m.upload_markers(case.marks, case.markt)
+            m.upload_nodes(case.nodes)
+            m.set_params(newton_guess=guess, newton_precision=prec,
+                         **{k: case.params[k] for k in ("timesum", "timestep")})
+            for k in (0, 1):
+                m.cycle_set_velocity(k, *fields[k])
+        st0 = m.status()
+        torch.cuda.synchronize()
+        rec = cycle.run(_GpuCycle(m, True), sched, steps, forced=seq)
+        st1 = m.status()
+        if seq is None:
+            seq = list(zip(rec.regime, rec.dt))
+        drv = cycle.Driver(sched)
+        own = [(0, sched.dt_inter)] + [drv.next(v) for v in rec.maxvel[:-1]]
+        forms[name] = {
+            "seconds": rec.seconds, "markers_per_s": case.n * steps / rec.seconds,
+            "newton_iters_per_marker": (st1["newton_iters"] - st0["newton_iters"]) / (case.n * steps),
+            "newton_nonconverged": st1["newton_nonconv"] - st0["newton_nonconv"],
+            "newton_max_res": st1["newton_max_res"],
+            "coseismic_steps": int(sum(r == 1 for r in rec.regime)),
+            "dt_co_steps": int(sum(d == sched.dt_co for d in rec.dt)),
+            "own_decisions_differ": int(sum(a != b for a, b in zip(own, seq))),
+            "events": int(sum(1 for a, b in zip(rec.regime[1:], rec.regime[:-1]) if a == 1 and b == 0)),
+            "max_slip_rate": max(rec.maxvel),
+            "_slip": m.cycle_slip(), "_mslip": m.cycle_marker_slip(),
+            "_slipv": m.download_markers([abi.MF_SLIPV])[abi.MF_SLIPV],
+        }
+        m.close()
+    p, l = forms["plain_fp64"], forms["learned_split"]
+    # the per-marker Newton writes only the marker slip rate, which the
+    # reference's own path does not read: node fields, stresses and positions
+    # of the two forms are identical (the node slip below checks it), and
+    # their difference is the Newton's
+    out["drift_learned_split_vs_plain_fp64"] = {
+        "node_slip_max": _rel(l["_slip"], p["_slip"]),
+        "marker_accumulated_slip": _drift(l["_mslip"], p["_mslip"]),
+        "marker_slip_rate_last_step": _drift(l["_slipv"], p["_slipv"])}
+    for f in forms.values():
+        for k in ("_slip", "_mslip", "_slipv"):
+            f.pop(k)
+    out["forms"] = forms
+    out["value"] = l["markers_per_s"]
+    # graph against eager launches on the same sequence (learned split)
+    timing = {}
+    for graph in (True, False):
+        m = ctx(newton_guess=abi.GUESS_PLAIN, newton_precision=abi.NEWTON_SPLIT)
+        n = max(1, min(steps - 20, 400))
+        cycle.run(_GpuCycle(m, graph), sched, 20, forced=seq[:20])
+        rec = cycle.run(_GpuCycle(m, graph), sched, n, forced=seq[20:20 + n])
+        timing["graph" if graph else "eager"] = {"steps": n, "seconds": rec.seconds,
+                                                 "markers_per_s": case.n * n / rec.seconds}
+        m.close()
+    out["graph_vs_eager_plain_split"] = timing
+    # the reference form against the FP64 oracle over one compressed event
+    if args.cycle_oracle_steps > 0:
+        import oracle
+        oracle.build()
+        k = args.cycle_oracle_steps
+        s2 = cycle.Schedule(n_inter=k // 3, slip_budget=sched.dt_co * k / 3)
+        ref = _OracleCycle(case, fields)
+        t0 = time.perf_counter()
+        rec_ref = cycle.run(ref, s2, k)
+        t_ref = time.perf_counter() - t0
+        m = ctx(newton_guess=abi.GUESS_OFF)
+        rec = cycle.run(_GpuCycle(m, True), s2, k, forced=list(zip(rec_ref.regime, rec_ref.dt)))
+        mk = m.download_markers([abi.MF_X, abi.MF_XY])
+        wx = np.diff(case.gx)[np.clip(np.searchsorted(case.gx, ref.r.marks[abi.MF_X], "right") - 1,
+                                      0, case.gx.size - 2)]
+        out["drift_reference_form_vs_fp64_oracle"] = {
+            "steps": k, "coseismic_steps": int(sum(r == 1 for r in rec_ref.regime)),
+            "statistic": "|gpu - oracle| over the entries relative to the RMS of the oracle field",
+            "accumulated_slip": _drift(m.cycle_slip()[ref.inner], ref.slip[ref.inner]),
+            "node_sxy": _drift(m.download_nodes([abi.NF_SXY])[abi.NF_SXY], ref.r.nodes[abi.NF_SXY]),
+            "marker_sxy": _drift(mk[abi.MF_XY], ref.r.marks[abi.MF_XY]),
+            "marker_x_cells": float((np.abs(mk[abi.MF_X] - ref.r.marks[abi.MF_X]) / wx).max()),
+            "oracle_seconds": t_ref, "gpu_seconds": rec.seconds}
+        m.close()
+    print(json.dumps(out), flush=True)
+
+
+def run_c2_parity(args) -> None:
+    """Config 2: the reference form (per-marker Newton off) on the C2 grid
+    (non-uniform, 1001 x 401 lines, 6.4 M markers) for K steps with dt
+    log-uniform in [1e-3, 1e10] s, against the reference's own routines
+    (compiled from its sources, all host threads) on the same sequence:
+    per-field error after the last step."""
+    from oracle import bindings as B
+    import oracle
+    from velo2cycles_gb300 import abi, mic, synth
+    oracle.build()
+    if not B.reference_available():
+        print(json.dumps({"c2_parity": "unavailable: the reference routines are not built"}))
+        return
+    k = args.c2_steps
+    case = synth.make_case("c2", seed=2)
+    dts = dt_sequence(k, seed=7)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ref = B.run_reference(case, nthreads=threads, nsteps=k, dts=dts)
+    t_ref = time.perf_counter() - t0
+    c = case.copy()
+    c.params.update(newton_guess=abi.GUESS_OFF)
+    m = mic.from_case(c)
+    ts = float(case.params["timesum"])
+    t0 = time.perf_counter()
+    for dt in dts:
+        m.set_params(timestep=float(dt), timesum=ts)
+        m.step()
+        ts += float(dt)
+    m.synchronize()
+    t_gpu = time.perf_counter() - t0
+    nodes = m.download_nodes()
+    marks = m.download_markers()
+    names_n, names_m = abi.node_field_names(), abi.marker_field_names()
+    per_node, per_mark = {}, {}
+    for f in range(abi.NF_N):
+        if np.array_equal(ref["nodes"][f], case.nodes[f]) and np.array_equal(nodes[f], case.nodes[f]):
+            continue  # not written by the step
+        per_node[names_n[f]] = {"max_rel": _rel(nodes[f], ref["nodes"][f]),
+                                **_drift(nodes[f], ref["nodes"][f])}
+    for f in range(abi.MF_N):
+        if f == abi.MF_SLIPV:
+            continue
+        per_mark[names_m[f]] = {"max_rel": _rel(marks[f], ref["marks"][f]),
+                                **_drift(marks[f], ref["marks"][f])}
+    gx = case.gx
+    ix = np.clip(np.searchsorted(gx, ref["marks"][abi.MF_X], "right") - 1, 0, gx.size - 2)
+    out = {"c2_parity": {"steps": k, "markers": case.n, "reference_threads": threads,
+                         "reference_seconds": t_ref, "gpu_seconds": t_gpu,
+                         "statistics": "max_rel: max |gpu - ref| / max |ref|; rms, p99, max: "
+                                       "relative to the RMS of the reference field",
+                         "marker_x_cells": float((np.abs(marks[abi.MF_X] - ref["marks"][abi.MF_X]) /
+                                                  np.diff(gx)[ix]).max()),
+                         "nodes": per_node, "markers": per_mark}}
+    m.close()
+    print(json.dumps(out), flush=True)
 
 
 def main():
@@ -499,11 +739,25 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end loop")
     ap.add_argument("--forms", default=",".join(f[0] for f in MODES),
                     help="Newton forms to time, comma-separated, learned_split first")
+    ap.add_argument("--cycle", action="store_true",
+                    help="the seismic-cycle step sequence (config 5) instead of the C4 step")
+    ap.add_argument("--cycle-steps", type=int, default=1000)
+    ap.add_argument("--cycle-oracle-steps", type=int, default=60,
+                    help="steps of the reference form against the FP64 oracle (0: skip)")
+    ap.add_argument("--c2-parity", action="store_true",
+                    help="config 2: per-field error against the reference's routines")
+    ap.add_argument("--c2-steps", type=int, default=100)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         run_reference_arm(args, rank)
+    elif args.cycle:
+        if rank == 0:
+            run_cycle(args)
+    elif args.c2_parity:
+        if rank == 0:
+            run_c2_parity(args)
     else:
         run_gpu(args, rank, world)
 

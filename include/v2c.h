@@ -169,6 +169,9 @@ enum {
   V2C_NF_PRS,
   /* interpolate_center2basic outputs (with SXXS, EXXPL, PRS above) */
   V2C_NF_EXXS, V2C_NF_EXXEL,
+  /* sxx - sxxe of the step as recompute_stress_strainrate forms it
+   * (2 nueff exx - Z sxxe, no cancellation); no reference array */
+  V2C_NF_DSXX,
   V2C_NF_N
 };
 
@@ -232,7 +235,10 @@ int v2c_download_cells(v2c_ctx *ctx, int32_t *cell, long n);
  * device's FP32.  The download returns when dst is filled.  The upload is
  * asynchronous on the context stream: from pinned host memory the copy runs
  * later, so src must stay unchanged until a call that synchronises the
- * stream (any download, v2c_synchronize). */
+ * stream (any download, v2c_synchronize).  The velocities VX and VY are also
+ * kept in FP64 on the device (allocated at their first upload, 2 x nodenum
+ * doubles): recompute_stress_strainrate forms strain rates from their
+ * differences, which FP32 storage would round away. */
 int v2c_upload_node_field(v2c_ctx *ctx, int field, const double *src);
 int v2c_download_node_field(v2c_ctx *ctx, int field, double *dst);
 /* count fields at once (fields[k] a V2C_NF_* id, src[k] / dst[k] nodenum
@@ -314,7 +320,8 @@ int v2c_cycle_set_velocity(v2c_ctx *ctx, int regime, const double *vx, const dou
  * interpolate_center2basic_old, compute_before_solve, interpolate_basic2center,
  * recompute_stress_strainrate, interpolate_center2basic, compute_after_solve
  * (no readback), copyarrays, the accumulated slip of every basic node
- * (+= dt * RK_sliprs_final), nodes2markers, moveandrotatemarkers and the next
+ * (+= dt * RK_sliprs_final) and of every marker (+= dt * the Newton's slip
+ * rate), nodes2markers, moveandrotatemarkers and the next
  * counting sort; then timesum += dt.  Asynchronous.
  * use_graph: the step is captured once into a CUDA graph per key (regime,
  * dt, the position buffer holding the current positions, every parameter
@@ -326,6 +333,10 @@ int v2c_cycle_set_velocity(v2c_ctx *ctx, int regime, const double *vx, const dou
 int v2c_cycle_step(v2c_ctx *ctx, int regime, double dt, int use_graph);
 /* accumulated slip of every node (nodenum doubles).  Synchronises. */
 int v2c_cycle_slip(v2c_ctx *ctx, double *out);
+/* accumulated slip of every marker, the per-marker Newton's slip rate times
+ * dt summed over the cycle steps (n doubles, reference numbering; zero
+ * while the Newton is off).  Synchronises. */
+int v2c_cycle_marker_slip(v2c_ctx *ctx, double *out, long n);
 
 int v2c_synchronize(v2c_ctx *ctx);
 int v2c_get_status(v2c_ctx *ctx, v2c_status *st);

@@ -288,9 +288,10 @@ RECOMPUTE_STAGE, COPY_STAGE = 1 << 9, 1 << 10
 
 
 def write_case(path: str, case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0,
-               timestep=None, oldornew=0) -> None:
+               timestep=None, oldornew=0, dts=None) -> None:
     """timestep: v2c_timestep_ctl values as a dict (abi.TIMESTEP_DEFAULTS when
-    None); oldornew: the argument of calc_timestep (stage bit 6)."""
+    None); oldornew: the argument of calc_timestep (stage bit 6); dts: a
+    time step per step (timesum advances after each)."""
     c = case
     nn = c.nodenum
     with open(path, "wb") as f:
@@ -312,6 +313,9 @@ def write_case(path: str, case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=
         ts = dict(abi.TIMESTEP_DEFAULTS, **(timestep or {}))
         np.array([ts["maxtmstep"], ts["dtfactor"], ts["tcnvp"], ts["tcd"], ts["tcphih"],
                   float(oldornew)], dtype=np.float64).tofile(f)
+        if dts is not None:
+            np.array([len(dts)], dtype=np.int64).tofile(f)
+            np.ascontiguousarray(dts, dtype=np.float64).tofile(f)
 
 
 def read_result(path: str, nodenum: int):
@@ -330,7 +334,7 @@ def read_result(path: str, nodenum: int):
 
 
 def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeout=3600,
-                  timestep=None, oldornew=0):
+                  timestep=None, oldornew=0, dts=None):
     """Run the reference routines on `case`; returns the arrays after the
     stages plus per-stage seconds summed over the timed steps."""
     if not reference_available():
@@ -339,7 +343,7 @@ def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeo
         raise RuntimeError("reference oracle not built (reference sources unavailable)")
     with tempfile.TemporaryDirectory() as d:
         cp, rp = os.path.join(d, "case.bin"), os.path.join(d, "res.bin")
-        write_case(cp, case, stages, nthreads, nsteps, warmup, timestep, oldornew)
+        write_case(cp, case, stages, nthreads, nsteps, warmup, timestep, oldornew, dts)
         env = dict(os.environ, OMP_NUM_THREADS=str(max(1, nthreads)))
         r = subprocess.run([reference_path(), cp, rp], env=env, capture_output=True,
                            timeout=timeout)

@@ -39,7 +39,7 @@ if [ -d "$REF/src" ]; then
     -e 's/^#define MAXVAL .*/#define MAXVAL  8000000/' \
     -e 's/^#define MAXXLN .*/#define MAXXLN  1100/' \
     -e 's/^#define MAXYLN .*/#define MAXYLN  420/' \
-    -e 's/^#define MAXMRK .*/#define MAXMRK  2100000/' \
+    -e 's/^#define MAXMRK .*/#define MAXMRK  6500001/' \
     "$OUT/src/headevps.c"
 fi
 

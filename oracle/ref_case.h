@@ -43,6 +43,8 @@ typedef struct {
   int nthreads, stages, nsteps, warmup;
   double *scratch;
   double ts[6];            /* maxtmstep, dtfactor, tcnvp, tcd, tcphih, oldornew */
+  long ndts;               /* per-step time steps (optional trailer), 0 if none */
+  double *dts;
   v2c_timestep_info info;  /* calc_timestep results (stage bit 6) */
   long ts_rc;              /* 0, or 1 when chi == 0 stopped it */
 } ref_case;
@@ -79,9 +81,10 @@ static int ref_load_case(const char *path, ref_case *C) {
       memcpy(rock_row(r), rt + (long)r * V2C_MAXTMR, sizeof(double) * V2C_MAXTMR);
     }
   }
-  for (int k = 0; k < V2C_NF_N; k++) rd(node_array(k), sizeof(double), nn, f);
-  double *scratch = (double *)malloc(sizeof(double) * (n + 1));
+  double *scratch = (double *)malloc(sizeof(double) * ((n > nn ? n : nn) + 1));
   C->scratch = scratch;
+  /* fields the reference has no array for are read into scratch */
+  for (int k = 0; k < V2C_NF_N; k++) rd(node_array(k) ? node_array(k) : scratch, sizeof(double), nn, f);
   for (int k = 0; k < V2C_MF_N; k++) {
     double *dst = marker_array(k);
     rd(dst ? dst : scratch, sizeof(double), n, f);
@@ -106,6 +109,15 @@ static int ref_load_case(const char *path, ref_case *C) {
     for (int k = 0; k < 4; k++) bondv[i][k] = bv[i * 4 + k];
   bondnum = nb;
   rd(C->ts, sizeof(double), 6, f);
+  /* optional trailer: int64 ndts, double dts[ndts] */
+  C->ndts = 0;
+  C->dts = NULL;
+  int64_t nd = 0;
+  if (fread(&nd, sizeof(int64_t), 1, f) == 1 && nd > 0) {
+    C->dts = (double *)malloc(sizeof(double) * nd);
+    rd(C->dts, sizeof(double), nd, f);
+    C->ndts = nd;
+  }
   memset(&C->info, 0, sizeof(C->info));
   C->ts_rc = 0;
   fclose(f);
@@ -123,7 +135,13 @@ static int ref_write_result(const char *path, const ref_case *C, const double *s
   wr("V2CRES01", 1, 8, o);
   int64_t nout = marknum;
   wr(&nout, sizeof(int64_t), 1, o);
-  for (int k = 0; k < V2C_NF_N; k++) wr(node_array(k), sizeof(double), nn, o);
+  for (int k = 0; k < V2C_NF_N; k++) {
+    if (node_array(k)) wr(node_array(k), sizeof(double), nn, o);
+    else {
+      memset(scratch, 0, sizeof(double) * nn);
+      wr(scratch, sizeof(double), nn, o);
+    }
+  }
   for (int k = 0; k < V2C_MF_N; k++) {
     double *src = marker_array(k);
     if (src) wr(src, sizeof(double), nout, o);

@@ -21,6 +21,7 @@
  *   double gx[xnumx], gy[ynumy], rt[V2C_RT_N][V2C_MAXTMR]
  *   double node[V2C_NF_N][nodenum], mark[V2C_MF_N][n]; int8 markt[n]
  *   int64 bondm[nodenum*4], bondn[bondnum*3]; double bondv[bondnum*4]
+ *   double ts[6]; optional: int64 ndts, double dts[ndts] (per-step dt)
  * Result file:
  *   char magic[8] = "V2CRES01"; int64 n
  *   double node[V2C_NF_N][nodenum], mark[V2C_MF_N][n]; int8 markt[n]
@@ -96,6 +97,9 @@ int main(int argc, char **argv) {
   for (int step = 0; step < warmup + nsteps; step++) {
     double t0;
     int timed = step >= warmup;
+    /* a per-step time step sequence: the step runs with dts[step] and
+     * timesum advances after it, as in the reference's main loop */
+    if (step < C.ndts) timestep = C.dts[step];
 #define STAGE(bit, idx, call)                               \
   if (stages & (1 << bit)) {                                \
     t0 = omp_get_wtime();                                   \
@@ -121,6 +125,7 @@ int main(int argc, char **argv) {
       if (timed) secs[6] += omp_get_wtime() - t0;
     }
 #undef STAGE
+    if (step < C.ndts) timesum += timestep;
   }
 
   return ref_write_result(argv[2], &C, secs, deltas);

@@ -46,7 +46,8 @@
 static double *save_arrays(long nn, long n) {
   double *s = (double *)malloc(sizeof(double) * (V2C_NF_N * nn + V2C_MF_N * (n + 1)) + n + 1);
   double *p = s;
-  for (int k = 0; k < V2C_NF_N; k++, p += nn) memcpy(p, node_array(k), sizeof(double) * nn);
+  for (int k = 0; k < V2C_NF_N; k++, p += nn)
+    if (node_array(k)) memcpy(p, node_array(k), sizeof(double) * nn);
   for (int k = 0; k < V2C_MF_N; k++, p += n + 1)
     if (marker_array(k)) memcpy(p, marker_array(k), sizeof(double) * (n + 1));
   memcpy(p, markt, n + 1);
@@ -55,7 +56,8 @@ static double *save_arrays(long nn, long n) {
 
 static void restore_arrays(const double *s, long nn, long n) {
   const double *p = s;
-  for (int k = 0; k < V2C_NF_N; k++, p += nn) memcpy(node_array(k), p, sizeof(double) * nn);
+  for (int k = 0; k < V2C_NF_N; k++, p += nn)
+    if (node_array(k)) memcpy(node_array(k), p, sizeof(double) * nn);
   for (int k = 0; k < V2C_MF_N; k++, p += n + 1)
     if (marker_array(k)) memcpy(marker_array(k), p, sizeof(double) * (n + 1));
   memcpy(markt, p, n + 1);

@@ -23,6 +23,9 @@ C2B_OUT = [abi.NF_EXXES, abi.NF_SXXES, abi.NF_SPPES]
 # interpolate_basic2center, interpolate_center2basic (interpolation.c:1600-1685);
 # nd, exxpl and exxel carry the viscosity fields' error
 B2C_C2B_OUT = [abi.NF_ND, abi.NF_EXXS, abi.NF_EXXPL, abi.NF_SXXS, abi.NF_PRS, abi.NF_EXXEL]
+# recompute_stress_strainrate, copyarrays (momentum_continuity_iterate.c:214-281)
+RECOMPUTE_OUT = [abi.NF_EXX, abi.NF_SXX, abi.NF_EXY, abi.NF_ESP, abi.NF_SXY]
+COPY_OUT = [abi.NF_SLIPRS, abi.NF_RK_SLIPRS_FINAL, abi.NF_RK_PHIDTS_FINAL]
 RSF_OUT = [abi.NF_PES, abi.NF_PHIS_IT, abi.NF_SYIELDS, abi.NF_NUVP_IT, abi.NF_SLIPRS, abi.NF_NU,
            abi.NF_RK_SLIPRS_SOLVED, abi.NF_RK_PHIDTS_SOLVED, abi.NF_RK_DELTAS]
 N2M_OUT = [abi.NF_PHISUM, abi.NF_WTPHISUM, abi.NF_SXYSUM, abi.NF_EXYSUM, abi.NF_ESUM,

@@ -97,10 +97,25 @@ def test_graph_replay_matches_eager(case):
     ma.close(); mb.close()
 
 
+def _drift(a, b):
+    """(rms, p99, max) of |a - b| over the finite entries, relative to the
+    RMS of b: the bulk of the field, its tail and its worst entry."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    fin = np.isfinite(a) & np.isfinite(b)
+    assert np.array_equal(np.isfinite(a), np.isfinite(b))
+    d = np.abs(a[fin] - b[fin])
+    s = np.sqrt(np.mean(b[fin] ** 2))
+    return np.sqrt(np.mean(d ** 2)) / s, np.quantile(d, 0.99) / s, d.max() / s
+
+
 def test_reference_form_tracks_oracle(case):
     """Per-marker Newton off (the reference's own algorithm): after an
     interseismic stretch, an event and the relaxation steps, the GPU state
-    stays within FP32 drift of the FP64 oracle."""
+    stays within FP32 drift of the FP64 oracle, in the bulk and the tail of
+    every field.  (A 1e-7 perturbation of the FP64 run's marker stresses
+    moves these statistics by about 1e-7 only.)  Measured: RMS 6e-8 (state)
+    to 1.6e-5 (accumulated slip), tails below 1.5e-5 except the slip
+    (4e-6 p99, 5e-4 max at the nodes of the pulse's edge)."""
     fields = cycle.pulse_fields(case, SCHED)
     m = _gpu(case, fields, newton_guess=abi.GUESS_OFF)
     ref = OracleStepper(case, fields)
@@ -111,36 +126,43 @@ def test_reference_form_tracks_oracle(case):
     drv = cycle.Driver(SCHED)
     own = [(0, SCHED.dt_inter)] + [drv.next(v) for v in rec.maxvel[:-1]]
     assert own == list(zip(rec_ref.regime, rec_ref.dt))
-    slip = m.cycle_slip()
-    e_slip = rel_err(slip[ref.inner], ref.slip[ref.inner])
-    nodes = m.download_nodes([abi.NF_SXY, abi.NF_PHIS])
-    e_sxy = rel_err(nodes[abi.NF_SXY], ref.r.nodes[abi.NF_SXY])
-    e_phi = rel_err(nodes[abi.NF_PHIS], ref.r.nodes[abi.NF_PHIS])
+    nodes = m.download_nodes([abi.NF_SXY, abi.NF_PHIS, abi.NF_SYIELDS, abi.NF_RK_SLIPRS_FINAL])
     mk = m.download_markers([abi.MF_X, abi.MF_XY])
+    got = {"slip": _drift(m.cycle_slip()[ref.inner], ref.slip[ref.inner]),
+           "sxy": _drift(nodes[abi.NF_SXY], ref.r.nodes[abi.NF_SXY]),
+           "phis": _drift(nodes[abi.NF_PHIS], ref.r.nodes[abi.NF_PHIS]),
+           "syields": _drift(nodes[abi.NF_SYIELDS], ref.r.nodes[abi.NF_SYIELDS]),
+           "slip_rate": _drift(nodes[abi.NF_RK_SLIPRS_FINAL], ref.r.nodes[abi.NF_RK_SLIPRS_FINAL]),
+           "marker_sxy": _drift(mk[abi.MF_XY], ref.r.marks[abi.MF_XY])}
+    for k, (r, p, x) in got.items():
+        print(f"drift vs oracle after {len(rec.dt)} steps, {k}: rms {r:.1e} p99 {p:.1e} max {x:.1e}")
+    bad = {k: v for k, v in got.items() if not (v[0] <= 1e-4 and v[1] <= 1e-4 and v[2] <= 5e-3)}
+    assert not bad, bad
     wx = np.diff(case.gx)[nxsearch_np(case.gx, ref.r.marks[abi.MF_X])]
-    e_x = (np.abs(mk[abi.MF_X] - ref.r.marks[abi.MF_X]) / wx).max()
-    e_mxy = rel_err(mk[abi.MF_XY], ref.r.marks[abi.MF_XY])
-    print(f"drift vs oracle after {len(rec.dt)} steps: slip {e_slip:.2e} sxy {e_sxy:.2e} "
-          f"phis {e_phi:.2e} x {e_x:.2e} cells, marker sxy {e_mxy:.2e}")
-    assert e_slip <= 1e-4 and e_sxy <= 1e-4 and e_phi <= 1e-4
-    assert e_x <= 1e-5 and e_mxy <= 1e-4
+    assert (np.abs(mk[abi.MF_X] - ref.r.marks[abi.MF_X]) / wx).max() <= 1e-5
     m.close()
 
 
 def test_learned_split_tracks_plain_fp64(case):
     """The learned-start split-precision form against the plain FP64 form on
-    the same regime sequence: the Newton converges to the same residual, so
-    accumulated slip and stresses agree to FP32 drift."""
+    the same regime sequence.  The per-marker Newton writes only the marker
+    slip rate, which the reference's path does not read, so node fields are
+    identical; the marker slip accumulated from the Newton's rates agrees to
+    the converged residual (1e-10) and the FP32 storage of the rate."""
     fields = cycle.pulse_fields(case, SCHED)
     mp = _gpu(case, fields, newton_guess=abi.GUESS_PLAIN, newton_precision=abi.NEWTON_FP64)
     rec = cycle.run(_G(mp, True), SCHED, 12)
     ml = _gpu(case, fields, newton_guess=abi.GUESS_LEARNED, newton_precision=abi.NEWTON_SPLIT)
     newton.load(ml, newton.random_params(5))  # any start: the Newton judges it
     cycle.run(_G(ml, True), SCHED, 12, forced=list(zip(rec.regime, rec.dt)))
-    sp, sl = mp.cycle_slip(), ml.cycle_slip()
-    assert rel_err(sl, sp) <= 1e-4
+    assert np.array_equal(mp.cycle_slip(), ml.cycle_slip())
     a, b = mp.download_nodes([abi.NF_SXY]), ml.download_nodes([abi.NF_SXY])
-    assert rel_err(b[abi.NF_SXY], a[abi.NF_SXY]) <= 1e-4
+    assert np.array_equal(a[abi.NF_SXY], b[abi.NF_SXY])
+    sp, sl = mp.cycle_marker_slip(), ml.cycle_marker_slip()
+    assert np.abs(sp).max() > 0
+    r, p, x = _drift(sl, sp)
+    print(f"marker slip, learned split vs plain FP64: rms {r:.1e} p99 {p:.1e} max {x:.1e}")
+    assert r <= 1e-5 and p <= 1e-5 and x <= 1e-3
     st = ml.status()
     assert st["newton_nonconv"] == 0 and st["newton_max_res"] <= 1e-10
     mp.close(); ml.close()

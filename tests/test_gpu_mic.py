@@ -14,7 +14,7 @@ import pytest
 import oracle
 from velo2cycles_gb300 import abi, mic, synth
 
-from .parity import (B2C_C2B_OUT, C2B_OUT, M2N_OUT, MOVE_MARK, N2M_MARK, N2M_OUT, RSF_OUT, VISCOUS,
+from .parity import (B2C_C2B_OUT, C2B_OUT, COPY_OUT, M2N_OUT, RECOMPUTE_OUT, MOVE_MARK, N2M_MARK, N2M_OUT, RSF_OUT, VISCOUS,
                      node_errors, marker_errors, nxsearch_np)
 
 pytestmark = pytest.mark.gpu
@@ -85,6 +85,24 @@ def test_basic2center_center2basic(case):
     m.interpolate_basic2center(); ref.basic2center()
     m.interpolate_center2basic(dt); ref.center2basic(dt)
     _check_nodes(node_errors(m.download_nodes(B2C_C2B_OUT), ref.nodes, B2C_C2B_OUT))
+    m.close()
+
+
+def test_picard_pass_node_routines(case):
+    """One Picard pass of node routines in the reference's order with the
+    stress recompute from the given velocities and the final-rate copy."""
+    dt = case.params["timestep"]
+    m = mic.from_case(case)
+    ref = oracle.Restatement(case.copy())
+    m.marker2nodes(); ref.marker2nodes()
+    m.compute_before_solve(dt, 0); ref.compute_before_solve(dt, 0)
+    m.interpolate_basic2center(); ref.basic2center()
+    m.recompute_stress_strainrate(dt); ref.recompute_stress(dt)
+    _check_nodes(node_errors(m.download_nodes(RECOMPUTE_OUT), ref.nodes, RECOMPUTE_OUT))
+    m.interpolate_center2basic(dt); ref.center2basic(dt)
+    m.compute_after_solve(dt, 0); ref.compute_after_solve(dt, 0)
+    m.copyarrays(); ref.copyarrays()
+    _check_nodes(node_errors(m.download_nodes(COPY_OUT + RSF_OUT), ref.nodes, COPY_OUT + RSF_OUT))
     m.close()
 
 

@@ -139,6 +139,23 @@ def test_picard_node_sequence_bit_exact_vs_reference(name, seed):
                           r.nodes[abi.NF_RK_SLIPRS_SOLVED][inner], equal_nan=True)
 
 
+@needs_ref
+def test_multi_step_dt_sequence_bit_exact_vs_reference():
+    """Three full steps with a different dt each (the harness's per-step dt
+    trailer; timesum advances after each step as in the reference's main
+    loop), restatement against the compiled reference."""
+    c = synth.make_case("small", 12)
+    dts = [1e9, 3e-2, 2e7]
+    ref = B.run_reference(c, nthreads=1, nsteps=3, dts=dts)
+    r = oracle.Restatement(c.copy(), phantom=True)
+    ts = float(c.params["timesum"])
+    for dt in dts:
+        r.set_params(timestep=dt, timesum=ts)
+        r.step()
+        ts += dt
+    assert not _compare(r, ref["nodes"], ref["marks"])
+
+
 def test_nxsearch_ties_and_clamps():
     g = np.array([0.0, 1.0, 2.0, 4.0, 8.0])
     assert B.nxsearch(g, 2.0) == 2          # on a line: ties go left of the upper limit

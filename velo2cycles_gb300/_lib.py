@@ -46,6 +46,7 @@ _SIGS = {
     "v2c_cycle_set_velocity": [c_ctx, ctypes.c_int, c_dp, c_dp],
     "v2c_cycle_step": [c_ctx, ctypes.c_int, ctypes.c_double, ctypes.c_int],
     "v2c_cycle_slip": [c_ctx, c_dp],
+    "v2c_cycle_marker_slip": [c_ctx, c_dp, ctypes.c_long],
     "v2c_upload_node_fields": [c_ctx, ctypes.c_int, P(ctypes.c_int), P(c_dp)],
     "v2c_download_node_fields": [c_ctx, ctypes.c_int, P(ctypes.c_int), P(c_dp)],
     "v2c_marker2nodes": [c_ctx],

@@ -122,13 +122,16 @@ static int v2c_bind_setup(void) {
 }
 
 static int v2c_bind_nodes_up(void) {
-  int fields[V2C_NF_N];
+  /* every node array the reference has (fields it lacks stay as they are) */
+  int fields[V2C_NF_N], nf = 0;
   const double *src[V2C_NF_N];
   for (int k = 0; k < V2C_NF_N; k++) {
-    fields[k] = k;
-    src[k] = v2c_bind_node_array(k);
+    const double *a = v2c_bind_node_array(k);
+    if (!a) continue;
+    fields[nf] = k;
+    src[nf++] = a;
   }
-  return v2c_bind_ok(v2c_upload_node_fields(v2c_bind_ctx, V2C_NF_N, fields, src),
+  return v2c_bind_ok(v2c_upload_node_fields(v2c_bind_ctx, nf, fields, src),
                      "v2c_upload_node_fields");
 }
 

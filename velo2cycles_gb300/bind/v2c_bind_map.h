@@ -7,7 +7,7 @@
  *
  * Include it inside the reference's translation unit, after headevps.c and
  * input_RSF.c, so that the globals are in scope.  Fields the reference does
- * not have (V2C_MF_SLIPV) map to NULL.
+ * not have (V2C_MF_SLIPV, V2C_NF_DSXX) map to NULL.
  */
 #ifndef V2C_BIND_MAP_H
 #define V2C_BIND_MAP_H

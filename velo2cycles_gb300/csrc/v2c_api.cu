@@ -65,6 +65,11 @@ struct v2c_ctx {
   long bondnum = 0;
   bool have_bonds = false;
   int bc_built_compressible = -1, bc_built_tempmod = -1;
+  bool dsxx_valid = false;  // DSXX holds sxx - sxxe of the current node fields
+  // FP64 node velocities (vx, then vy) for the strain rates, kept from the
+  // uploads; valid per component while it matches the FP32 field
+  double *d_vel64 = nullptr;
+  bool vel64_ok[2] = {false, false};
   int bc_n = 0;
   void *bc_mem = nullptr;
   BcRows bc{};
@@ -87,7 +92,9 @@ struct v2c_ctx {
   // seismic-cycle workload: per-regime velocity fields, accumulated slip,
   // captured step graphs
   float *d_cyc_v[2] = {nullptr, nullptr};  // [regime]: vx then vy, 2 nn floats
+  double *d_cyc_v64[2] = {nullptr, nullptr};  // the same in FP64
   double *d_slip = nullptr;                 // accumulated slip per node
+  double *d_mslip = nullptr;                // accumulated slip per marker (array order)
   struct CycleGraph {
     int regime;
     double dt;
@@ -305,7 +312,11 @@ extern "C" int v2c_destroy(v2c_ctx *ctx) {
   ctx->graphs.clear();
   for (float *v : ctx->d_cyc_v)
     if (v) cudaFree(v);
+  for (double *v : ctx->d_cyc_v64)
+    if (v) cudaFree(v);
+  if (ctx->d_vel64) cudaFree(ctx->d_vel64);
   if (ctx->d_slip) cudaFree(ctx->d_slip);
+  if (ctx->d_mslip) cudaFree(ctx->d_mslip);
   void *ptrs[] = {ctx->d_gx, ctx->d_gy, ctx->d_wx, ctx->d_wy, ctx->d_gxf, ctx->d_gyf,
                   ctx->d_rock, ctx->d_node, ctx->d_node64, ctx->d_sticky, ctx->d_quad, ctx->d_list_n, ctx->d_ts,
                   ctx->d_stat, ctx->d_red, ctx->d_nstage,
@@ -660,10 +671,23 @@ extern "C" int v2c_download_cells(v2c_ctx *ctx, int32_t *cell, long n) {
 // ============================================================== node arrays
 // node fields live in FP32 on the device; they are converted on the way in
 // and out (the conversion kernels run on the context stream)
+// keep the FP64 copy of an uploaded velocity field (staged at dev64)
+static int keep_vel64(v2c_ctx *ctx, int field, const double *dev64) {
+  if (field != V2C_NF_VX && field != V2C_NF_VY) return V2C_OK;
+  const int k = field == V2C_NF_VX ? 0 : 1;
+  if (!ctx->d_vel64) CK(cudaMalloc(&ctx->d_vel64, sizeof(double) * 2 * ctx->nn));
+  CK(cudaMemcpyAsync(ctx->d_vel64 + k * ctx->nn, dev64, sizeof(double) * ctx->nn,
+                     cudaMemcpyDeviceToDevice, ctx->stream));
+  ctx->vel64_ok[k] = true;
+  return V2C_OK;
+}
+
 extern "C" int v2c_upload_node_field(v2c_ctx *ctx, int field, const double *src) {
   if (!ctx || !src || field < 0 || field >= V2C_NF_N) return V2C_ERR_ARG;
+  ctx->dsxx_valid = false;
   CK(cudaMemcpyAsync(ctx->d_node64, src, sizeof(double) * ctx->nn, cudaMemcpyHostToDevice,
                      ctx->stream));
+  if (int rc = keep_vel64(ctx, field, ctx->d_node64)) return fail(ctx, rc);
   launch_node_to_f32(ctx->d_node64, ctx->d_node + (long)field * ctx->nn, ctx->nn, ctx->stream);
   ctx->launches += 1;
   CK(cudaGetLastError());
@@ -703,6 +727,7 @@ extern "C" int v2c_upload_node_fields(v2c_ctx *ctx, int count, const int *fields
   if (!ctx) return V2C_ERR_ARG;
   if (!node_field_list_ok(count, fields, (const void *const *)src)) return fail(ctx, V2C_ERR_ARG);
   if (count == 0) return V2C_OK;
+  ctx->dsxx_valid = false;
   int rc = grow_node_stage(ctx, count);
   if (rc) return fail(ctx, rc);
   for (int k = 0; k < count; k++)
@@ -710,6 +735,8 @@ extern "C" int v2c_upload_node_fields(v2c_ctx *ctx, int count, const int *fields
                        cudaMemcpyHostToDevice, ctx->stream));
   launch_fields_to_f32(ctx->d_nstage, ctx->nn, fields, count, ctx->d_node, ctx->stream);
   ctx->launches += 1;
+  for (int k = 0; k < count; k++)
+    if (int rc2 = keep_vel64(ctx, fields[k], ctx->d_nstage + (long)k * ctx->nn)) return fail(ctx, rc2);
   CK(cudaGetLastError());
   return V2C_OK;
 }
@@ -774,6 +801,7 @@ extern "C" int v2c_marker2nodes(v2c_ctx *ctx) {
   a.gyf = ctx->d_gyf;
   a.TX = pick_tx(ctx);
   CK(cudaMemsetAsync(ctx->d_sticky, 0, sizeof(uint32_t) * ctx->nn, st));
+  ctx->dsxx_valid = false;  // the scatter writes sxxe
   {
     PhysArgs ph;
     ph.g = a.g; ph.N = a.N; ph.m = a.m; ph.R = a.R; ph.S = a.S; ph.n = ctx->n;
@@ -852,7 +880,7 @@ extern "C" int v2c_interpolate_center2basic(v2c_ctx *ctx, double dt) {
   if (!ctx->have_grid) return fail(ctx, V2C_ERR_STATE);
   {
     Prof pr(ctx, V2C_PROF_B2C);
-    launch_c2b(make_grid(ctx), make_nodes(ctx), (float)dt, ctx->stream);
+    launch_c2b(make_grid(ctx), make_nodes(ctx), (float)dt, ctx->dsxx_valid ? 1 : 0, ctx->stream);
   }
   ctx->launches += 1;
   CK(cudaGetLastError());
@@ -864,9 +892,12 @@ extern "C" int v2c_recompute_stress_strainrate(v2c_ctx *ctx, double dt) {
   if (!ctx->have_grid) return fail(ctx, V2C_ERR_STATE);
   {
     Prof pr(ctx, V2C_PROF_B2C);
+    const bool v64 = ctx->d_vel64 && ctx->vel64_ok[0] && ctx->vel64_ok[1];
     launch_recompute(make_grid(ctx), make_nodes(ctx), make_scal(ctx->p, ctx->h_rt), (float)dt,
+                     v64 ? ctx->d_vel64 : nullptr, v64 ? ctx->d_vel64 + ctx->nn : nullptr,
                      ctx->stream);
   }
+  ctx->dsxx_valid = true;
   ctx->launches += 1;
   CK(cudaGetLastError());
   return V2C_OK;
@@ -994,14 +1025,21 @@ extern "C" int v2c_cycle_set_velocity(v2c_ctx *ctx, int regime, const double *vx
   if (!ctx->have_grid) return fail(ctx, V2C_ERR_STATE);
   const long nn = ctx->nn;
   if (!ctx->d_cyc_v[regime]) CK(cudaMalloc(&ctx->d_cyc_v[regime], sizeof(float) * 2 * nn));
+  if (!ctx->d_cyc_v64[regime]) CK(cudaMalloc(&ctx->d_cyc_v64[regime], sizeof(double) * 2 * nn));
+  if (!ctx->d_vel64) CK(cudaMalloc(&ctx->d_vel64, sizeof(double) * 2 * nn));
   if (!ctx->d_slip) CK(cudaMalloc(&ctx->d_slip, sizeof(double) * nn));
+  if (!ctx->d_mslip && ctx->cap > 0) CK(cudaMalloc(&ctx->d_mslip, sizeof(double) * ctx->cap));
   cudaStream_t st = ctx->stream;
   const double *src[2] = {vx, vy};
   for (int k = 0; k < 2; k++) {
-    CK(cudaMemcpyAsync(ctx->d_node64, src[k], sizeof(double) * nn, cudaMemcpyHostToDevice, st));
-    launch_node_to_f32(ctx->d_node64, ctx->d_cyc_v[regime] + k * nn, nn, st);
+    CK(cudaMemcpyAsync(ctx->d_cyc_v64[regime] + k * nn, src[k], sizeof(double) * nn,
+                       cudaMemcpyHostToDevice, st));
+    launch_node_to_f32(ctx->d_cyc_v64[regime] + k * nn, ctx->d_cyc_v[regime] + k * nn, nn, st);
   }
-  if (regime == 0) CK(cudaMemsetAsync(ctx->d_slip, 0, sizeof(double) * nn, st));
+  if (regime == 0) {
+    CK(cudaMemsetAsync(ctx->d_slip, 0, sizeof(double) * nn, st));
+    if (ctx->d_mslip) CK(cudaMemsetAsync(ctx->d_mslip, 0, sizeof(double) * ctx->cap, st));
+  }
   CK(cudaStreamSynchronize(st));
   return V2C_OK;
 }
@@ -1014,6 +1052,9 @@ static int cycle_enqueue(v2c_ctx *ctx, int regime, double dt) {
                      sizeof(float) * nn, cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(ctx->d_node + (long)V2C_NF_VY * nn, ctx->d_cyc_v[regime] + nn,
                      sizeof(float) * nn, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_vel64, ctx->d_cyc_v64[regime], sizeof(double) * 2 * nn,
+                     cudaMemcpyDeviceToDevice, st));
+  ctx->vel64_ok[0] = ctx->vel64_ok[1] = true;
   int rc;
   if ((rc = v2c_marker2nodes(ctx))) return rc;
   if ((rc = v2c_center2basic_old(ctx))) return rc;
@@ -1025,6 +1066,10 @@ static int cycle_enqueue(v2c_ctx *ctx, int regime, double dt) {
   if ((rc = v2c_copyarrays(ctx))) return rc;
   launch_slip_acc(make_grid(ctx), make_nodes(ctx), dt, ctx->d_slip, st);
   ctx->launches += 1;
+  if (ctx->p.newton_guess != V2C_GUESS_OFF && ctx->n > 0) {
+    launch_marker_slip_acc(ctx->m.slipv, ctx->n, dt, ctx->d_mslip, st);
+    ctx->launches += 1;
+  }
   return n2m_move(ctx, 1, 1);
 }
 
@@ -1098,6 +1143,16 @@ extern "C" int v2c_cycle_step(v2c_ctx *ctx, int regime, double dt, int use_graph
   ctx->graphs.push_back({regime, dt, pos, pk, flags, exec, ctx->launches - l0});
   CK(cudaGraphLaunch(exec, st));
   ctx->p.timesum += dt;
+  return V2C_OK;
+}
+
+extern "C" int v2c_cycle_marker_slip(v2c_ctx *ctx, double *out, long n) {
+  if (!ctx || !out || n != ctx->n) return V2C_ERR_ARG;
+  if (!ctx->d_mslip) return fail(ctx, V2C_ERR_STATE);
+  launch_unpermute_f64(ctx->d_mslip, ctx->m.id, ctx->d_stage64, n, ctx->stream);
+  CK(cudaMemcpyAsync(out, ctx->d_stage64, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   return V2C_OK;
 }
 

@@ -92,10 +92,15 @@ void launch_fields_to_f32(const double *stage, long nn, const int *fields, int c
                           cudaStream_t st);
 
 void launch_c2b_old(const Grid &g, const Nodes &N, cudaStream_t st);
-void launch_c2b(const Grid &g, const Nodes &N, float dt, cudaStream_t st);
+void launch_c2b(const Grid &g, const Nodes &N, float dt, int use_dsxx, cudaStream_t st);
 void launch_b2c(const Grid &g, const Nodes &N, unsigned long long *stat, cudaStream_t st);
-void launch_recompute(const Grid &g, const Nodes &N, const Scal &S, float dt, cudaStream_t st);
+// vx64, vy64: FP64 node velocities for the strain rates (nullptr: the FP32 fields)
+void launch_recompute(const Grid &g, const Nodes &N, const Scal &S, float dt, const double *vx64,
+                      const double *vy64, cudaStream_t st);
 void launch_copyarrays(const Grid &g, const Nodes &N, cudaStream_t st);
+// accumulated slip of every marker: acc[i] += dt * slipv[i]
+void launch_marker_slip_acc(const float *slipv, long n, double dt, double *acc, cudaStream_t st);
+void launch_unpermute_f64(const double *src, const int32_t *id, double *out, long n, cudaStream_t st);
 void launch_slip_acc(const Grid &g, const Nodes &N, double dt, double *acc, cudaStream_t st);
 void launch_before_solve(const Grid &g, const Nodes &N, const Scal &S, double dt, int rk,
                          unsigned long long *stat, cudaStream_t st);

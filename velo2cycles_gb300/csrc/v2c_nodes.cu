@@ -55,8 +55,10 @@ __device__ __forceinline__ float new_state(float ph, float V, float dt, float L,
 // interpolate_center2basic (interpolation.c:1600-1637): means of the four
 // pressure nodes around each interior basic node; the plastic and elastic
 // strain rates use the reference's per-node terms (IEEE division: a node no
-// marker reached has gd = 0 and gives inf as in the reference)
-__global__ void k_c2b(Grid g, Nodes N, float dt) {
+// marker reached has gd = 0 and gives inf as in the reference).  use_dsxx:
+// sxx - sxxe is taken from DSXX, which recompute_stress_strainrate wrote
+// for the current sxx and sxxe (the FP32 difference cancels at small dt)
+__global__ void k_c2b(Grid g, Nodes N, float dt, int use_dsxx) {
   long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (m3 >= g.nn) return;
   const long yn = g.yn;
@@ -64,6 +66,7 @@ __global__ void k_c2b(Grid g, Nodes N, float dt) {
   if (!(m1 >= 1 && m2 >= 1 && m1 < g.xn - 1 && m2 < g.yn - 1)) return;
   const float *exx = N.f(V2C_NF_EXX), *sxx = N.f(V2C_NF_SXX), *sxxe = N.f(V2C_NF_SXXE);
   const float *gd = N.f(V2C_NF_GD), *nd = N.f(V2C_NF_ND_M2C), *pr = N.f(V2C_NF_PR);
+  const float *dsxx = N.f(V2C_NF_DSXX);
   float se = 0.f, ss = 0.f, sp = 0.f, spl = 0.f, sel = 0.f;
   const long k[4] = {m3, m3 + 1, m3 + yn, m3 + yn + 1};
 #pragma unroll
@@ -71,7 +74,7 @@ __global__ void k_c2b(Grid g, Nodes N, float dt) {
     const long i = k[q];
     const float e = exx[i], s = sxx[i], s0 = sxxe[i], G = gd[i];
     se += e; ss += s; sp += pr[i];
-    spl += e - (s - s0) / (2.f * G * dt) - s / (2.f * nd[i]);
+    spl += e - (use_dsxx ? dsxx[i] : s - s0) / (2.f * G * dt) - s / (2.f * nd[i]);
     sel += 2.f * G * dt * e + s0;
   }
   N.f(V2C_NF_EXXS)[m3] = 0.25f * se;
@@ -130,7 +133,8 @@ __device__ __forceinline__ float nueff_of(float nvp, float ggeff, float dt, floa
 // strain rates from the node velocities, visco-elastic stresses from the
 // node viscosities and the previous elastic stresses.  Line spacings are
 // sums of the FP32 cell widths.
-__global__ void k_recompute(Grid g, Nodes N, float dt, float nubeg) {
+__global__ void k_recompute(Grid g, Nodes N, float dt, float nubeg, const double *vx64,
+                            const double *vy64) {
   long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (m3 >= g.nn) return;
   const long yn = g.yn;
@@ -140,14 +144,26 @@ __global__ void k_recompute(Grid g, Nodes N, float dt, float nubeg) {
   const float *vx = N.f(V2C_NF_VX), *vy = N.f(V2C_NF_VY);
   float Z;
   float nueff = nueff_of(N.f(V2C_NF_ND)[m3], N.f(V2C_NF_GD)[m3], dt, nubeg, Z);
-  const float edotxx = 0.5f * ((vx[v2] - vx[v0]) / __ldg(g.wx + m1 - 1) -
-                               (vy[v1] - vy[v0]) / __ldg(g.wy + m2 - 1));
+  // velocity differences from the FP64 copy where there is one: adjacent
+  // velocities agree in their leading digits, which FP32 storage would keep
+  // and the differences would lose
+  auto dvx = [&](long a, long b) {
+    return vx64 ? (float)(__ldg(vx64 + a) - __ldg(vx64 + b)) : vx[a] - vx[b];
+  };
+  auto dvy = [&](long a, long b) {
+    return vy64 ? (float)(__ldg(vy64 + a) - __ldg(vy64 + b)) : vy[a] - vy[b];
+  };
+  const float edotxx = 0.5f * (dvx(v2, v0) / __ldg(g.wx + m1 - 1) - dvy(v1, v0) / __ldg(g.wy + m2 - 1));
+  const float s0 = N.f(V2C_NF_SXXE)[m3];
   N.f(V2C_NF_EXX)[m3] = edotxx;
-  N.f(V2C_NF_SXX)[m3] = 2.f * nueff * edotxx + N.f(V2C_NF_SXXE)[m3] * (1.f - Z);
+  N.f(V2C_NF_SXX)[m3] = 2.f * nueff * edotxx + s0 * (1.f - Z);
+  // the increment itself: at a coseismic dt sxx and sxxe agree to a few
+  // FP32 ulps and their difference would be rounding
+  N.f(V2C_NF_DSXX)[m3] = 2.f * nueff * edotxx - Z * s0;
   if (m1 < g.xn - 1 && m2 < g.yn - 1) {
     nueff = nueff_of(N.f(V2C_NF_NU)[m3], N.f(V2C_NF_GG)[m3], dt, nubeg, Z);
-    const float exy1 = (vx[m3] - vx[v2]) / (__ldg(g.wy + m2 - 1) + __ldg(g.wy + m2));
-    const float exy2 = (vy[m3] - vy[v1]) / (__ldg(g.wx + m1 - 1) + __ldg(g.wx + m1));
+    const float exy1 = dvx(m3, v2) / (__ldg(g.wy + m2 - 1) + __ldg(g.wy + m2));
+    const float exy2 = dvy(m3, v1) / (__ldg(g.wx + m1 - 1) + __ldg(g.wx + m1));
     N.f(V2C_NF_EXY)[m3] = exy1 + exy2;
     N.f(V2C_NF_ESP)[m3] = exy1 - exy2;
     N.f(V2C_NF_SXY)[m3] = 2.f * nueff * (exy1 + exy2) + N.f(V2C_NF_SXYE)[m3] * (1.f - Z);
@@ -166,6 +182,12 @@ __global__ void k_copyarrays(Grid g, Nodes N) {
   N.f(V2C_NF_SLIPRS)[m3] = v;
   N.f(V2C_NF_RK_SLIPRS_FINAL)[m3] = v;
   N.f(V2C_NF_RK_PHIDTS_FINAL)[m3] = N.f(V2C_NF_RK_PHIDTS_SOLVED)[m3];
+}
+
+// accumulated slip of every marker (the per-marker Newton's slip rate)
+__global__ void k_marker_slip_acc(const float *slipv, long n, double dt, double *acc) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) acc[i] += dt * (double)slipv[i];
 }
 
 // accumulated slip of every interior basic node: acc += dt * slip rate
@@ -390,14 +412,18 @@ void launch_c2b_old(const Grid &g, const Nodes &N, cudaStream_t st) {
   k_c2b_old<<<nblk(g.nn, 256), 256, 0, st>>>(g, N);
 }
 
-void launch_c2b(const Grid &g, const Nodes &N, float dt, cudaStream_t st) {
-  k_c2b<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, dt);
+void launch_c2b(const Grid &g, const Nodes &N, float dt, int use_dsxx, cudaStream_t st) {
+  k_c2b<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, dt, use_dsxx);
 }
-void launch_recompute(const Grid &g, const Nodes &N, const Scal &S, float dt, cudaStream_t st) {
-  k_recompute<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, dt, S.nubeg_f);
+void launch_recompute(const Grid &g, const Nodes &N, const Scal &S, float dt, const double *vx64,
+                      const double *vy64, cudaStream_t st) {
+  k_recompute<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, dt, S.nubeg_f, vx64, vy64);
 }
 void launch_copyarrays(const Grid &g, const Nodes &N, cudaStream_t st) {
   k_copyarrays<<<nblk(g.nn, 256), 256, 0, st>>>(g, N);
+}
+void launch_marker_slip_acc(const float *slipv, long n, double dt, double *acc, cudaStream_t st) {
+  if (n > 0) k_marker_slip_acc<<<nblk(n, 256), 256, 0, st>>>(slipv, n, dt, acc);
 }
 void launch_slip_acc(const Grid &g, const Nodes &N, double dt, double *acc, cudaStream_t st) {
   k_slip_acc<<<nblk(g.nn, 256), 256, 0, st>>>(g, N.f(V2C_NF_RK_SLIPRS_FINAL), dt, acc);

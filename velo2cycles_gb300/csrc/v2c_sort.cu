@@ -251,6 +251,9 @@ void launch_gather_u8(const uint8_t *src, const int32_t *perm, uint8_t *dst, lon
 void launch_unpermute_f32(const float *src, const int32_t *id, double *out, long n, cudaStream_t st) {
   if (n > 0) k_unperm_f32<<<nblk(n, 256), 256, 0, st>>>(src, id, out, n);
 }
+void launch_unpermute_f64(const double *src, const int32_t *id, double *out, long n, cudaStream_t st) {
+  if (n > 0) k_unperm<double><<<nblk(n, 256), 256, 0, st>>>(src, id, out, n);
+}
 void launch_unpermute_i32(const int32_t *src, const int32_t *id, int32_t *out, long n, cudaStream_t st) {
   if (n > 0) k_unperm<int32_t><<<nblk(n, 256), 256, 0, st>>>(src, id, out, n);
 }

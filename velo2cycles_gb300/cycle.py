@@ -10,8 +10,8 @@ stream function psi = V/2 w log cosh((y - y_f)/w)).  Events are nucleated
 after a fixed number of interseismic steps and the pulse stops once its slip
 budget is spent.  The pulse steps are coseismic; otherwise the time step
 follows the pipeline's own maximum slip rate from calc_timestep
-(calc_RSF.c:352-572): coseismic dt while the rate exceeds `v_switch`,
-interseismic dt below it.  Each (regime, dt) pair runs as a captured CUDA
+(calc_RSF.c:352-572): coseismic dt while the rate exceeds `v_switch` (for at
+most `relax_max` steps after an event), interseismic dt below it.  Each (regime, dt) pair runs as a captured CUDA
 graph (v2c_cycle_step).
 """
 from __future__ import annotations
@@ -33,6 +33,7 @@ class Schedule:
     v_pulse: float = 1.0         # m/s across the band during an event
     width: float = 1000.0        # m, half-width of the pulse shear zone
     slip_budget: float = 0.1     # m of pulse slip per event
+    relax_max: int = 50          # coseismic-dt steps after a pulse at most
 
 
 def pulse_fields(case, s: Schedule):
@@ -73,25 +74,30 @@ class Driver:
         self.regime = 0
         self.dt = s.dt_inter
         self.n_in_regime = 0
+        self.n_relax = 0
         self.slip = 0.0
 
     def next(self, maxvel: float):
         """Advance the decisions after a step whose maximum slip rate was
         maxvel; returns (regime, dt) of the next step.  While the pulse runs
-        the step is coseismic; afterwards dt follows the slip rate, and only
-        interseismic steps count towards the next event."""
+        the step is coseismic; afterwards dt follows the slip rate for at most
+        `relax_max` steps (the stand-in has no healing: with a coseismic dt
+        simulated time hardly advances), and only interseismic steps count
+        towards the next event."""
         s = self.s
         if self.regime == 1:
             self.slip += s.v_pulse * self.dt
             if self.slip < s.slip_budget:
                 return self.regime, self.dt
-            self.regime, self.n_in_regime = 0, 0
+            self.regime, self.n_in_regime, self.n_relax = 0, 0, 0
         elif self.dt == s.dt_inter:
             self.n_in_regime += 1
             if self.n_in_regime >= s.n_inter:
                 self.regime, self.slip, self.dt = 1, 0.0, s.dt_co
                 return self.regime, self.dt
-        self.dt = s.dt_co if maxvel > s.v_switch else s.dt_inter
+        co = maxvel > s.v_switch and self.n_relax < s.relax_max
+        self.n_relax = self.n_relax + 1 if co else s.relax_max
+        self.dt = s.dt_co if co else s.dt_inter
         return self.regime, self.dt
 
 

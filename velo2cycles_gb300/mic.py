@@ -195,6 +195,11 @@ class MarkerInCell:
         call("v2c_cycle_slip", self.h, _ptr(a))
         return a
 
+    def cycle_marker_slip(self) -> np.ndarray:
+        a = np.zeros(self.n)
+        call("v2c_cycle_marker_slip", self.h, _ptr(a), int(self.n))
+        return a
+
     def compute_before_solve(self, dt: float, rk: int = 0):
         call("v2c_compute_before_solve", self.h, float(dt), int(rk))
 
