@@ -172,6 +172,9 @@ enum {
   /* sxx - sxxe of the step as recompute_stress_strainrate forms it
    * (2 nueff exx - Z sxxe, no cancellation); no reference array */
   V2C_NF_DSXX,
+  /* node temperature before the thermal solve (solve_temperature saves it
+   * as tk2, temperature_iterate.c:62) */
+  V2C_NF_TK2,
   V2C_NF_N
 };
 
@@ -309,6 +312,19 @@ typedef struct v2c_timestep_info {
 int v2c_calc_timestep(v2c_ctx *ctx, int oldornew, const v2c_timestep_ctl *ctl,
                       v2c_timestep_info *info);            /* [calc_RSF.c:352] */
 
+/* Marker part of solve_temperature [temperature_iterate.c:181-412], after
+ * the host's thermal solve: node TK holds the solved temperature, TK2 the
+ * one before it.  Fluid markers (type 50..99) take the interpolated solved
+ * temperature; rock markers (type < 50) strictly inside the model start
+ * from the old nodal temperature (at least tdeep) when their temperature is
+ * not positive, get the subgrid diffusion towards the old nodal
+ * temperature when heatdif > 0 (conductivity and rho*cp from the nodes kt,
+ * ro, cp, over the step's timestep), the solution's change, and then lose
+ * the node-averaged diffusion change again; the reference sums that
+ * average at each marker's upper-left node only, here per cell in sorted
+ * order (no float atomics). */
+int v2c_marker_temperature(v2c_ctx *ctx, double heatdif);
+
 /* ========================================================= seismic cycle
  * The seismic-cycle workload (no counterpart in the reference: it stands in
  * for the host Stokes solve with prescribed velocities).  Regime 0
@@ -358,6 +374,7 @@ enum {
   V2C_PROF_MOVE,        /* moveandrotatemarkers                        */
   V2C_PROF_TIMESTEP,    /* calc_timestep                                */
   V2C_PROF_B2C,         /* basic2center, center2basic, recompute stress */
+  V2C_PROF_TEMP,        /* marker temperature update                    */
   V2C_PROF_N
 };
 int v2c_set_profiling(v2c_ctx *ctx, int on);

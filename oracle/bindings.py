@@ -88,6 +88,8 @@ def _lib():
         lib.v2c_oracle_basic2center.argtypes = [P(_State)]
         lib.v2c_oracle_recompute_stress.restype = ctypes.c_int
         lib.v2c_oracle_recompute_stress.argtypes = [P(_State), ctypes.c_double]
+        lib.v2c_oracle_marker_temperature.restype = ctypes.c_int
+        lib.v2c_oracle_marker_temperature.argtypes = [P(_State), ctypes.c_double]
         lib.v2c_oracle_copyarrays.restype = ctypes.c_int
         lib.v2c_oracle_copyarrays.argtypes = [P(_State)]
         lib.v2c_oracle_center2basic.restype = ctypes.c_int
@@ -173,6 +175,9 @@ class Restatement:
 
     def recompute_stress(self, dt):
         return self.lib.v2c_oracle_recompute_stress(ctypes.byref(self.st), dt)
+
+    def marker_temperature(self, heatdif):
+        return self.lib.v2c_oracle_marker_temperature(ctypes.byref(self.st), heatdif)
 
     def copyarrays(self):
         return self.lib.v2c_oracle_copyarrays(ctypes.byref(self.st))
@@ -285,10 +290,13 @@ TIMESTEP_STAGE = 1 << 6
 B2C_STAGE, C2B_FULL_STAGE = 1 << 7, 1 << 8
 # recompute_stress_strainrate between them, copyarrays after compute_after_solve
 RECOMPUTE_STAGE, COPY_STAGE = 1 << 9, 1 << 10
+# solve_temperature with the thermal solve replaced by the node field TK2
+# (the new temperatures); afterwards TK holds them and TK2 the old ones
+TEMPERATURE_STAGE = 1 << 11
 
 
 def write_case(path: str, case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0,
-               timestep=None, oldornew=0, dts=None) -> None:
+               timestep=None, oldornew=0, dts=None, heatdif=None) -> None:
     """timestep: v2c_timestep_ctl values as a dict (abi.TIMESTEP_DEFAULTS when
     None); oldornew: the argument of calc_timestep (stage bit 6); dts: a
     time step per step (timesum advances after each)."""
@@ -313,9 +321,12 @@ def write_case(path: str, case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=
         ts = dict(abi.TIMESTEP_DEFAULTS, **(timestep or {}))
         np.array([ts["maxtmstep"], ts["dtfactor"], ts["tcnvp"], ts["tcd"], ts["tcphih"],
                   float(oldornew)], dtype=np.float64).tofile(f)
-        if dts is not None:
-            np.array([len(dts)], dtype=np.int64).tofile(f)
-            np.ascontiguousarray(dts, dtype=np.float64).tofile(f)
+        if dts is not None or heatdif is not None:
+            d = [] if dts is None else dts
+            np.array([len(d)], dtype=np.int64).tofile(f)
+            np.ascontiguousarray(d, dtype=np.float64).tofile(f)
+        if heatdif is not None:
+            np.array([heatdif], dtype=np.float64).tofile(f)
 
 
 def read_result(path: str, nodenum: int):
@@ -334,7 +345,7 @@ def read_result(path: str, nodenum: int):
 
 
 def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeout=3600,
-                  timestep=None, oldornew=0, dts=None):
+                  timestep=None, oldornew=0, dts=None, heatdif=None):
     """Run the reference routines on `case`; returns the arrays after the
     stages plus per-stage seconds summed over the timed steps."""
     if not reference_available():
@@ -343,7 +354,7 @@ def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeo
         raise RuntimeError("reference oracle not built (reference sources unavailable)")
     with tempfile.TemporaryDirectory() as d:
         cp, rp = os.path.join(d, "case.bin"), os.path.join(d, "res.bin")
-        write_case(cp, case, stages, nthreads, nsteps, warmup, timestep, oldornew, dts)
+        write_case(cp, case, stages, nthreads, nsteps, warmup, timestep, oldornew, dts, heatdif)
         env = dict(os.environ, OMP_NUM_THREADS=str(max(1, nthreads)))
         r = subprocess.run([reference_path(), cp, rp], env=env, capture_output=True,
                            timeout=timeout)

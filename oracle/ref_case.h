@@ -45,6 +45,7 @@ typedef struct {
   double ts[6];            /* maxtmstep, dtfactor, tcnvp, tcd, tcphih, oldornew */
   long ndts;               /* per-step time steps (optional trailer), 0 if none */
   double *dts;
+  double heatdif;          /* solve_temperature's subgrid diffusion (optional trailer) */
   v2c_timestep_info info;  /* calc_timestep results (stage bit 6) */
   long ts_rc;              /* 0, or 1 when chi == 0 stopped it */
 } ref_case;
@@ -118,6 +119,8 @@ static int ref_load_case(const char *path, ref_case *C) {
     rd(C->dts, sizeof(double), nd, f);
     C->ndts = nd;
   }
+  C->heatdif = 0;
+  if (fread(&C->heatdif, sizeof(double), 1, f) != 1) C->heatdif = 0;
   memset(&C->info, 0, sizeof(C->info));
   C->ts_rc = 0;
   fclose(f);

@@ -21,7 +21,8 @@
  *   double gx[xnumx], gy[ynumy], rt[V2C_RT_N][V2C_MAXTMR]
  *   double node[V2C_NF_N][nodenum], mark[V2C_MF_N][n]; int8 markt[n]
  *   int64 bondm[nodenum*4], bondn[bondnum*3]; double bondv[bondnum*4]
- *   double ts[6]; optional: int64 ndts, double dts[ndts] (per-step dt)
+ *   double ts[6]; optional: int64 ndts, double dts[ndts] (per-step dt),
+ *   double heatdif (stage bit 11: solve_temperature, new temperatures in tk2)
  * Result file:
  *   char magic[8] = "V2CRES01"; int64 n
  *   double node[V2C_NF_N][nodenum], mark[V2C_MF_N][n]; int8 markt[n]
@@ -114,6 +115,18 @@ int main(int argc, char **argv) {
     STAGE(8, 7, interpolate_center2basic(timestep));
     STAGE(3, 3, deltas = compute_after_solve(timestep, 0));
     STAGE(10, 7, copyarrays(0));
+    if (stages & (1 << 11)) {
+      /* solve_temperature (temperature_iterate.c:2-412) with the solver
+       * stubbed: the solution vector x holds the new temperatures (the case
+       * passes them in tk2), so after the call tk holds them and tk2 the old
+       * ones, and the marker part runs as in the reference */
+      for (long m = 0; m < C.nn; m++) x[m] = tk2[m];
+      heatdif = C.heatdif;
+      maxtkstep = 1e30;  /* one thermal substep */
+      t0 = omp_get_wtime();
+      solve_temperature(0);
+      if (timed) secs[7] += omp_get_wtime() - t0;
+    }
     STAGE(4, 4, nodes2markers());
     STAGE(5, 5, moveandrotatemarkers());
     if (stages & (1 << 6)) {

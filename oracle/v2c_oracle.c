@@ -838,6 +838,105 @@ int v2c_oracle_copyarrays(v2c_oracle_state *s) {
   return 0;
 }
 
+/* interpolate_temperature, interpolation.c:1492-1533: solved (TK) and old
+ * (TK2) node temperature at a point clamped into the model */
+static void temperature_at(const v2c_oracle_state *s, double x, double y, double *TK,
+                           double *TK2) {
+  const v2c_params *p = &s->p;
+  long xn = p->xnumx, yn = p->ynumy;
+  if (x < 0) x = 0; else if (x > p->xsize) x = p->xsize;
+  if (y < 0) y = 0; else if (y > p->ysize) y = p->ysize;
+  long m10 = v2c_oracle_nxsearch(s->gx, xn, x), m20 = v2c_oracle_nxsearch(s->gy, yn, y);
+  if (m10 < 0) m10 = 0;
+  if (m10 > xn - 2) m10 = xn - 2;
+  if (m20 < 0) m20 = 0;
+  if (m20 > yn - 2) m20 = yn - 2;
+  double e = (x - s->gx[m10]) / (s->gx[m10 + 1] - s->gx[m10]);
+  double n = (y - s->gy[m20]) / (s->gy[m20 + 1] - s->gy[m20]);
+  double dm0 = (1.0 - e) * (1.0 - n), dm1 = (1.0 - e) * n, dm2 = e * (1.0 - n), dm3 = e * n;
+  long m3 = m10 * yn + m20;
+  const double *tk = s->N[V2C_NF_TK], *tk2 = s->N[V2C_NF_TK2];
+  *TK = dm0 * tk[m3] + dm1 * tk[m3 + 1] + dm2 * tk[m3 + yn] + dm3 * tk[m3 + yn + 1];
+  *TK2 = dm0 * tk2[m3] + dm1 * tk2[m3 + 1] + dm2 * tk2[m3 + yn] + dm3 * tk2[m3 + yn + 1];
+}
+
+/* the marker part of solve_temperature, temperature_iterate.c:181-412:
+ * fluid markers take the solved temperature; rock markers the subgrid
+ * diffusion towards the old temperature, the solution's change, and the
+ * antidiffusion of the node-averaged diffusion change, summed at each
+ * marker's upper-left node only (the reference's loop bounds) */
+int v2c_oracle_marker_temperature(v2c_oracle_state *s, double heatdif) {
+  const v2c_params *p = &s->p;
+  long xn = p->xnumx, yn = p->ynumy, nn = nnodes(s), n = s->n;
+  const double *gx = s->gx, *gy = s->gy, *kt = s->N[V2C_NF_KT], *cp = s->N[V2C_NF_CP];
+  const double *ro = s->N[V2C_NF_RO];
+  double *mx = s->M[V2C_MF_X], *my = s->M[V2C_MF_Y], *mk = s->M[V2C_MF_K];
+  const double dt = p->timestep;
+  double *tol0 = calloc(nn, sizeof(double)), *tol1 = calloc(nn, sizeof(double));
+  (void)xn;
+#define INSIDE(m) (mx[m] > 0 && my[m] > 0 && mx[m] < p->xsize && my[m] < p->ysize)
+  for (long m3 = 0; m3 < n; m3++) {
+    if (INSIDE(m3) && s->t[m3] >= 50 && s->t[m3] < 100) {
+      double TK, TK2;
+      temperature_at(s, mx[m3], my[m3], &TK, &TK2);
+      mk[m3] = TK;
+    }
+  }
+  const long last = s->phantom ? n : n - 1;
+  for (long m3 = 0; m3 <= last; m3++) {
+    if (!(INSIDE(m3) && s->t[m3] < 50)) continue;
+    long m10 = v2c_oracle_nxsearch(gx, p->xnumx, mx[m3]);
+    long m20 = v2c_oracle_nxsearch(gy, p->ynumy, my[m3]);
+    double TK, TK2;
+    temperature_at(s, mx[m3], my[m3], &TK, &TK2);
+    if (mk[m3] <= 0) {
+      mk[m3] = TK2;
+      if (mk[m3] < p->tdeep) mk[m3] = p->tdeep;
+    }
+    if (heatdif) {
+      double dtk = TK2 - mk[m3];
+      double celdx = gx[m10 + 1] - gx[m10], celdy = gy[m20 + 1] - gy[m20];
+      double swt1 = 1.0 / celdx / celdy;
+      double ex = (mx[m3] - gx[m10]) / (gx[m10 + 1] - gx[m10]);
+      double ey = (my[m3] - gy[m20]) / (gy[m20 + 1] - gy[m20]);
+      /* the reference's loop order: m1 outer, m2 inner */
+      double w[4] = {(1.0 - ex) * (1.0 - ey), (1.0 - ex) * ey, ex * (1.0 - ey), ex * ey};
+      long nd[4] = {m10 * yn + m20, m10 * yn + m20 + 1, (m10 + 1) * yn + m20,
+                    (m10 + 1) * yn + m20 + 1};
+      double mkt = 0, mrocp = 0;
+      for (int q = 0; q < 4; q++) {
+        mkt += kt[nd[q]] * w[q];
+        mrocp += cp[nd[q]] * ro[nd[q]] * w[q];
+      }
+      double dtk1 = -heatdif * mkt / mrocp * 2.0 * (1.0 / celdx / celdx + 1.0 / celdy / celdy) * dt;
+      if (dtk1 < -150.0) dtk1 = -150.0;
+      dtk1 = dtk * (1.0 - exp(dtk1));
+      mk[m3] += dtk1;
+      double ival = (1.0 - ex) * (1.0 - ey) * swt1;
+      tol0[nd[0]] += ival;
+      tol1[nd[0]] += dtk1 * ival;
+    }
+    mk[m3] += (TK - TK2);
+  }
+  if (heatdif) {
+    for (long m = 0; m < nn; m++)
+      if (tol0[m]) tol1[m] /= tol0[m];
+    for (long m3 = 0; m3 <= last; m3++) {
+      if (!(INSIDE(m3) && s->t[m3] < 50)) continue;
+      long m10 = v2c_oracle_nxsearch(gx, p->xnumx, mx[m3]);
+      long m20 = v2c_oracle_nxsearch(gy, p->ynumy, my[m3]);
+      double ex = (mx[m3] - gx[m10]) / (gx[m10 + 1] - gx[m10]);
+      double ey = (my[m3] - gy[m20]) / (gy[m20 + 1] - gy[m20]);
+      long m4 = m10 * yn + m20;
+      if (tol1[m4]) mk[m3] -= (tol1[m4] * ((1.0 - ex) * (1.0 - ey)));
+    }
+  }
+#undef INSIDE
+  free(tol0);
+  free(tol1);
+  return 0;
+}
+
 /* calc_vpvisc, calc_RSF.c:33-169 (rkmod 0 and 1) */
 static double vpvisc(v2c_oracle_state *s, int rk, double dt, long m3, double nP,
                      double W, int *err) {

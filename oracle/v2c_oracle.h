@@ -47,6 +47,7 @@ int v2c_oracle_center2basic(v2c_oracle_state *s, double dt);
 int v2c_oracle_basic2center(v2c_oracle_state *s);
 int v2c_oracle_recompute_stress(v2c_oracle_state *s, double dt);
 int v2c_oracle_copyarrays(v2c_oracle_state *s);
+int v2c_oracle_marker_temperature(v2c_oracle_state *s, double heatdif);
 int v2c_oracle_compute_before_solve(v2c_oracle_state *s, double dt, int rk);
 double v2c_oracle_compute_after_solve(v2c_oracle_state *s, double dt, int rk);
 int v2c_oracle_nodes2markers(v2c_oracle_state *s);

@@ -41,7 +41,7 @@ int main(void) {
 
 
 def test_enums_parsed():
-    assert abi.NF_DSXX == abi.NF_N - 1 and abi.NF_EXXS == abi.NF_PRS + 1
+    assert abi.NF_TK2 == abi.NF_N - 1 and abi.NF_EXXS == abi.NF_PRS + 1
     assert abi.MF_SLIPV == abi.MF_N - 1
     assert abi.MLP_NPARAM == 64 * 8 + 64 + 64 * 64 + 64 + 2 * 64 + 2 + 20
     assert abi.ERR_NOCONV == 6

@@ -108,6 +108,7 @@ static double *v2c_bind_node_array(int f) {
     case V2C_NF_PRS: return prs;
     case V2C_NF_EXXS: return exxs;
     case V2C_NF_EXXEL: return exxel;
+    case V2C_NF_TK2: return tk2;
   }
   return NULL;
 }

@@ -47,6 +47,7 @@ struct v2c_ctx {
   int nstage_cap = 0;          // fields d_nstage holds
   uint32_t *d_sticky = nullptr;
   float4 *d_quad = nullptr;                  // move: velocity forms per cell quarter
+  float *d_tol = nullptr;                    // temperature update: node scratch
   unsigned *d_list_n = nullptr;              // count of listed Newton problems
   double *d_ts = nullptr;                    // calc_timestep scratch
   // markers
@@ -269,6 +270,7 @@ extern "C" int v2c_create(const v2c_params *p, long max_markers, void *cuda_stre
   AL(ctx->d_node64, ctx->nn);
   AL(ctx->d_sticky, ctx->nn);
   AL(ctx->d_quad, (size_t)ctx->ncell * QUAD_FLOAT4);
+  AL(ctx->d_tol, ctx->nn);
   AL(ctx->d_list_n, 1);
   AL(ctx->d_ts, TIMESTEP_SCRATCH);
   AL(ctx->d_stat, ST_N);
@@ -318,7 +320,7 @@ extern "C" int v2c_destroy(v2c_ctx *ctx) {
   if (ctx->d_slip) cudaFree(ctx->d_slip);
   if (ctx->d_mslip) cudaFree(ctx->d_mslip);
   void *ptrs[] = {ctx->d_gx, ctx->d_gy, ctx->d_wx, ctx->d_wy, ctx->d_gxf, ctx->d_gyf,
-                  ctx->d_rock, ctx->d_node, ctx->d_node64, ctx->d_sticky, ctx->d_quad, ctx->d_list_n, ctx->d_ts,
+                  ctx->d_rock, ctx->d_node, ctx->d_node64, ctx->d_sticky, ctx->d_quad, ctx->d_tol, ctx->d_list_n, ctx->d_ts,
                   ctx->d_stat, ctx->d_red, ctx->d_nstage,
                   ctx->sb.counts, ctx->sb.start, ctx->sb.qstart, ctx->sb.slot, ctx->sb.tmp, ctx->sb.perm,
                   ctx->sb.blocksum, ctx->d_stage64, ctx->d_stage64b, ctx->bc_mem,
@@ -1014,6 +1016,41 @@ extern "C" int v2c_calc_timestep(v2c_ctx *ctx, int oldornew, const v2c_timestep_
 extern "C" int v2c_synchronize(v2c_ctx *ctx) {
   if (!ctx) return V2C_ERR_ARG;
   CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaGetLastError());
+  return V2C_OK;
+}
+
+// ================================================== marker temperature
+extern "C" int v2c_marker_temperature(v2c_ctx *ctx, double heatdif) {
+  int rc = ready(ctx);
+  if (rc) return rc;
+  cudaStream_t st = ctx->stream;
+  if (!ctx->sorted) {
+    launch_sort(ctx->m.cell_in, ctx->m.u_in, ctx->m.v_in, ctx->n, ctx->ncell, ctx->sb,
+                ctx->d_stat, st);
+    ctx->launches += ctx->n > 0 ? 6 : 3;
+    ctx->sorted = true;
+  }
+  TempArgs a;
+  a.g = make_grid(ctx);
+  a.N = make_nodes(ctx);
+  a.m = ctx->m;
+  a.perm = ctx->sb.perm;
+  a.start = ctx->sb.start;
+  a.n = ctx->n;
+  a.ncell = ctx->ncell;
+  a.heatdif = (float)heatdif;
+  a.dt = (float)ctx->p.timestep;
+  a.tdeep = (float)ctx->p.tdeep;
+  // the sort's slot buffers hold nothing between sorts (one entry per marker)
+  a.dtk1 = reinterpret_cast<float *>(ctx->sb.tmp);
+  a.wt = reinterpret_cast<float *>(ctx->sb.slot);
+  a.tol = ctx->d_tol;
+  {
+    Prof pr(ctx, V2C_PROF_TEMP);
+    launch_temperature(a, st);
+  }
+  ctx->launches += ctx->n > 0 ? (heatdif != 0 ? 3 : 1) : 0;
   CK(cudaGetLastError());
   return V2C_OK;
 }

@@ -131,6 +131,20 @@ void launch_n2m(const N2MArgs &a, cudaStream_t st);
 // moveandrotatemarkers: one thread per marker, new positions to *_out
 void launch_move(const N2MArgs &a, cudaStream_t st);
 
+// the marker part of solve_temperature (v2c_temp.cu)
+struct TempArgs {
+  Grid g;
+  Nodes N;
+  Markers m;
+  const int32_t *perm;
+  const int32_t *start;
+  long n, ncell;
+  float heatdif, dt, tdeep;
+  float *dtk1, *wt;  // per sorted position (scratch)
+  float *tol;        // per node (scratch)
+};
+void launch_temperature(const TempArgs &a, cudaStream_t st);
+
 // calc_timestep over the device node fields (synchronises the stream);
 // scratch: TIMESTEP_SCRATCH doubles
 constexpr long TIMESTEP_SCRATCH = (152 * 4 * 8 + 1) * 32 + 64;

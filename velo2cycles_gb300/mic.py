@@ -172,6 +172,11 @@ class MarkerInCell:
         node strain rates and visco-elastic stresses from vx, vy."""
         call("v2c_recompute_stress_strainrate", self.h, float(dt))
 
+    def marker_temperature(self, heatdif: float = 1.0):
+        """The marker part of solve_temperature (temperature_iterate.c:181):
+        node TK holds the solved temperature, TK2 the previous one."""
+        call("v2c_marker_temperature", self.h, float(heatdif))
+
     def copyarrays(self):
         """copyarrays (momentum_continuity_iterate.c:265)."""
         call("v2c_copyarrays", self.h)
