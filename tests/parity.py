@@ -48,6 +48,21 @@ VISCOUS = {abi.NF_NU_M2C, abi.NF_GG, abi.NF_ND_M2C, abi.NF_GD, abi.NF_NUVP_IT, a
            abi.NF_RK_PHIDTS_SOLVED, abi.NF_ND, abi.NF_EXXPL, abi.NF_EXXEL}
 
 
+def temperature_case(seed, name="small"):
+    """(case, old node T, new node T) for the marker temperature update: a
+    smooth change of the node temperatures, newly arrived rock markers
+    (T = 0) and fluid markers (type 50)."""
+    from velo2cycles_gb300 import synth
+    c = synth.make_case(name, seed)
+    yn = c.gy.size
+    m = np.arange(c.nodenum)
+    told = c.nodes[abi.NF_TK].copy()
+    tnew = told + 5.0 * np.sin(0.3 * (m // yn)) * np.cos(0.2 * (m % yn))
+    c.marks[abi.MF_K][50:60] = 0.0
+    c.markt[100:110] = 50
+    return c, told, tnew
+
+
 def rel_err(a: np.ndarray, b: np.ndarray) -> float:
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)

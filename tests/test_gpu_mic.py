@@ -14,7 +14,8 @@ import pytest
 import oracle
 from velo2cycles_gb300 import abi, mic, synth
 
-from .parity import (B2C_C2B_OUT, C2B_OUT, COPY_OUT, M2N_OUT, RECOMPUTE_OUT, MOVE_MARK, N2M_MARK, N2M_OUT, RSF_OUT, VISCOUS,
+from .parity import (B2C_C2B_OUT, C2B_OUT, COPY_OUT, M2N_OUT, RECOMPUTE_OUT, rel_err,
+                     temperature_case, MOVE_MARK, N2M_MARK, N2M_OUT, RSF_OUT, VISCOUS,
                      node_errors, marker_errors, nxsearch_np)
 
 pytestmark = pytest.mark.gpu
@@ -103,6 +104,22 @@ def test_picard_pass_node_routines(case):
     m.compute_after_solve(dt, 0); ref.compute_after_solve(dt, 0)
     m.copyarrays(); ref.copyarrays()
     _check_nodes(node_errors(m.download_nodes(COPY_OUT + RSF_OUT), ref.nodes, COPY_OUT + RSF_OUT))
+    m.close()
+
+
+@pytest.mark.parametrize("heatdif", [1.0, 0.0])
+def test_marker_temperature(heatdif, built_lib, oracle_built):
+    """The marker part of solve_temperature: fluid markers, newly arrived
+    markers, subgrid diffusion and the per-cell antidiffusion."""
+    c, told, tnew = temperature_case(15)
+    c.nodes[abi.NF_TK], c.nodes[abi.NF_TK2] = tnew, told
+    m = mic.from_case(c)
+    ref = oracle.Restatement(c.copy())
+    m.marker_temperature(heatdif)
+    ref.marker_temperature(heatdif)
+    got = m.download_markers([abi.MF_K])[abi.MF_K]
+    assert not np.array_equal(ref.marks[abi.MF_K], c.marks[abi.MF_K])
+    assert rel_err(got, ref.marks[abi.MF_K]) <= TOL
     m.close()
 
 

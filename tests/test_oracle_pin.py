@@ -19,6 +19,8 @@ import oracle
 from oracle import bindings as B
 from velo2cycles_gb300 import abi, synth
 
+from .parity import temperature_case
+
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ref_micro.npz")
 
 
@@ -156,26 +158,13 @@ def test_multi_step_dt_sequence_bit_exact_vs_reference():
     assert not _compare(r, ref["nodes"], ref["marks"])
 
 
-def _temperature_case(seed):
-    """A case with new node temperatures (old + a smooth change), newly
-    arrived rock markers (T = 0) and fluid markers (type 50)."""
-    c = synth.make_case("small", seed)
-    yn = c.gy.size
-    m = np.arange(c.nodenum)
-    told = c.nodes[abi.NF_TK].copy()
-    tnew = told + 5.0 * np.sin(0.3 * (m // yn)) * np.cos(0.2 * (m % yn))
-    c.marks[abi.MF_K][50:60] = 0.0
-    c.markt[100:110] = 50
-    return c, told, tnew
-
-
 @needs_ref
 @pytest.mark.parametrize("heatdif", [1.0, 0.0])
 def test_marker_temperature_bit_exact_vs_reference(heatdif):
     """The marker part of solve_temperature (temperature_iterate.c:181-412):
     the reference's own routine, with its thermal solve stubbed to return
     the given new temperatures, against the restatement."""
-    c, told, tnew = _temperature_case(14)
+    c, told, tnew = temperature_case(14)
     cr = c.copy()
     cr.nodes[abi.NF_TK], cr.nodes[abi.NF_TK2] = told, tnew  # harness convention
     ref = B.run_reference(cr, stages=B.TEMPERATURE_STAGE, heatdif=heatdif)

@@ -191,6 +191,16 @@ double v2c_bind_interpolate_center2basic(double dt) {
   return 0;
 }
 
+/* the marker part of solve_temperature (temperature_iterate.c:181-412),
+ * after the host's thermal solve has left the solved temperature in tk and
+ * the previous one in tk2 */
+void v2c_bind_marker_temperature(void) {
+  if (!v2c_bind_setup() || !v2c_bind_nodes_up()) return;
+  if (!v2c_bind_ok(v2c_marker_temperature(v2c_bind_ctx, heatdif), "v2c_marker_temperature"))
+    return;
+  if (v2c_bind_sync_markers) v2c_bind_markers_to_host();
+}
+
 void v2c_bind_compute_before_solve(double dt, int rk) {
   if (!v2c_bind_setup() || !v2c_bind_nodes_up()) return;
   if (!v2c_bind_ok(v2c_compute_before_solve(v2c_bind_ctx, dt, rk), "v2c_compute_before_solve"))

@@ -50,6 +50,10 @@ void v2c_bind_moveandrotatemarkers(void);
 double v2c_bind_calc_timestep(int oldornew);
 double v2c_bind_interpolate_basic2center(void);
 double v2c_bind_interpolate_center2basic(double dt);
+/* the marker part of solve_temperature; the thermal solve stays on the host
+ * (temperature_iterate.c:2-179), followed by this call in place of its
+ * lines 181-412 */
+void v2c_bind_marker_temperature(void);
 
 /* the host changed marker arrays (temperature solve, loading a file) */
 void v2c_bind_markers_changed(void);
