@@ -312,6 +312,41 @@ typedef struct v2c_timestep_info {
 int v2c_calc_timestep(v2c_ctx *ctx, int oldornew, const v2c_timestep_ctl *ctl,
                       v2c_timestep_info *info);            /* [calc_RSF.c:352] */
 
+/* ============================================================ restart files
+ * The reference's binary restart format (.prn: load_model / save_model,
+ * load_save.c:164-527, with the RSF extras of input_RSF.c:94-132), read and
+ * written on the host (no GPU needed).  Arrays are the caller's, sized from
+ * the info: rt[V2C_RT_N * V2C_MAXTMR] (the rock rows the path uses, markim
+ * in V2C_RT_IM), rock_extra[V2C_PRN_ROCK_EXTRA * V2C_MAXTMR] (s0 s1 ll a0 a1
+ * b0 b1 e0 e1 f0 f1, which the path does not read), node[V2C_NF_N] (each
+ * nodenum doubles; the file holds sxxee sxx exxee exx sxyee sxy exyee exy
+ * sppee pr phie phis_it mvxe vx mvye vy pes pee RK_sliprs_final
+ * RK_phidts_final), bondm[4 * nodenum], gx[xnumx], gy[ynumy],
+ * bondv[4 * bondnum], bondn[3 * bondnum] (equation 0 unused, as in the
+ * reference), mark[V2C_MF_N] (each marknum doubles: x y k e xx v xy p exx
+ * exy d w vx vy phi L L0 C C0), markt[marknum].  A NULL array is skipped
+ * when reading and written as zeros. */
+typedef struct v2c_prn_info {
+  long xnumx, ynumy, mnumx, mnumy, marknum, bondnum;
+  double xsize, ysize, pinit, pkf[4], timestep, timesum, gxkoef, gykoef;
+  int rocknum, cycle;
+  double timesave[5];
+} v2c_prn_info;
+#define V2C_PRN_ROCK_EXTRA 11
+/* the header; V2C_ERR_UNSUPPORTED when the file's int/long/float/double
+ * sizes differ from this machine's or its counts are out of range */
+int v2c_prn_read_info(const char *path, v2c_prn_info *info);
+/* the whole file into arrays sized from *info (from v2c_prn_read_info);
+ * V2C_ERR_CAPACITY when the file's counts differ from *info,
+ * V2C_ERR_UNSUPPORTED when bytes remain after the markers */
+int v2c_prn_read(const char *path, v2c_prn_info *info, double *rt, double *rock_extra,
+                 double *const *node, long *bondm, double *gx, double *gy, double *bondv,
+                 long *bondn, double *const *mark, signed char *markt);
+int v2c_prn_write(const char *path, const v2c_prn_info *info, const double *rt,
+                  const double *rock_extra, const double *const *node, const long *bondm,
+                  const double *gx, const double *gy, const double *bondv, const long *bondn,
+                  const double *const *mark, const signed char *markt);
+
 /* Marker part of solve_temperature [temperature_iterate.c:181-412], after
  * the host's thermal solve: node TK holds the solved temperature, TK2 the
  * one before it.  Fluid markers (type 50..99) take the interpolated solved

@@ -293,6 +293,9 @@ RECOMPUTE_STAGE, COPY_STAGE = 1 << 9, 1 << 10
 # solve_temperature with the thermal solve replaced by the node field TK2
 # (the new temperatures); afterwards TK holds them and TK2 the old ones
 TEMPERATURE_STAGE = 1 << 11
+# save_model (load_save.c:353) after the steps: the result holds the bytes
+# of the restart file the reference wrote ("prn")
+SAVE_STAGE = 1 << 12
 
 
 def write_case(path: str, case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0,
@@ -357,7 +360,11 @@ def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeo
         write_case(cp, case, stages, nthreads, nsteps, warmup, timestep, oldornew, dts, heatdif)
         env = dict(os.environ, OMP_NUM_THREADS=str(max(1, nthreads)))
         r = subprocess.run([reference_path(), cp, rp], env=env, capture_output=True,
-                           timeout=timeout)
+                           timeout=timeout, cwd=d)
         if r.returncode != 0:
             raise RuntimeError(f"v2c_ref failed ({r.returncode}): {r.stderr.decode()[-2000:]}")
-        return read_result(rp, case.nodenum)
+        res = read_result(rp, case.nodenum)
+        if stages & SAVE_STAGE:
+            with open(os.path.join(d, "state.prn"), "rb") as f:
+                res["prn"] = f.read()
+        return res

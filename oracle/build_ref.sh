@@ -27,7 +27,7 @@ $CC -std=gnu99 -O2 -ffp-contract=off -fPIC -shared -Wall \
 FILES="headevps.c input_RSF.c calc_RSF.c gausevps.c interpolation.c \
 density_ductilevisc_calc.c moveandrotatemarkers.c \
 momentum_continuity_addmatrix_checkerror.c momentum_continuity_iterate.c \
-temperature_iterate.c plastic.c recalc_marker_properties.c"
+temperature_iterate.c plastic.c recalc_marker_properties.c load_save.c"
 
 if [ -d "$REF/src" ]; then
   mkdir -p "$OUT/src"

@@ -11,10 +11,11 @@
  *   interpolate_basic2center, recompute_stress_strainrate,
  *   interpolate_center2basic, copyarrays (stage bits 7, 9, 8, 10),
  *   compute_after_solve, nodes2markers, moveandrotatemarkers, calc_timestep
- * and writes the arrays back.  Stdout (the reference's progress prints) is
- * discarded.
+ * and writes the arrays back; with stage bit 12 it also runs save_model,
+ * which writes the restart file state.prn into the working directory.
+ * Stdout (the reference's progress prints) is discarded.
  *
- * Case file (native endianness), written by velo2cycles_gb300/oracle_io.py:
+ * Case file (native endianness), written by oracle/bindings.py:
  *   char magic[8] = "V2CCASE1"
  *   int64 xnumx, ynumy, n, bondnum, nthreads, stages, nsteps, warmup
  *   v2c_params
@@ -54,6 +55,7 @@
 #include "temperature_iterate.c"
 #include "plastic.c"
 #include "recalc_marker_properties.c"
+#include "load_save.c"
 
 #include "../include/v2c.h"
 #include "../velo2cycles_gb300/bind/v2c_bind_map.h"
@@ -139,6 +141,15 @@ int main(int argc, char **argv) {
     }
 #undef STAGE
     if (step < C.ndts) timesum += timestep;
+  }
+
+  if (stages & (1 << 12)) {
+    /* save_model (load_save.c:353-527) of the state after the steps, into
+     * the working directory as state.prn (it also writes file.t3c and
+     * file_hdf5.t3c there); the cycle number is the step count */
+    rocknum = V2C_MAXTMR;
+    strcpy(fl1out, "state.prn");
+    save_model(0, warmup + nsteps, 0);
   }
 
   return ref_write_result(argv[2], &C, secs, deltas);

@@ -1,6 +1,8 @@
 """Generate tests/golden/ref_micro.npz: inputs and outputs of the reference's
 own routines (compiled from its sources by oracle/build_ref.sh) on two micro
-cases, for pinning the oracle restatement where the reference is absent.
+cases, for pinning the oracle restatement where the reference is absent,
+and the restart file (.prn) the reference's save_model wrote after the step
+on the first case.
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -33,7 +35,7 @@ def main():
     out = {}
     for name, kw in CASES.items():
         c = micro(7, **kw)
-        res = B.run_reference(c, nthreads=1)
+        res = B.run_reference(c, stages=B.ALL_STAGES | B.SAVE_STAGE, nthreads=1)
         out[f"{name}/params"] = np.array(json.dumps(c.params, sort_keys=True))
         out[f"{name}/gx"], out[f"{name}/gy"], out[f"{name}/rt"] = c.gx, c.gy, c.rt
         out[f"{name}/nodes_in"] = np.stack([c.nodes[k] for k in range(abi.NF_N)])
@@ -42,6 +44,8 @@ def main():
         out[f"{name}/bondm"], out[f"{name}/bondn"], out[f"{name}/bondv"] = c.bondm, c.bondn, c.bondv
         out[f"{name}/nodes_out"] = np.stack([res["nodes"][k] for k in range(abi.NF_N)])
         out[f"{name}/marks_out"] = np.stack([res["marks"][k] for k in range(abi.MF_N)])
+        if name == "default":
+            out[f"{name}/prn"] = np.frombuffer(res["prn"], dtype=np.uint8)
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "ref_micro.npz")
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path))

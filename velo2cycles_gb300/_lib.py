@@ -44,6 +44,11 @@ _SIGS = {
     "v2c_recompute_stress_strainrate": [c_ctx, ctypes.c_double],
     "v2c_copyarrays": [c_ctx],
     "v2c_marker_temperature": [c_ctx, ctypes.c_double],
+    "v2c_prn_read_info": [ctypes.c_char_p, P(abi.PrnInfo)],
+    "v2c_prn_read": [ctypes.c_char_p, P(abi.PrnInfo), c_dp, c_dp, P(c_dp), P(ctypes.c_long),
+                     c_dp, c_dp, c_dp, P(ctypes.c_long), P(c_dp), P(ctypes.c_byte)],
+    "v2c_prn_write": [ctypes.c_char_p, P(abi.PrnInfo), c_dp, c_dp, P(c_dp), P(ctypes.c_long),
+                      c_dp, c_dp, c_dp, P(ctypes.c_long), P(c_dp), P(ctypes.c_byte)],
     "v2c_cycle_set_velocity": [c_ctx, ctypes.c_int, c_dp, c_dp],
     "v2c_cycle_step": [c_ctx, ctypes.c_int, ctypes.c_double, ctypes.c_int],
     "v2c_cycle_slip": [c_ctx, c_dp],

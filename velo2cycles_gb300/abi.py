@@ -55,7 +55,9 @@ def _struct_fields(name: str) -> list:
             continue
         typ, names = decl.split(None, 1)
         for nm in names.split(","):
-            out.append((nm.strip(), _CT[typ]))
+            nm = nm.strip()
+            a = re.match(r"(\w+)\[(\d+)\]$", nm)
+            out.append((a.group(1), _CT[typ] * int(a.group(2))) if a else (nm, _CT[typ]))
     return out
 
 
@@ -121,6 +123,11 @@ class TimestepInfo(ctypes.Structure):
 
     def to_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class PrnInfo(ctypes.Structure):
+    """v2c_prn_info: the header of a restart file."""
+    _fields_ = _struct_fields("v2c_prn_info")
 
 
 # reference defaults (input_RSF.c:17-20); maxtmstep comes from the model file
