@@ -666,6 +666,24 @@ def run_cycle(args) -> None:
             "marker_x_cells": float((np.abs(mk[abi.MF_X] - ref.r.marks[abi.MF_X]) / wx).max()),
             "oracle_seconds": t_ref, "gpu_seconds": rec.seconds}
         m.close()
+        # the sensitivity of the sequence itself: the FP64 oracle from the
+        # same state with its marker fields rounded to FP32 (what the device
+        # stores at upload; positions kept) and from the state scaled by
+        # 1 + 1e-12, same regime and dt sequence
+        seq_ref = list(zip(rec_ref.regime, rec_ref.dt))
+        sens = {}
+        for name, rel in (("fp32_rounded_marker_fields", None), ("relative_1e-12", 1e-12)):
+            c = case.copy()
+            for f in c.marks:
+                if f not in (abi.MF_X, abi.MF_Y):
+                    c.marks[f] = (c.marks[f].astype(np.float32).astype(np.float64) if rel is None
+                                  else c.marks[f] * (1.0 + rel))
+            o2 = _OracleCycle(c, fields)
+            cycle.run(o2, s2, k, forced=seq_ref)
+            sens[name] = {"accumulated_slip": _drift(o2.slip[o2.inner], ref.slip[ref.inner]),
+                          "node_sxy": _drift(o2.r.nodes[abi.NF_SXY], ref.r.nodes[abi.NF_SXY]),
+                          "marker_sxy": _drift(o2.r.marks[abi.MF_XY], ref.r.marks[abi.MF_XY])}
+        out["drift_fp64_oracle_from_perturbed_state"] = sens
     print(json.dumps(out), flush=True)
 
 

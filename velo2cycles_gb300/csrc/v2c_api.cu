@@ -225,11 +225,11 @@ int check_params(const v2c_params *p) {
 }
 
 int pick_tx(const v2c_ctx *c) {
-  // widest column strip that still gives 1.5 waves of 6 resident CTAs on
+  // widest column strip that still gives 1.5 waves of 7 resident CTAs on
   // each of the 152 SMs; a strip of tx columns restages one halo column
   long rows = (c->yn + 31) / 32;
   int tx = 32;
-  while (tx > 4 && rows * ((c->xn + tx - 1) / tx) < 152 * 6 * 3 / 2) tx /= 2;
+  while (tx > 4 && rows * ((c->xn + tx - 1) / tx) < 152 * 7 * 3 / 2) tx /= 2;
   return tx;
 }
 

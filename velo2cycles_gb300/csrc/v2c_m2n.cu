@@ -156,7 +156,7 @@ __device__ __forceinline__ void node_friction(const M2NArgs &a, int ci, int j, f
     A[6].add(w);                                                      \
   } while (0)
 
-__global__ void __launch_bounds__(NTH, 6) k_m2n(M2NArgs a) {
+__global__ void __launch_bounds__(NTH, 7) k_m2n(M2NArgs a) {
   __shared__ Smem sm;
   const Grid &g = a.g;
   const int tid = threadIdx.x, role = tid / TY, jl = tid % TY;
