@@ -34,8 +34,12 @@ def _check_nodes(errs):
     assert not bad, f"node fields over tolerance: {bad}"
 
 
-@pytest.fixture(scope="module", params=["tiny", "small"])
+@pytest.fixture(scope="module", params=["tiny", "small", "dense"])
 def case(request, built_lib, oracle_built):
+    if request.param == "dense":
+        # 48 markers per cell: a column strip of a tile holds about 1000
+        # markers, so the tile kernels stage it in several chunks
+        return synth.make_case("small", seed=7, n_markers=3 * 50 * 20 * 16)
     return synth.make_case(request.param, seed=7)
 
 
