@@ -36,6 +36,7 @@ workload; the reference has no per-marker Newton.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -687,6 +688,74 @@ def run_cycle(args) -> None:
     print(json.dumps(out), flush=True)
 
 
+def run_stokes(args) -> None:
+    """The Stokes matrix assembly (preparematrix + gausmat4_add) on the C2
+    grid (1001 x 401 lines, 1.2 M equations) from the node fields of one
+    marker2nodes / compute_before_solve / basic2center pass: device time
+    (count, scan and fill kernels, CUDA events), the call end to end (CSR
+    arrays copied to host memory), the arrays against the oracle
+    restatement on the same node values (bit for bit), and the reference's
+    own preparematrix on the same values (one host thread; it has no
+    OpenMP)."""
+    from oracle import bindings as B
+    import oracle
+    from velo2cycles_gb300 import abi, mic, synth
+    oracle.build()
+    case = synth.make_case("c2", seed=2)
+    dt = float(case.params["timestep"])
+    m = mic.from_case(case)
+    m.marker2nodes()
+    m.compute_before_solve(dt, 0)
+    m.interpolate_basic2center()
+    ctl = dict(abi.STOKES_DEFAULTS, mukoef=dt * 30e5, dt=dt)
+    got = m.stokes_assemble(**ctl)
+    rows, nnz = got["b"].size, got["ja"].size
+    c = abi.StokesCtl(**ctl)
+    P = ctypes.POINTER
+    ia, ja = np.zeros(rows + 1, dtype=np.int32), np.zeros(nnz, dtype=np.int32)
+    a, b = np.zeros(nnz), np.zeros(rows)
+    n_out = ctypes.c_long(0)
+    ptrs = (ia.ctypes.data_as(P(ctypes.c_int)), ja.ctypes.data_as(P(ctypes.c_int)),
+            a.ctypes.data_as(P(ctypes.c_double)), b.ctypes.data_as(P(ctypes.c_double)))
+    from velo2cycles_gb300._lib import call
+    for _ in range(args.warmup):
+        call("v2c_stokes_assemble", m.h, ctypes.byref(c), nnz, *ptrs, ctypes.byref(n_out))
+    m.set_profiling(True)
+    p0 = m.profile()["stokes"]
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        call("v2c_stokes_assemble", m.h, ctypes.byref(c), nnz, *ptrs, ctypes.byref(n_out))
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    p1 = m.profile()["stokes"]
+    dev_ms = (p1[0] - p0[0]) / args.steps
+    # the same node values as FP64 for the restatement and the reference
+    cc = case.copy()
+    nodes = m.download_nodes(list(range(abi.NF_N)))
+    for f in range(abi.NF_N):
+        cc.nodes[f] = nodes[f]
+    t0 = time.perf_counter()
+    rc, ref = oracle.Restatement(cc.copy()).stokes_assemble(**ctl)
+    t_port = time.perf_counter() - t0
+    same = rc == 0 and all(np.array_equal(got[k], ref[k], equal_nan=k in ("a", "b"))
+                           for k in ("ia", "ja", "a", "b"))
+    t_ref = None
+    if B.reference_available():
+        t_ref = B.run_reference(cc, stages=B.STOKES_STAGE, stokes=ctl)["stokes"]["seconds"]
+    out_bytes = nnz * 12 + rows * 12
+    print(json.dumps({
+        "metric": "Stokes assembly (preparematrix) equations/s", "unit": "equations/s",
+        "value": rows / (dev_ms * 1e-3), "config": {"workload": f"c2 grid, {rows} equations, "
+                                                                f"{nnz} coefficients"},
+        "device_ms": dev_ms, "e2e": {"value": rows / t_e2e, "unit": "equations/s",
+                                     "ms": t_e2e * 1e3, "d2h_bytes": out_bytes},
+        "csr_output_gbs_device": out_bytes / (dev_ms * 1e-3) / 1e9,
+        "bit_exact_vs_oracle": bool(same),
+        "cpu_oracle_port_1thread": {"value": rows / t_port, "seconds": t_port},
+        "cpu_reference_1thread": ({"value": rows / t_ref, "seconds": t_ref} if t_ref else None),
+    }), flush=True)
+    m.close()
+
+
 def run_c2_parity(args) -> None:
     """Config 2: the reference form (per-marker Newton off) on the C2 grid
     (non-uniform, 1001 x 401 lines, 6.4 M markers) for K steps with dt
@@ -765,6 +834,8 @@ def main():
     ap.add_argument("--c2-parity", action="store_true",
                     help="config 2: per-field error against the reference's routines")
     ap.add_argument("--c2-steps", type=int, default=100)
+    ap.add_argument("--stokes", action="store_true",
+                    help="the Stokes matrix assembly on the C2 grid")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -776,6 +847,9 @@ def main():
     elif args.c2_parity:
         if rank == 0:
             run_c2_parity(args)
+    elif args.stokes:
+        if rank == 0:
+            run_stokes(args)
     else:
         run_gpu(args, rank, world)
 

@@ -360,6 +360,40 @@ int v2c_prn_write(const char *path, const v2c_prn_info *info, const double *rt,
  * order (no float atomics). */
 int v2c_marker_temperature(v2c_ctx *ctx, double heatdif);
 
+/* ====================================================== Stokes assembly
+ * preparematrix [momentum_continuity_addmatrix_checkerror.c:22-213] with
+ * gausmat4_add [gausevps.c:137-214]: the continuity and x/y Stokes
+ * equations of every node (ghost rows, boundary equations, the continuity
+ * form of a vx/vy boundary, the drunken-sailor terms), as the CSR arrays
+ * handed to Pardiso: row 3 m3 + 0 is node m3's pressure (continuity)
+ * equation, + 1 its vx and + 2 its vy equation; ia[3 nodenum + 1] holds
+ * 1-based row starts, ja[nnz] 1-based columns in increasing order within a
+ * row, a[nnz] the coefficients (terms of one column summed in equation
+ * order, zero terms and zero sums left out), b[3 nodenum] the right-hand
+ * side.  Evaluated on the device in FP64 from the device's node fields
+ * (nd, gd, sxxe, nu, gg, sxye, mrx, mvx, mry, mvy, ro; sppe and bm in
+ * compressible mode) and the boundary equations of v2c_set_bonds; FP64
+ * arithmetic in the reference's order, so the arrays equal the reference's
+ * for the same node values.
+ * Pass ja = a = NULL to only count: *nnz receives the number of
+ * coefficients (ia and b are still filled when given).  Returns
+ * V2C_ERR_CAPACITY (with *nnz set) when cap < nnz, V2C_ERR_STATE without
+ * boundary equations, V2C_ERR_UNSUPPORTED where the reference stops
+ * (an inconsistent continuity boundary, addvx/addvy) or where a Stokes or
+ * continuity row would reach past the grid (an edge node without a
+ * boundary equation). */
+typedef struct v2c_stokes_ctl {
+  double mukoef;        /* scale of continuity and boundary rows; the reference
+                           uses dt*30e5 (momentum_continuity_iterate.c:64)  */
+  double dt;            /* time step of the solve, s                        */
+  double gxkoef, gykoef;/* gravity, m/s^2 (GXKOEF, GYKOEF, headevps.c:42)   */
+  double timebond;      /* interior vx boundary equations apply until this
+                           time, s (headevps.c:341)                          */
+  int drunkensailor;    /* [1] free-surface stabilisation terms              */
+} v2c_stokes_ctl;
+int v2c_stokes_assemble(v2c_ctx *ctx, const v2c_stokes_ctl *ctl, long cap, int *ia, int *ja,
+                        double *a, double *b, long *nnz);
+
 /* ========================================================= seismic cycle
  * The seismic-cycle workload (no counterpart in the reference: it stands in
  * for the host Stokes solve with prescribed velocities).  Regime 0
@@ -410,6 +444,7 @@ enum {
   V2C_PROF_TIMESTEP,    /* calc_timestep                                */
   V2C_PROF_B2C,         /* basic2center, center2basic, recompute stress */
   V2C_PROF_TEMP,        /* marker temperature update                    */
+  V2C_PROF_STOKES,      /* Stokes matrix assembly                       */
   V2C_PROF_N
 };
 int v2c_set_profiling(v2c_ctx *ctx, int on);

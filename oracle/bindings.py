@@ -90,6 +90,10 @@ def _lib():
         lib.v2c_oracle_recompute_stress.argtypes = [P(_State), ctypes.c_double]
         lib.v2c_oracle_marker_temperature.restype = ctypes.c_int
         lib.v2c_oracle_marker_temperature.argtypes = [P(_State), ctypes.c_double]
+        lib.v2c_oracle_stokes_assemble.restype = ctypes.c_int
+        lib.v2c_oracle_stokes_assemble.argtypes = [
+            P(_State), P(abi.StokesCtl), ctypes.c_long, P(ctypes.c_int), P(ctypes.c_int),
+            P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_long)]
         lib.v2c_oracle_copyarrays.restype = ctypes.c_int
         lib.v2c_oracle_copyarrays.argtypes = [P(_State)]
         lib.v2c_oracle_center2basic.restype = ctypes.c_int
@@ -181,6 +185,27 @@ class Restatement:
 
     def copyarrays(self):
         return self.lib.v2c_oracle_copyarrays(ctypes.byref(self.st))
+
+    def stokes_assemble(self, **ctl):
+        """preparematrix + gausmat4_add on the current node fields: (rc, dict
+        of ia, ja, a, b as the reference leaves them)."""
+        c = abi.StokesCtl(**ctl)
+        rows = 3 * self.case.nodenum
+        nnz = ctypes.c_long(0)
+        P = ctypes.POINTER
+        rc = self.lib.v2c_oracle_stokes_assemble(ctypes.byref(self.st), ctypes.byref(c), 0, None,
+                                                 None, None, None, ctypes.byref(nnz))
+        if rc:
+            return rc, None
+        ia = np.zeros(rows + 1, dtype=np.int32)
+        ja = np.zeros(max(nnz.value, 1), dtype=np.int32)
+        a = np.zeros(max(nnz.value, 1))
+        b = np.zeros(rows)
+        rc = self.lib.v2c_oracle_stokes_assemble(
+            ctypes.byref(self.st), ctypes.byref(c), nnz.value, ia.ctypes.data_as(P(ctypes.c_int)),
+            ja.ctypes.data_as(P(ctypes.c_int)), a.ctypes.data_as(P(ctypes.c_double)),
+            b.ctypes.data_as(P(ctypes.c_double)), ctypes.byref(nnz))
+        return rc, dict(ia=ia, ja=ja[:nnz.value], a=a[:nnz.value], b=b)
 
     def compute_before_solve(self, dt, rk=0):
         return self.lib.v2c_oracle_compute_before_solve(ctypes.byref(self.st), dt, rk)
@@ -296,10 +321,15 @@ TEMPERATURE_STAGE = 1 << 11
 # save_model (load_save.c:353) after the steps: the result holds the bytes
 # of the restart file the reference wrote ("prn")
 SAVE_STAGE = 1 << 12
+# preparematrix (momentum_continuity_addmatrix_checkerror.c:22) after the
+# steps: the result holds the CSR arrays gausmat4_add built ("stokes": ia,
+# ja, a, b); needs the stokes= argument (v2c_stokes_ctl values)
+STOKES_STAGE = 1 << 13
+STOKES_KEYS = ("mukoef", "dt", "gxkoef", "gykoef", "timebond", "drunkensailor")
 
 
 def write_case(path: str, case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0,
-               timestep=None, oldornew=0, dts=None, heatdif=None) -> None:
+               timestep=None, oldornew=0, dts=None, heatdif=None, stokes=None) -> None:
     """timestep: v2c_timestep_ctl values as a dict (abi.TIMESTEP_DEFAULTS when
     None); oldornew: the argument of calc_timestep (stage bit 6); dts: a
     time step per step (timesum advances after each)."""
@@ -324,12 +354,29 @@ def write_case(path: str, case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=
         ts = dict(abi.TIMESTEP_DEFAULTS, **(timestep or {}))
         np.array([ts["maxtmstep"], ts["dtfactor"], ts["tcnvp"], ts["tcd"], ts["tcphih"],
                   float(oldornew)], dtype=np.float64).tofile(f)
-        if dts is not None or heatdif is not None:
+        if dts is not None or heatdif is not None or stokes is not None:
             d = [] if dts is None else dts
             np.array([len(d)], dtype=np.int64).tofile(f)
             np.ascontiguousarray(d, dtype=np.float64).tofile(f)
-        if heatdif is not None:
-            np.array([heatdif], dtype=np.float64).tofile(f)
+        if heatdif is not None or stokes is not None:
+            np.array([heatdif or 0.0], dtype=np.float64).tofile(f)
+        if stokes is not None:
+            np.array([float(stokes[k]) for k in STOKES_KEYS], dtype=np.float64).tofile(f)
+
+
+def read_csr(path: str) -> dict:
+    """The CSR arrays the harness writes: int64 rows, nnz; int32 ia[rows+1],
+    ja[nnz]; double a[nnz], b[rows]; then (harness only) the seconds the
+    reference's preparematrix took."""
+    with open(path, "rb") as f:
+        rows, nnz = (int(v) for v in np.fromfile(f, dtype=np.int64, count=2))
+        out = dict(ia=np.fromfile(f, dtype=np.int32, count=rows + 1),
+                   ja=np.fromfile(f, dtype=np.int32, count=nnz),
+                   a=np.fromfile(f, dtype=np.float64, count=nnz),
+                   b=np.fromfile(f, dtype=np.float64, count=rows))
+        t = np.fromfile(f, dtype=np.float64, count=1)
+        out["seconds"] = float(t[0]) if t.size else None
+        return out
 
 
 def read_result(path: str, nodenum: int):
@@ -348,7 +395,7 @@ def read_result(path: str, nodenum: int):
 
 
 def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeout=3600,
-                  timestep=None, oldornew=0, dts=None, heatdif=None):
+                  timestep=None, oldornew=0, dts=None, heatdif=None, stokes=None):
     """Run the reference routines on `case`; returns the arrays after the
     stages plus per-stage seconds summed over the timed steps."""
     if not reference_available():
@@ -357,7 +404,8 @@ def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeo
         raise RuntimeError("reference oracle not built (reference sources unavailable)")
     with tempfile.TemporaryDirectory() as d:
         cp, rp = os.path.join(d, "case.bin"), os.path.join(d, "res.bin")
-        write_case(cp, case, stages, nthreads, nsteps, warmup, timestep, oldornew, dts, heatdif)
+        write_case(cp, case, stages, nthreads, nsteps, warmup, timestep, oldornew, dts, heatdif,
+                   stokes)
         env = dict(os.environ, OMP_NUM_THREADS=str(max(1, nthreads)))
         r = subprocess.run([reference_path(), cp, rp], env=env, capture_output=True,
                            timeout=timeout, cwd=d)
@@ -367,4 +415,6 @@ def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeo
         if stages & SAVE_STAGE:
             with open(os.path.join(d, "state.prn"), "rb") as f:
                 res["prn"] = f.read()
+        if stages & STOKES_STAGE:
+            res["stokes"] = read_csr(os.path.join(d, "stokes.bin"))
         return res

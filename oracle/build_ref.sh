@@ -32,11 +32,11 @@ temperature_iterate.c plastic.c recalc_marker_properties.c load_save.c"
 if [ -d "$REF/src" ]; then
   mkdir -p "$OUT/src"
   for f in $FILES; do cp "$REF/src/$f" "$OUT/src/$f"; done
-  # grid up to 1100 x 420 lines, 2.1 M markers; the Stokes matrix arrays are
-  # only used by the small boundary-correction solves on this path.
+  # grid up to 1100 x 420 lines, 6.5 M markers; the Stokes matrix arrays
+  # (MAXVAL coefficients) hold the assembly of a 1001 x 401 grid.
   sed -i \
     -e 's/^#define MAXMAT .*/#define MAXMAT  8000000/' \
-    -e 's/^#define MAXVAL .*/#define MAXVAL  8000000/' \
+    -e 's/^#define MAXVAL .*/#define MAXVAL  24000000/' \
     -e 's/^#define MAXXLN .*/#define MAXXLN  1100/' \
     -e 's/^#define MAXYLN .*/#define MAXYLN  420/' \
     -e 's/^#define MAXMRK .*/#define MAXMRK  6500001/' \

@@ -46,6 +46,8 @@ typedef struct {
   long ndts;               /* per-step time steps (optional trailer), 0 if none */
   double *dts;
   double heatdif;          /* solve_temperature's subgrid diffusion (optional trailer) */
+  double stokes[6];        /* preparematrix (stage bit 13, optional trailer): mukoef, dt,
+                              GXKOEF, GYKOEF, timebond, drunkensailor */
   v2c_timestep_info info;  /* calc_timestep results (stage bit 6) */
   long ts_rc;              /* 0, or 1 when chi == 0 stopped it */
 } ref_case;
@@ -121,6 +123,8 @@ static int ref_load_case(const char *path, ref_case *C) {
   }
   C->heatdif = 0;
   if (fread(&C->heatdif, sizeof(double), 1, f) != 1) C->heatdif = 0;
+  memset(C->stokes, 0, sizeof(C->stokes));
+  if (fread(C->stokes, sizeof(double), 6, f) != 6) memset(C->stokes, 0, sizeof(C->stokes));
   memset(&C->info, 0, sizeof(C->info));
   C->ts_rc = 0;
   fclose(f);

@@ -12,7 +12,8 @@
  *   interpolate_center2basic, copyarrays (stage bits 7, 9, 8, 10),
  *   compute_after_solve, nodes2markers, moveandrotatemarkers, calc_timestep
  * and writes the arrays back; with stage bit 12 it also runs save_model,
- * which writes the restart file state.prn into the working directory.
+ * which writes the restart file state.prn into the working directory, and
+ * with bit 13 preparematrix, whose CSR arrays go to stokes.bin there.
  * Stdout (the reference's progress prints) is discarded.
  *
  * Case file (native endianness), written by oracle/bindings.py:
@@ -24,6 +25,8 @@
  *   int64 bondm[nodenum*4], bondn[bondnum*3]; double bondv[bondnum*4]
  *   double ts[6]; optional: int64 ndts, double dts[ndts] (per-step dt),
  *   double heatdif (stage bit 11: solve_temperature, new temperatures in tk2)
+ *   double stokes[6] (stage bit 13: preparematrix's mukoef, dt and GXKOEF,
+ *   GYKOEF, timebond, drunkensailor)
  * Result file:
  *   char magic[8] = "V2CRES01"; int64 n
  *   double node[V2C_NF_N][nodenum], mark[V2C_MF_N][n]; int8 markt[n]
@@ -143,6 +146,28 @@ int main(int argc, char **argv) {
     if (step < C.ndts) timesum += timestep;
   }
 
+  if (stages & (1 << 13)) {
+    /* preparematrix (momentum_continuity_addmatrix_checkerror.c:22-38) of
+     * the state after the steps; the CSR arrays gausmat4_add leaves for
+     * Pardiso go to stokes.bin in the working directory:
+     * int64 rows, nnz; int32 ia[rows+1], ja[nnz]; double a[nnz], b[rows] */
+    GXKOEF = C.stokes[2]; GYKOEF = C.stokes[3]; timebond = C.stokes[4];
+    drunkensailor = (int)C.stokes[5];
+    pos0cur = 0;
+    const double t0s = omp_get_wtime();
+    preparematrix(C.stokes[0], C.stokes[1], 0);
+    const double ts = omp_get_wtime() - t0s;
+    FILE *o = fopen("stokes.bin", "wb");
+    if (!o) return 6;
+    int64_t hdr[2] = {nodenum3, pos0cur};
+    wr(hdr, sizeof(int64_t), 2, o);
+    wr(ia, sizeof(int), nodenum3 + 1, o);
+    wr(ja, sizeof(int), pos0cur, o);
+    wr(a, sizeof(double), pos0cur, o);
+    wr(b, sizeof(double), nodenum3, o);
+    wr(&ts, sizeof(double), 1, o);
+    fclose(o);
+  }
   if (stages & (1 << 12)) {
     /* save_model (load_save.c:353-527) of the state after the steps, into
      * the working directory as state.prn (it also writes file.t3c and

@@ -1831,3 +1831,287 @@ void v2c_oracle_mlp_forward(const float *P, const double *X, long n, double *Y) 
   }
 }
 #undef H
+
+/* ------------------------------------------------------- Stokes assembly
+ * preparematrix (momentum_continuity_addmatrix_checkerror.c:22-213) with
+ * contadd (:932-998), xstoksadd (:642-731), ystoksadd (:794-877),
+ * sxxcalc_prepare (:395-443), sxycalc_prepare (:483-525), bondadd
+ * (:192-211), and the row layout of gausmat4_add (gausevps.c:137-214).
+ * Where the reference calls exit(0) (an inconsistent continuity boundary)
+ * or would index past the grid (an edge node without a boundary equation)
+ * this returns V2C_ERR_UNSUPPORTED. */
+#define SK_MAXT 24
+typedef struct {
+  double c;
+  int n;
+  long col[SK_MAXT];
+  double w[SK_MAXT];
+} sk_eq;
+
+static void sk_add(sk_eq *E, long k, double v) {
+  if (E->n < SK_MAXT) {
+    E->col[E->n] = k;
+    E->w[E->n] = v;
+  }
+  E->n++;
+}
+
+typedef struct {
+  const v2c_oracle_state *s;
+  const v2c_stokes_ctl *c;
+  long xn, yn, nn;
+  int bad;
+} sk_ctx;
+
+static void sk_sxx(sk_ctx *K, sk_eq *E, long m1, long m2, double ynval) {
+  const v2c_oracle_state *s = K->s;
+  long yn = K->yn;
+  long v0 = (m1 - 1) * yn + (m2 - 1), v1 = v0 + 1, v2 = v0 + yn, v3 = v2 + 1;
+  double sxxeeff = s->N[V2C_NF_SXXE][v3], Z;
+  double nueff = nueff_of(&s->p, s->N[V2C_NF_ND][v3], s->N[V2C_NF_GD][v3], K->c->dt, &Z);
+  sk_add(E, v0 * 3 + 1, -ynval * nueff / (s->gx[m1] - s->gx[m1 - 1]));
+  sk_add(E, v2 * 3 + 1, +ynval * nueff / (s->gx[m1] - s->gx[m1 - 1]));
+  sk_add(E, v0 * 3 + 2, +ynval * nueff / (s->gy[m2] - s->gy[m2 - 1]));
+  sk_add(E, v1 * 3 + 2, -ynval * nueff / (s->gy[m2] - s->gy[m2 - 1]));
+  E->c -= (1.0 - Z) * ynval * sxxeeff;
+}
+
+static void sk_sxy(sk_ctx *K, sk_eq *E, long m1, long m2, double ynval) {
+  const v2c_oracle_state *s = K->s;
+  long yn = K->yn;
+  long v0 = (m1 - 1) * yn + (m2 - 1), v1 = v0 + 1, v2 = v0 + yn, v3 = v2 + 1;
+  double sxyeeff = s->N[V2C_NF_SXYE][v3], Z;
+  double nueff = nueff_of(&s->p, s->N[V2C_NF_NU][v3], s->N[V2C_NF_GG][v3], K->c->dt, &Z);
+  sk_add(E, v2 * 3 + 1, -ynval * 2.0 * nueff / (s->gy[m2 + 1] - s->gy[m2 - 1]));
+  sk_add(E, v3 * 3 + 1, +ynval * 2.0 * nueff / (s->gy[m2 + 1] - s->gy[m2 - 1]));
+  sk_add(E, v1 * 3 + 2, -ynval * 2.0 * nueff / (s->gx[m1 + 1] - s->gx[m1 - 1]));
+  sk_add(E, v3 * 3 + 2, +ynval * 2.0 * nueff / (s->gx[m1 + 1] - s->gx[m1 - 1]));
+  E->c -= (1.0 - Z) * ynval * sxyeeff;
+}
+
+static void sk_cont(sk_ctx *K, sk_eq *E, long m1, long m2) {
+  const v2c_oracle_state *s = K->s;
+  long yn = K->yn;
+  long v0 = (m1 - 1) * yn + (m2 - 1), v1 = v0 + 1, v2 = v0 + yn, v3 = v2 + 1;
+  E->n = 0;
+  E->c = 0;
+  if (s->p.compressiblemode == 1)
+    E->c = s->N[V2C_NF_SPPE][v3] / s->N[V2C_NF_BM][v3] / s->p.timestep;
+  sk_add(E, v0 * 3 + 1, -1.0 / (s->gx[m1] - s->gx[m1 - 1]));
+  sk_add(E, v2 * 3 + 1, +1.0 / (s->gx[m1] - s->gx[m1 - 1]));
+  sk_add(E, v0 * 3 + 2, -1.0 / (s->gy[m2] - s->gy[m2 - 1]));
+  sk_add(E, v1 * 3 + 2, +1.0 / (s->gy[m2] - s->gy[m2 - 1]));
+  if (s->p.compressiblemode == 1)
+    sk_add(E, v3 * 3 + 0, 1.0 / s->N[V2C_NF_BM][v3] / s->p.timestep);
+}
+
+static void sk_bond(sk_ctx *K, sk_eq *E, long r) {
+  const v2c_oracle_state *s = K->s;
+  long B = s->bondm[r];
+  E->n = 0;
+  E->c = s->bondv[B * 4 + 0];
+  sk_add(E, r, 1.0);
+  for (int k = 0; k < 3; k++) {
+    long bn = s->bondn[B * 3 + k];
+    if (bn) {
+      if (bn - 1 < 0 || bn - 1 >= 3 * K->nn) K->bad = 1;
+      sk_add(E, bn - 1, -s->bondv[B * 4 + k + 1]);
+    }
+  }
+}
+
+static void sk_xstokes(sk_ctx *K, sk_eq *E, long m1, long m2) {
+  const v2c_oracle_state *s = K->s;
+  const double *gx = s->gx, *gy = s->gy, *ro = s->N[V2C_NF_RO];
+  double dt = K->c->dt, GX = K->c->gxkoef;
+  int inertyn = s->p.inertyn;
+  long yn = K->yn;
+  long v0 = m1 * yn + m2, v1 = v0 + 1, v2 = v0 + yn, v3 = v2 + 1;
+  double xkf = (gx[m1 + 1] - gx[m1 - 1]) / 2.0, ykf = gy[m2 + 1] - gy[m2];
+  E->n = 0;
+  E->c = (-GX - inertyn * s->N[V2C_NF_MVX][v0] / dt) * s->N[V2C_NF_MRX][v0];
+  sk_add(E, v1 * 3 + 0, +1.0 / xkf);
+  sk_add(E, v3 * 3 + 0, -1.0 / xkf);
+  sk_add(E, v0 * 3 + 1, -inertyn * s->N[V2C_NF_MRX][v0] / dt);
+  sk_sxx(K, E, m1, m2 + 1, -1.0 / xkf);
+  sk_sxx(K, E, m1 + 1, m2 + 1, 1.0 / xkf);
+  sk_sxy(K, E, m1, m2, -1.0 / ykf);
+  sk_sxy(K, E, m1, m2 + 1, 1.0 / ykf);
+  if (K->c->drunkensailor == 1) {
+    sk_add(E, v0 * 3 + 1,
+           -dt / 2.0 * GX * (ro[v2] + ro[v3] - ro[v0 - yn] - ro[v1 - yn]) /
+               (gx[m1 + 1] - gx[m1 - 1]) / 2.0);
+    sk_add(E, v0 * 3 + 2,
+           -dt / 2.0 * GX * (gx[m1] - gx[m1 - 1]) / (gx[m1 + 1] - gx[m1 - 1]) / 2.0 *
+               (ro[v1] - ro[v0]) / (gy[m2 + 1] - gy[m2]));
+    sk_add(E, v1 * 3 + 2,
+           -dt / 2.0 * GX * (gx[m1] - gx[m1 - 1]) / (gx[m1 + 1] - gx[m1 - 1]) / 2.0 *
+               (ro[v1] - ro[v0]) / (gy[m2 + 1] - gy[m2]));
+    sk_add(E, (v0 - yn) * 3 + 2,
+           -dt / 2.0 * GX * (gx[m1 + 1] - gx[m1]) / (gx[m1 + 1] - gx[m1 - 1]) / 2.0 *
+               (ro[v1] - ro[v0]) / (gy[m2 + 1] - gy[m2]));
+    sk_add(E, (v1 - yn) * 3 + 2,
+           -dt / 2.0 * GX * (gx[m1 + 1] - gx[m1]) / (gx[m1 + 1] - gx[m1 - 1]) / 2.0 *
+               (ro[v1] - ro[v0]) / (gy[m2 + 1] - gy[m2]));
+  }
+}
+
+static void sk_ystokes(sk_ctx *K, sk_eq *E, long m1, long m2) {
+  const v2c_oracle_state *s = K->s;
+  const double *gx = s->gx, *gy = s->gy, *ro = s->N[V2C_NF_RO];
+  double dt = K->c->dt, GY = K->c->gykoef;
+  int inertyn = s->p.inertyn;
+  long yn = K->yn;
+  long v0 = m1 * yn + m2, v1 = v0 + 1, v2 = v0 + yn, v3 = v2 + 1;
+  double xkf = gx[m1 + 1] - gx[m1], ykf = (gy[m2 + 1] - gy[m2 - 1]) / 2.0;
+  E->n = 0;
+  E->c = (-GY - inertyn * s->N[V2C_NF_MVY][v0] / dt) * s->N[V2C_NF_MRY][v0];
+  sk_add(E, v2 * 3 + 0, +1.0 / ykf);
+  sk_add(E, v3 * 3 + 0, -1.0 / ykf);
+  sk_add(E, v0 * 3 + 2, -inertyn * s->N[V2C_NF_MRY][v0] / dt);
+  sk_sxx(K, E, m1 + 1, m2, 1.0 / ykf);
+  sk_sxx(K, E, m1 + 1, m2 + 1, -1.0 / ykf);
+  sk_sxy(K, E, m1, m2, -1.0 / xkf);
+  sk_sxy(K, E, m1 + 1, m2, 1.0 / xkf);
+  if (K->c->drunkensailor == 1) {
+    sk_add(E, v0 * 3 + 2,
+           -dt / 2.0 * GY * (ro[v1] + ro[v3] - ro[v0 - 1] - ro[v2 - 1]) /
+               (gy[m2 + 1] - gy[m2 - 1]) / 2.0);
+    sk_add(E, v0 * 3 + 1,
+           -dt / 2.0 * GY * (gy[m2] - gy[m2 - 1]) / (gy[m2 + 1] - gy[m2 - 1]) / 2.0 *
+               (ro[v2] - ro[v0]) / (gx[m1 + 1] - gx[m1]));
+    sk_add(E, v2 * 3 + 1,
+           -dt / 2.0 * GY * (gy[m2] - gy[m2 - 1]) / (gy[m2 + 1] - gy[m2 - 1]) / 2.0 *
+               (ro[v2] - ro[v0]) / (gx[m1 + 1] - gx[m1]));
+    sk_add(E, (v0 - 1) * 3 + 1,
+           -dt / 2.0 * GY * (gy[m2 + 1] - gy[m2]) / (gy[m2 + 1] - gy[m2 - 1]) / 2.0 *
+               (ro[v2] - ro[v0]) / (gx[m1 + 1] - gx[m1]));
+    sk_add(E, (v2 - 1) * 3 + 1,
+           -dt / 2.0 * GY * (gy[m2 + 1] - gy[m2]) / (gy[m2 + 1] - gy[m2 - 1]) / 2.0 *
+               (ro[v2] - ro[v0]) / (gx[m1 + 1] - gx[m1]));
+  }
+}
+
+/* the continuity form of a vx (k = 2) or vy (k = 3) boundary, addvx
+ * :92-108 / addvy :150-166 */
+static int sk_cont_bond(sk_ctx *K, sk_eq *E, long r, long m1, long m2, int k) {
+  const v2c_oracle_state *s = K->s;
+  long B = s->bondm[r], ref = s->bondn[B * 3 + 0];
+  long m3 = (ref - 1 - r) / 3, dm1 = 0, dm2 = 0;
+  if (m3 >= K->yn) dm1 = 1;
+  if (m3 == 1 || m3 > K->yn) dm2 = 1;
+  if (m3 < 0 || m3 > K->yn + 1 || !(m1 + dm1) || !(m2 + dm2) || ref - k < 0 ||
+      ref - k >= 4 * K->nn || !s->bondm[ref - k])
+    return 0;
+  if (m1 + dm1 > K->xn - 1 || m2 + dm2 > K->yn - 1) return 0;
+  sk_cont(K, E, m1 + dm1, m2 + dm2);
+  return 1;
+}
+
+static int sk_build(sk_ctx *K, long r, sk_eq *E) {
+  const v2c_oracle_state *s = K->s;
+  long m3 = r / 3, kind = r % 3, m2 = m3 % K->yn, m1 = (m3 - m2) / K->yn;
+  long xn = K->xn, yn = K->yn;
+  int scale = 1;
+  E->n = 0;
+  E->c = 0;
+  if (kind == 0) { /* addcont */
+    if (m1 && m2) {
+      if (!s->bondm[r] || s->p.compressiblemode == 1) sk_cont(K, E, m1, m2);
+      else sk_bond(K, E, r);
+    } else {
+      sk_add(E, r, 1.0);
+    }
+  } else if (kind == 1) { /* addvx */
+    if (m2 < yn - 1) {
+      if (!s->bondm[r] ||
+          (s->p.timesum > K->c->timebond && m1 > 2 && m2 > 2 && m1 < xn - 4 && m2 < yn - 3)) {
+        if (m1 < 1 || m1 > xn - 2 || m2 < 1 || m2 > yn - 3) return 0;
+        sk_xstokes(K, E, m1, m2);
+        scale = 0;
+      } else if (s->bondv[s->bondm[r] * 4 + 1] > 1e+30) {
+        if (!sk_cont_bond(K, E, r, m1, m2, 2)) return 0;
+      } else {
+        sk_bond(K, E, r);
+      }
+    } else {
+      sk_add(E, r, 1.0);
+    }
+  } else { /* addvy */
+    if (m1 < xn - 1) {
+      if (!s->bondm[r]) {
+        if (m1 < 1 || m1 > xn - 3 || m2 < 1 || m2 > yn - 2) return 0;
+        sk_ystokes(K, E, m1, m2);
+        scale = 0;
+      } else if (s->bondv[s->bondm[r] * 4 + 1] > 1e+30) {
+        if (!sk_cont_bond(K, E, r, m1, m2, 3)) return 0;
+      } else {
+        sk_bond(K, E, r);
+      }
+    } else {
+      sk_add(E, r, 1.0);
+    }
+  }
+  if (E->n > SK_MAXT) return 0;
+  if (scale) {
+    E->c *= K->c->mukoef;
+    for (int i = 0; i < E->n; i++) E->w[i] *= K->c->mukoef;
+  }
+  return 1;
+}
+
+int v2c_oracle_stokes_assemble(const v2c_oracle_state *s, const v2c_stokes_ctl *c, long cap,
+                               int *ia, int *ja, double *a, double *b, long *nnz) {
+  sk_ctx K = {s, c, s->p.xnumx, s->p.ynumy, s->p.xnumx * s->p.ynumy, 0};
+  long rows = 3 * K.nn, pos = 0;
+  if (!s->bondm) return V2C_ERR_STATE;
+  /* gausmat4_add's column buffer: bufv[] and the marks cur0[] */
+  double *bufv = calloc((size_t)rows, sizeof(double));
+  char *cur0 = calloc((size_t)rows, 1);
+  if (!bufv || !cur0) {
+    free(bufv);
+    free(cur0);
+    return V2C_ERR_CAPACITY;
+  }
+  int rc = V2C_OK;
+  for (long r = 0; r < rows; r++) {
+    sk_eq E;
+    if (!sk_build(&K, r, &E) || K.bad) {
+      rc = V2C_ERR_UNSUPPORTED;
+      break;
+    }
+    long lo = rows, hi = -1;
+    for (int i = 0; i < E.n; i++)
+      if (E.w[i]) {
+        bufv[E.col[i]] = 0.0;
+        cur0[E.col[i]] = 1;
+      }
+    for (int i = 0; i < E.n; i++)
+      if (E.w[i]) {
+        if (E.col[i] < lo) lo = E.col[i];
+        if (E.col[i] > hi) hi = E.col[i];
+        bufv[E.col[i]] += E.w[i];
+      }
+    if (b) b[r] = E.c;
+    if (ia) ia[r] = (int)(pos + 1);
+    for (long k = lo; k <= hi; k++)
+      if (cur0[k]) {
+        if (bufv[k]) {
+          if (ja && pos < cap) {
+            ja[pos] = (int)(k + 1);
+            a[pos] = bufv[k];
+          }
+          pos++;
+        }
+        bufv[k] = 0.0;
+        cur0[k] = 0;
+      }
+  }
+  if (ia && rc == V2C_OK) ia[rows] = (int)(pos + 1);
+  free(bufv);
+  free(cur0);
+  *nnz = pos;
+  if (rc == V2C_OK && ja && pos > cap) rc = V2C_ERR_CAPACITY;
+  return rc;
+}
+#undef SK_MAXT

@@ -48,6 +48,9 @@ int v2c_oracle_basic2center(v2c_oracle_state *s);
 int v2c_oracle_recompute_stress(v2c_oracle_state *s, double dt);
 int v2c_oracle_copyarrays(v2c_oracle_state *s);
 int v2c_oracle_marker_temperature(v2c_oracle_state *s, double heatdif);
+/* preparematrix + gausmat4_add: the Stokes matrix as CSR (1-based ia, ja) */
+int v2c_oracle_stokes_assemble(const v2c_oracle_state *s, const v2c_stokes_ctl *c, long cap,
+                               int *ia, int *ja, double *a, double *b, long *nnz);
 int v2c_oracle_compute_before_solve(v2c_oracle_state *s, double dt, int rk);
 double v2c_oracle_compute_after_solve(v2c_oracle_state *s, double dt, int rk);
 int v2c_oracle_nodes2markers(v2c_oracle_state *s);

@@ -5,8 +5,11 @@
  * and interpolate_center2basic between the node updates, as the Picard loop
  * calls them), writes the result,
  * restores the initial globals, runs the same step through the binding
- * (GPU) and writes that result.
- *   bind_check <case.bin> <ref_result.bin> <bind_result.bin>
+ * (GPU) and writes that result.  With two more paths it also assembles the
+ * Stokes matrix after interpolate_basic2center (preparematrix, its scalars
+ * from the case's stokes trailer) on both sides and writes the CSR arrays
+ * (int64 rows, nnz; int32 ia, ja; double a, b).
+ *   bind_check <case.bin> <ref_result.bin> <bind_result.bin> [ref.csr bind.csr]
  * Compiled against the reference sources staged by oracle/build_ref.sh.
  */
 #ifndef _GNU_SOURCE
@@ -63,6 +66,19 @@ static void restore_arrays(const double *s, long nn, long n) {
   memcpy(markt, p, n + 1);
 }
 
+static int write_csr(const char *path) {
+  FILE *o = fopen(path, "wb");
+  if (!o) return 2;
+  int64_t hdr[2] = {nodenum3, pos0cur};
+  wr(hdr, sizeof(int64_t), 2, o);
+  wr(ia, sizeof(int), nodenum3 + 1, o);
+  wr(ja, sizeof(int), pos0cur, o);
+  wr(a, sizeof(double), pos0cur, o);
+  wr(b, sizeof(double), nodenum3, o);
+  fclose(o);
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc < 4) { fprintf(stderr, "usage: bind_check case ref_out bind_out\n"); return 2; }
   ref_case C;
@@ -74,10 +90,18 @@ int main(int argc, char **argv) {
   FILE *keep = stdout;
   if (!freopen("/dev/null", "w", stdout)) return 5;
 
+  const int csr = argc >= 6;
+  GXKOEF = C.stokes[2]; GYKOEF = C.stokes[3]; timebond = C.stokes[4];
+  drunkensailor = (int)C.stokes[5];
   marker2nodes();
   interpolate_center2basic_old(timestep);
   compute_before_solve(timestep, 0);
   interpolate_basic2center();
+  if (csr) {
+    pos0cur = 0;
+    preparematrix(C.stokes[0], C.stokes[1], 0);
+    if (write_csr(argv[4])) return 2;
+  }
   interpolate_center2basic(timestep);
   double d_ref = compute_after_solve(timestep, 0);
   nodes2markers();
@@ -91,6 +115,11 @@ int main(int argc, char **argv) {
   v2c_bind_interpolate_center2basic_old(timestep);
   v2c_bind_compute_before_solve(timestep, 0);
   v2c_bind_interpolate_basic2center();
+  if (csr) {
+    pos0cur = 0;
+    v2c_bind_preparematrix(C.stokes[0], C.stokes[1], 0);
+    if (write_csr(argv[5])) return 2;
+  }
   v2c_bind_interpolate_center2basic(timestep);
   double d_bind = v2c_bind_compute_after_solve(timestep, 0);
   v2c_bind_nodes2markers();

@@ -63,6 +63,43 @@ def temperature_case(seed, name="small"):
     return c, told, tnew
 
 
+def stokes_case(seed, name="tiny", variant="default"):
+    """(case, ctl) for the Stokes assembly: node fields of the oracle's
+    marker2nodes, compute_before_solve and basic2center, rounded to FP32
+    (what the device holds) and kept as FP64, so that the device, the
+    restatement and the reference all see the same values.  Variants:
+    'no_sailor' (drunkensailor 0), 'inertia' (inertyn 1), 'compressible'
+    (compressiblemode 1), 'cont_bond' (the vx boundary of node (0, 0) given
+    as the continuity equation of cell (1, 1), addvx's bondv > 1e30 form),
+    'open_edge' (a left-edge vx node without a boundary equation: the
+    reference would read past the grid)."""
+    import oracle
+    from velo2cycles_gb300 import synth
+    kw = {"inertia": dict(inertyn=1), "compressible": dict(compressiblemode=1)}.get(variant, {})
+    c = synth.make_case(name, seed, **kw)
+    dt = float(c.params["timestep"])
+    r = oracle.Restatement(c.copy())
+    r.marker2nodes()
+    r.compute_before_solve(dt, 0)
+    r.basic2center()
+    for f in range(abi.NF_N):
+        c.nodes[f] = np.asarray(r.nodes[f], dtype=np.float32).astype(np.float64)
+    c.bondn, c.bondv = c.bondn.copy(), c.bondv.copy()
+    yn = c.gy.size
+    if variant == "cont_bond":
+        b = int(c.bondm[1])
+        c.bondn[b * 3 + 0] = 3 * yn + 5   # the vx unknown of node (1, 1), 1-based
+        c.bondv[b * 4 + 1] = 2e30
+    if variant == "open_edge":
+        c.bondm = c.bondm.copy()
+        c.bondm[(0 * yn + 3) * 3 + 1] = 0
+    from velo2cycles_gb300 import abi as _abi
+    ctl = dict(_abi.STOKES_DEFAULTS, mukoef=dt * 30e5, dt=dt)
+    if variant == "no_sailor":
+        ctl["drunkensailor"] = 0
+    return c, ctl
+
+
 def rel_err(a: np.ndarray, b: np.ndarray) -> float:
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)

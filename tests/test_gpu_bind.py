@@ -51,8 +51,19 @@ def test_binding_step_matches_reference(bind_check):
     exe, d = bind_check
     c = synth.make_case("small", seed=17)
     case, r_ref, r_bind = str(d / "case.bin"), str(d / "ref.bin"), str(d / "bind.bin")
-    B.write_case(case, c)
-    subprocess.run([exe, case, r_ref, r_bind], check=True, timeout=600)
+    csr_ref, csr_bind = str(d / "ref.csr"), str(d / "bind.csr")
+    dt = float(c.params["timestep"])
+    B.write_case(case, c, stokes=dict(abi.STOKES_DEFAULTS, mukoef=dt * 30e5, dt=dt))
+    subprocess.run([exe, case, r_ref, r_bind, csr_ref, csr_bind], check=True, timeout=600)
+    # preparematrix through the binding: the same sparsity, coefficients
+    # within the FP32 storage of the device's node fields
+    sr, sb = B.read_csr(csr_ref), B.read_csr(csr_bind)
+    assert np.array_equal(sb["ia"], sr["ia"]) and np.array_equal(sb["ja"], sr["ja"])
+    row = np.repeat(np.arange(sr["ia"].size - 1), np.diff(sr["ia"]))
+    scale = np.zeros(sr["ia"].size - 1)
+    np.maximum.at(scale, row, np.abs(sr["a"]))
+    assert (np.abs(sb["a"] - sr["a"]) <= 1e-6 * scale[row]).all()  # per row
+    assert rel_err(sb["b"], sr["b"]) <= 1e-6
     ref = B.read_result(r_ref, c.nodenum)
     got = B.read_result(r_bind, c.nodenum)
     names = abi.node_field_names()

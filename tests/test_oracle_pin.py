@@ -19,7 +19,7 @@ import oracle
 from oracle import bindings as B
 from velo2cycles_gb300 import abi, synth
 
-from .parity import temperature_case
+from .parity import stokes_case, temperature_case
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ref_micro.npz")
 
@@ -175,6 +175,30 @@ def test_marker_temperature_bit_exact_vs_reference(heatdif):
     assert np.array_equal(ref["nodes"][abi.NF_TK], tnew)
     assert not _compare(r, ref["nodes"], ref["marks"])
     assert not np.array_equal(r.marks[abi.MF_K], c.marks[abi.MF_K])
+
+
+@needs_ref
+@pytest.mark.parametrize("variant", ["default", "no_sailor", "inertia", "compressible",
+                                     "cont_bond"])
+def test_stokes_assembly_bit_exact_vs_reference(variant):
+    """preparematrix + gausmat4_add (momentum_continuity_addmatrix_checkerror.c
+    :22-213, gausevps.c:137-214): the reference's own assembly of the CSR
+    arrays against the restatement, on node fields from the MIC step."""
+    c, ctl = stokes_case(5, variant=variant)
+    ref = B.run_reference(c, stages=B.STOKES_STAGE, stokes=ctl)["stokes"]
+    rc, ours = oracle.Restatement(c.copy()).stokes_assemble(**ctl)
+    assert rc == 0
+    for k in ("ia", "ja", "a", "b"):
+        assert np.array_equal(ours[k], ref[k], equal_nan=k in ("a", "b")), k
+    assert ref["ja"].size > 10 * c.nodenum
+
+
+def test_stokes_assembly_open_edge_is_refused():
+    """A Stokes row on the model's edge would index past the grid in the
+    reference; the restatement refuses it."""
+    c, ctl = stokes_case(5, variant="open_edge")
+    rc, _ = oracle.Restatement(c.copy()).stokes_assemble(**ctl)
+    assert rc == abi.ERR_UNSUPPORTED
 
 
 def test_nxsearch_ties_and_clamps():

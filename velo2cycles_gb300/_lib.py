@@ -44,6 +44,8 @@ _SIGS = {
     "v2c_recompute_stress_strainrate": [c_ctx, ctypes.c_double],
     "v2c_copyarrays": [c_ctx],
     "v2c_marker_temperature": [c_ctx, ctypes.c_double],
+    "v2c_stokes_assemble": [c_ctx, P(abi.StokesCtl), ctypes.c_long, P(ctypes.c_int),
+                            P(ctypes.c_int), c_dp, c_dp, P(ctypes.c_long)],
     "v2c_prn_read_info": [ctypes.c_char_p, P(abi.PrnInfo)],
     "v2c_prn_read": [ctypes.c_char_p, P(abi.PrnInfo), c_dp, c_dp, P(c_dp), P(ctypes.c_long),
                      c_dp, c_dp, c_dp, P(ctypes.c_long), P(c_dp), P(ctypes.c_byte)],

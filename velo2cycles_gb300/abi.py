@@ -125,6 +125,16 @@ class TimestepInfo(ctypes.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class StokesCtl(ctypes.Structure):
+    """v2c_stokes_ctl: the scalars of preparematrix that are not parameters."""
+    _fields_ = _struct_fields("v2c_stokes_ctl")
+
+
+# the reference's values: drunkensailor = 1 (headevps.c:288); mukoef = dt*30e5
+# (momentum_continuity_iterate.c:64) is set per call
+STOKES_DEFAULTS = dict(gxkoef=0.0, gykoef=9.81, timebond=0.0, drunkensailor=1)
+
+
 class PrnInfo(ctypes.Structure):
     """v2c_prn_info: the header of a restart file."""
     _fields_ = _struct_fields("v2c_prn_info")

@@ -201,6 +201,23 @@ void v2c_bind_marker_temperature(void) {
   if (v2c_bind_sync_markers) v2c_bind_markers_to_host();
 }
 
+/* preparematrix (momentum_continuity_addmatrix_checkerror.c:22-38): the
+ * Stokes matrix assembled on the device into the reference's Pardiso
+ * arrays ia, ja, a, b and pos0cur, as gausmat4_add leaves them */
+void v2c_bind_preparematrix(double mukoef, double dt, int rk) {
+  (void)rk;
+  if (!v2c_bind_setup() || !v2c_bind_nodes_up()) return;
+  v2c_stokes_ctl c = {mukoef, dt, GXKOEF, GYKOEF, timebond, drunkensailor};
+  long nnz = 0;
+  int rc = v2c_stokes_assemble(v2c_bind_ctx, &c, MAXVAL, ia, ja, a, b, &nnz);
+  if (rc == V2C_ERR_CAPACITY) { /* the reference's own limit */
+    printf("EXIT PROGRAM: Space out in a[] %ld", nnz);
+    exit(0);
+  }
+  if (!v2c_bind_ok(rc, "v2c_stokes_assemble")) return;
+  pos0cur = nnz;
+}
+
 void v2c_bind_compute_before_solve(double dt, int rk) {
   if (!v2c_bind_setup() || !v2c_bind_nodes_up()) return;
   if (!v2c_bind_ok(v2c_compute_before_solve(v2c_bind_ctx, dt, rk), "v2c_compute_before_solve"))

@@ -17,6 +17,7 @@
  *   calc_timestep(oldornew)              -> v2c_bind_calc_timestep(oldornew)
  *                                           (momentum_continuity_iterate.c:44,92)
  *   interpolate_basic2center()           -> v2c_bind_interpolate_basic2center()
+ *   preparematrix(mukoef, dt, rk)        -> v2c_bind_preparematrix(mukoef, dt, rk)
  *   interpolate_center2basic(dt)         -> v2c_bind_interpolate_center2basic(dt)
  *                                           (momentum_continuity_iterate.c:71,87)
  *
@@ -44,6 +45,7 @@ extern int v2c_bind_sync_markers;
 void v2c_bind_marker2nodes(void);
 double v2c_bind_interpolate_center2basic_old(double dt);
 void v2c_bind_compute_before_solve(double dt, int rk);
+void v2c_bind_preparematrix(double mukoef, double dt, int rk);
 double v2c_bind_compute_after_solve(double dt, int rk);
 double v2c_bind_nodes2markers(void);
 void v2c_bind_moveandrotatemarkers(void);

@@ -1055,6 +1055,117 @@ extern "C" int v2c_marker_temperature(v2c_ctx *ctx, double heatdif) {
   return V2C_OK;
 }
 
+// ====================================================== Stokes assembly
+namespace {
+// device memory of one call, freed on every return path
+struct DevBuf {
+  void *p = nullptr;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  template <class T>
+  cudaError_t alloc(long n) {
+    return cudaMalloc(&p, sizeof(T) * (size_t)(n > 0 ? n : 1));
+  }
+  template <class T>
+  T *get() const {
+    return static_cast<T *>(p);
+  }
+};
+}  // namespace
+
+extern "C" int v2c_stokes_assemble(v2c_ctx *ctx, const v2c_stokes_ctl *ctl, long cap, int *ia,
+                                   int *ja, double *a, double *b, long *nnz) {
+  if (!ctx || !ctl || !nnz || cap < 0 || (ja == nullptr) != (a == nullptr)) return V2C_ERR_ARG;
+  if (!ctx->have_grid || !ctx->have_bonds) return fail(ctx, V2C_ERR_STATE);
+  const long rows = 3 * ctx->nn;
+  if (rows + 1 > 0x7fffffffL) return fail(ctx, V2C_ERR_CAPACITY);
+  cudaStream_t st = ctx->stream;
+  const long nb = ctx->bondnum;
+  DevBuf bm, bn, bv, cnt, rhs, bsum, err, dja, da;
+  CK(bm.alloc<long>(ctx->nn * 4));
+  CK(bn.alloc<long>(nb * 3));
+  CK(bv.alloc<double>(nb * 4));
+  CK(cnt.alloc<int32_t>(rows + 1));
+  CK(rhs.alloc<double>(rows));
+  CK(bsum.alloc<int32_t>(scan_blocks(rows)));
+  CK(err.alloc<int>(1));
+  CK(cudaMemcpyAsync(bm.p, ctx->h_bondm.data(), sizeof(long) * ctx->nn * 4,
+                     cudaMemcpyHostToDevice, st));
+  if (nb > 0) {
+    CK(cudaMemcpyAsync(bn.p, ctx->h_bondn.data(), sizeof(long) * nb * 3, cudaMemcpyHostToDevice,
+                       st));
+    CK(cudaMemcpyAsync(bv.p, ctx->h_bondv.data(), sizeof(double) * nb * 4,
+                       cudaMemcpyHostToDevice, st));
+  }
+  CK(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+  StokesArgs s;
+  s.g = make_grid(ctx);
+  s.N = make_nodes(ctx);
+  s.bondm = bm.get<long>();
+  s.bondn = bn.get<long>();
+  s.bondv = bv.get<double>();
+  s.bondnum = nb;
+  s.mukoef = ctl->mukoef;
+  s.dt = ctl->dt;
+  s.gxkoef = ctl->gxkoef;
+  s.gykoef = ctl->gykoef;
+  s.timebond = ctl->timebond;
+  s.drunkensailor = ctl->drunkensailor;
+  s.timesum = ctx->p.timesum;
+  s.timestep = ctx->p.timestep;
+  s.nubeg = ctx->p.nubeg;
+  s.inertyn = ctx->p.inertyn;
+  s.compressible = ctx->p.compressiblemode;
+  s.cnt = cnt.get<int32_t>();
+  s.b = rhs.get<double>();
+  s.ja = nullptr;
+  s.a = nullptr;
+  s.err = err.get<int>();
+  int h_err = 0;
+  int32_t total = 0;
+  {
+    Prof pr(ctx, V2C_PROF_STOKES);
+    launch_stokes_count(s, st);
+    launch_scan(s.cnt, rows, s.cnt, bsum.get<int32_t>(), st);
+    ctx->launches += 4;
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(&h_err, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&total, s.cnt + rows, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (h_err) return fail(ctx, V2C_ERR_UNSUPPORTED);
+  if (total < 0) return fail(ctx, V2C_ERR_CAPACITY);  // more than 2^31 - 1 coefficients
+  *nnz = total;
+  if (ia) {
+    CK(cudaMemcpyAsync(ia, s.cnt, sizeof(int32_t) * (rows + 1), cudaMemcpyDeviceToHost, st));
+  }
+  if (b) CK(cudaMemcpyAsync(b, s.b, sizeof(double) * rows, cudaMemcpyDeviceToHost, st));
+  if (ja) {
+    if (cap < total) {
+      CK(cudaStreamSynchronize(st));
+      return fail(ctx, V2C_ERR_CAPACITY);
+    }
+    CK(dja.alloc<int32_t>(total));
+    CK(da.alloc<double>(total));
+    s.ja = dja.get<int32_t>();
+    s.a = da.get<double>();
+    {
+      Prof pr(ctx, V2C_PROF_STOKES);
+      launch_stokes_fill(s, st);
+      ctx->launches += 1;
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ja, s.ja, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(a, s.a, sizeof(double) * total, cudaMemcpyDeviceToHost, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  // row starts are 1-based, as gausmat4_add leaves them for Pardiso
+  if (ia)
+    for (long r = 0; r <= rows; r++) ia[r] += 1;
+  return V2C_OK;
+}
+
 // ======================================================= seismic cycle
 extern "C" int v2c_cycle_set_velocity(v2c_ctx *ctx, int regime, const double *vx,
                                       const double *vy) {

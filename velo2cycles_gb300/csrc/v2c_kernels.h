@@ -25,6 +25,31 @@ constexpr long SORT_MAX_MARKERS = 1L << 30;
 void launch_sort(const int32_t *cell, const float *u, const float *v, long n, long ncell,
                  SortBufs &b, unsigned long long *stat, cudaStream_t st);
 
+// exclusive scan of in[0, m) into out[0, m], total in out[m]; blocksum
+// holds scan_blocks(m) entries
+long scan_blocks(long m);
+void launch_scan(const int32_t *in, long m, int32_t *out, int32_t *blocksum, cudaStream_t st);
+
+// preparematrix + gausmat4_add (v2c_stokes.cu): two passes over the
+// 3 nodenum equations, counting then filling
+struct StokesArgs {
+  Grid g;
+  Nodes N;
+  const long *bondm;   // [nodenum * 4]
+  const long *bondn;   // [bondnum * 3]
+  const double *bondv; // [bondnum * 4]
+  long bondnum;
+  double mukoef, dt, gxkoef, gykoef, timebond, timesum, timestep, nubeg;
+  int drunkensailor, inertyn, compressible;
+  int32_t *cnt;        // [3 nodenum + 1]: coefficients per row, then row starts
+  int32_t *ja;         // [nnz] (fill pass)
+  double *a;           // [nnz] (fill pass)
+  double *b;           // [3 nodenum]
+  int *err;            // set where the reference stops or a row leaves the grid
+};
+void launch_stokes_count(const StokesArgs &a, cudaStream_t st);
+void launch_stokes_fill(const StokesArgs &a, cudaStream_t st);
+
 // marker2nodes sweep (scatter + node tail) and its follow-ups
 struct M2NArgs {
   Grid g;

@@ -220,6 +220,15 @@ void launch_assign(const Grid &g, const double *x, const double *y, long n, Mark
   if (n > 0) k_assign<<<nblk(n, 256), 256, 0, st>>>(g, x, y, n, m);
 }
 
+long scan_blocks(long m) { return (m + SB * SE - 1) / (SB * SE); }
+
+void launch_scan(const int32_t *in, long m, int32_t *out, int32_t *blocksum, cudaStream_t st) {
+  const long nb = scan_blocks(m);
+  if (nb > 0) k_scan_block<<<(unsigned)nb, SB, 0, st>>>(in, m, out, blocksum);
+  k_scan_sums<<<1, SB, 0, st>>>(blocksum, nb, out + m);
+  if (m > 0) k_scan_add<<<nblk(m, 256), 256, 0, st>>>(out, m, blocksum);
+}
+
 void launch_sort(const int32_t *cell, const float *u, const float *v, long n, long ncell,
                  SortBufs &b, unsigned long long *stat, cudaStream_t st) {
   cudaMemsetAsync(b.counts, 0, sizeof(int32_t) * ncell, st);

@@ -181,6 +181,27 @@ class MarkerInCell:
         """copyarrays (momentum_continuity_iterate.c:265)."""
         call("v2c_copyarrays", self.h)
 
+    def stokes_assemble(self, mukoef: float, dt: float, **ctl) -> dict:
+        """preparematrix (momentum_continuity_addmatrix_checkerror.c:22) on
+        the device's node fields: the CSR arrays gausmat4_add builds for
+        Pardiso (ia, ja 1-based; a; right-hand side b).  ctl: gxkoef, gykoef,
+        timebond, drunkensailor (abi.STOKES_DEFAULTS otherwise)."""
+        c = abi.StokesCtl(**dict(abi.STOKES_DEFAULTS, mukoef=mukoef, dt=dt, **ctl))
+        P = ctypes.POINTER
+        nnz = ctypes.c_long(0)
+        call("v2c_stokes_assemble", self.h, ctypes.byref(c), 0, None, None, None, None,
+             ctypes.byref(nnz))
+        rows = 3 * self.nn
+        ia = np.zeros(rows + 1, dtype=np.int32)
+        ja = np.zeros(max(nnz.value, 1), dtype=np.int32)
+        a = np.zeros(max(nnz.value, 1))
+        b = np.zeros(rows)
+        call("v2c_stokes_assemble", self.h, ctypes.byref(c), nnz.value,
+             ia.ctypes.data_as(P(ctypes.c_int)), ja.ctypes.data_as(P(ctypes.c_int)),
+             a.ctypes.data_as(P(ctypes.c_double)), b.ctypes.data_as(P(ctypes.c_double)),
+             ctypes.byref(nnz))
+        return dict(ia=ia, ja=ja[:nnz.value], a=a[:nnz.value], b=b)
+
     def cycle_set_velocity(self, regime: int, vx: np.ndarray, vy: np.ndarray):
         """Velocity field of a seismic-cycle regime (0 interseismic, 1
         coseismic); regime 0 also zeroes the accumulated slip."""
