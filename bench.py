@@ -312,7 +312,7 @@ def run_gpu(args, rank: int, world: int) -> None:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     t0 = time.time()
-    case = synth.make_case(args.config, seed=1 + rank)
+    case = synth.make_case(args.config, seed=1 + rank, interpolationmod=args.interpolationmod)
     log(f"[bench] {args.config}: {case.n} markers, {case.nodenum} nodes, generated in "
         f"{time.time() - t0:.1f}s")
     stream = torch.cuda.Stream()
@@ -459,7 +459,8 @@ def run_gpu(args, rank: int, world: int) -> None:
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 fields, f64 node normalisation", "data": "synthetic",
         "config": {"workload": f"{args.config}: {case.params['xnumx']}x{case.params['ynumy']} grid, "
-                               f"{n} markers ({mpn:.1f}/node), RK4, interpolationmod=2, "
+                               f"{n} markers ({mpn:.1f}/node), RK4, "
+                               f"interpolationmod={args.interpolationmod}, "
                                "antidiffinter=1, per-marker VEP+RSF Newton to 1e-10, learned "
                                "start, split precision",
                    "dt": "per step log-uniform [1e-3, 1e10] s, seeded, same sequence for every form",
@@ -834,6 +835,8 @@ def main():
     ap.add_argument("--c2-parity", action="store_true",
                     help="config 2: per-field error against the reference's routines")
     ap.add_argument("--c2-steps", type=int, default=100)
+    ap.add_argument("--interpolationmod", type=int, default=2, choices=[1, 2],
+                    help="marker-node stencil: 2 (shipped default) or 1 (13-node)")
     ap.add_argument("--stokes", action="store_true",
                     help="the Stokes matrix assembly on the C2 grid")
     args = ap.parse_args()

@@ -34,8 +34,11 @@ def _check_nodes(errs):
     assert not bad, f"node fields over tolerance: {bad}"
 
 
-@pytest.fixture(scope="module", params=["tiny", "small", "dense"])
+@pytest.fixture(scope="module", params=["tiny", "small", "dense", "mode1"])
 def case(request, built_lib, oracle_built):
+    if request.param == "mode1":
+        # interpolationmod 1: the 13-node stencil (per-node gather kernels)
+        return synth.make_case("small", seed=7, interpolationmod=1)
     if request.param == "dense":
         # 48 markers per cell: a column strip of a tile holds about 1000
         # markers, so the tile kernels stage it in several chunks
@@ -213,9 +216,9 @@ def test_flag_variants_full_step(variant, built_lib, oracle_built):
     m.close()
 
 
-def test_interpolationmod1_reported_unsupported(built_lib):
+def test_interpolation_mode_checked(built_lib):
     from velo2cycles_gb300._lib import V2CError
-    c = synth.make_case("tiny", seed=1, interpolationmod=1)
+    c = synth.make_case("tiny", seed=1, interpolationmod=3)
     with pytest.raises(V2CError) as e:
         mic.from_case(c)
     assert e.value.code == abi.ERR_UNSUPPORTED

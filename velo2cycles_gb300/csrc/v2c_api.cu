@@ -48,6 +48,7 @@ struct v2c_ctx {
   uint32_t *d_sticky = nullptr;
   float4 *d_quad = nullptr;                  // move: velocity forms per cell quarter
   float *d_tol = nullptr;                    // temperature update: node scratch
+  float *d_bs = nullptr;                     // interpolationmod 1 back-scatter payload
   unsigned *d_list_n = nullptr;              // count of listed Newton problems
   double *d_ts = nullptr;                    // calc_timestep scratch
   // markers
@@ -215,7 +216,7 @@ int fail(v2c_ctx *ctx, int code) {
 
 int check_params(const v2c_params *p) {
   if (p->xnumx < 4 || p->ynumy < 4) return V2C_ERR_ARG;
-  if (p->interpolationmod != 2) return V2C_ERR_UNSUPPORTED;
+  if (p->interpolationmod != 1 && p->interpolationmod != 2) return V2C_ERR_UNSUPPORTED;
   if (p->rkmod == 3) return V2C_ERR_UNSUPPORTED;
   if (p->newton_guess < V2C_GUESS_PLAIN || p->newton_guess > V2C_GUESS_OFF) return V2C_ERR_ARG;
   if (p->newton_precision != V2C_NEWTON_SPLIT && p->newton_precision != V2C_NEWTON_FP64)
@@ -271,6 +272,7 @@ extern "C" int v2c_create(const v2c_params *p, long max_markers, void *cuda_stre
   AL(ctx->d_sticky, ctx->nn);
   AL(ctx->d_quad, (size_t)ctx->ncell * QUAD_FLOAT4);
   AL(ctx->d_tol, ctx->nn);
+  if (p->interpolationmod == 1) AL(ctx->d_bs, (size_t)BS_N * (ctx->cap > 0 ? ctx->cap : 1));
   AL(ctx->d_list_n, 1);
   AL(ctx->d_ts, TIMESTEP_SCRATCH);
   AL(ctx->d_stat, ST_N);
@@ -317,6 +319,7 @@ extern "C" int v2c_destroy(v2c_ctx *ctx) {
   for (double *v : ctx->d_cyc_v64)
     if (v) cudaFree(v);
   if (ctx->d_vel64) cudaFree(ctx->d_vel64);
+  if (ctx->d_bs) cudaFree(ctx->d_bs);
   if (ctx->d_slip) cudaFree(ctx->d_slip);
   if (ctx->d_mslip) cudaFree(ctx->d_mslip);
   void *ptrs[] = {ctx->d_gx, ctx->d_gy, ctx->d_wx, ctx->d_wy, ctx->d_gxf, ctx->d_gyf,
@@ -343,6 +346,10 @@ extern "C" int v2c_set_params(v2c_ctx *ctx, const v2c_params *p) {
   int rc = check_params(p);
   if (rc) return fail(ctx, rc);
   ctx->p = *p;
+  // the full-stencil back-scatter's payload, allocated here so that no
+  // step (or captured step) allocates
+  if (p->interpolationmod == 1 && !ctx->d_bs)
+    CK(cudaMalloc(&ctx->d_bs, sizeof(float) * BS_N * (ctx->cap > 0 ? ctx->cap : 1)));
   return V2C_OK;
 }
 
@@ -821,11 +828,12 @@ extern "C" int v2c_marker2nodes(v2c_ctx *ctx) {
   {
     Prof pr(ctx, V2C_PROF_M2N);
     launch_m2n(a, st);
+    ctx->launches += ctx->p.interpolationmod == 1 ? 4 : 1;
   }
   {
     Prof pr(ctx, V2C_PROF_M2N_TAIL);
     launch_sticky(a.N, ctx->d_sticky, ctx->nn, st);
-    ctx->launches += 2;
+    ctx->launches += 1;
     if (ctx->p.Dphis > 0) { launch_dphis(a.g, a.N, st); ctx->launches += 1; }
     if (ctx->have_bonds && ctx->bc.n > 0) { launch_bc(ctx->bc, a.N, ctx->d_bc_scratch, st); ctx->launches += 2; }
   }
@@ -970,10 +978,15 @@ static int n2m_move(v2c_ctx *ctx, int do_n2m, int do_move) {
   a.n = ctx->n;
   a.TX = pick_tx(ctx);
   a.do_n2m = 1;
+  if (do_n2m && ctx->p.interpolationmod == 1 && ctx->p.antidiffinter == 1) {
+    // the full-stencil back-scatter: one payload record per marker
+    if (!ctx->d_bs) return fail(ctx, V2C_ERR_STATE);
+    a.bs = ctx->d_bs;
+  }
   if (do_n2m) {
     Prof pr(ctx, V2C_PROF_N2M);
     launch_n2m(a, st);
-    ctx->launches += 1;
+    ctx->launches += a.bs ? 3 : 1;
   }
   if (do_move) {
     {

@@ -148,7 +148,12 @@ struct N2MArgs {
   long n;            // markers
   int TX;
   int do_n2m;
+  // interpolationmod 1: the tile sweep writes each marker's back-scatter
+  // payload (BS_N fields, SoA by sorted position) here and per-node gather
+  // kernels sum it; null for interpolationmod 2
+  float *bs = nullptr;
 };
+enum { BS_U = 0, BS_V, BS_PHIS, BS_SXY, BS_EXY, BS_ES, BS_PR, BS_SXX, BS_EXX, BS_N };
 // float4 coefficient sets per cell: 4 quarters x (VX, VY, ESP)
 constexpr int QUAD_FLOAT4 = 12;
 // nodes2markers: gather, marker update, back-scatter (cell-column tiles)

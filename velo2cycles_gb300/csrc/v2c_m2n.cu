@@ -156,6 +156,144 @@ __device__ __forceinline__ void node_friction(const M2NArgs &a, int ci, int j, f
     A[6].add(w);                                                      \
   } while (0)
 
+// The node tail of marker2nodes (interpolation.c:714-824) for node row j
+// of column ci, from the compensated sums of one role: 0 basic node (ci, j)
+// stress/state group (cur[0..7]: nu, nu/G, e, sxy, exy, C, phi, w), 1 its
+// thermal group (cur[0..6]: ro, et, ht, cp, kt, tk, w), 2 the centre node
+// (ci+1, j+1) of cell (ci, j) (cur[0..5]: nu, nu/G, sxx, exx, p, w) and the
+// centre fields of (ci, j) when no cell feeds it, 3 vx node (ci, j)
+// (cur[0..2]: vx*ro, ro, w) and vy node (ci, j) (vy3[0..2]).
+__device__ __forceinline__ void node_tail(const M2NArgs &a, int role, int ci, int j,
+                                          const Acc (&cur)[8], const Acc (&vy3)[3]) {
+  const Grid &g = a.g;
+  const int ncy = g.ncy;
+  const long m3 = (long)ci * g.yn + j;
+  const Nodes &N = a.N;
+  const int antid = a.S.antid;
+  if (role == 0) {
+    const float ss = cur[7].value();
+    const bool interior = ci >= 1 && j >= 1 && ci < g.xn - 1 && j < g.yn - 1;
+    if (ss != 0.f && interior) {
+      float phin = __fdividef(cur[6].value(), ss), sxyen = __fdividef(cur[3].value(), ss);
+      float exyen = __fdividef(cur[4].value(), ss), pen = __fdividef(cur[2].value(), ss);
+      float phis, sxye, exye, pe;
+      if (antid) {
+        phis = N.f(V2C_NF_PHIS_IT)[m3] + (phin - N.f(V2C_NF_PHIE)[m3]);
+        sxye = N.f(V2C_NF_SXY)[m3] + (sxyen - N.f(V2C_NF_SXYEE)[m3]);
+        exye = N.f(V2C_NF_EXY)[m3] + (exyen - N.f(V2C_NF_EXYEE)[m3]);
+        pe = N.f(V2C_NF_PES)[m3] + (pen - N.f(V2C_NF_PEE)[m3]);
+      } else {
+        phis = phin; sxye = sxyen; exye = exyen; pe = pen;
+      }
+      if (pe < 0.f) pe = 0.f;
+      float nu_m2c = __fdividef(cur[0].value(), ss);
+      N.f(V2C_NF_PHIN)[m3] = phin;
+      N.f(V2C_NF_SXYEN)[m3] = sxyen;
+      N.f(V2C_NF_EXYEN)[m3] = exyen;
+      N.f(V2C_NF_PEN)[m3] = pen;
+      N.f(V2C_NF_PHIS)[m3] = phis;
+      N.f(V2C_NF_SXYE)[m3] = sxye;
+      N.f(V2C_NF_EXYE)[m3] = exye;
+      N.f(V2C_NF_PE)[m3] = pe;
+      N.f(V2C_NF_COHESION)[m3] = __fdividef(cur[5].value(), ss);
+      N.f(V2C_NF_NU_M2C)[m3] = nu_m2c;
+      N.f(V2C_NF_GG)[m3] = __fdividef(nu_m2c, __fdividef(cur[1].value(), ss));
+    } else {
+      N.f(V2C_NF_PHIN)[m3] = 0; N.f(V2C_NF_SXYEN)[m3] = 0; N.f(V2C_NF_EXYEN)[m3] = 0;
+      N.f(V2C_NF_PHIS)[m3] = 0; N.f(V2C_NF_SXYE)[m3] = 0; N.f(V2C_NF_EXYE)[m3] = 0;
+      N.f(V2C_NF_COHESION)[m3] = 0; N.f(V2C_NF_GG)[m3] = 0;
+    }
+  } else if (role == 1) {
+    const float ss = cur[6].value();
+    const bool interior = ci >= 1 && j >= 1 && ci < g.xn - 1 && j < g.yn - 1;
+    float mu = 0.f, fa = 0.f, fb = 0.f, fL = 0.f, fV0 = 0.f;
+    if (ss != 0.f && interior) node_friction(a, ci, j, mu, fa, fb, fL, fV0);
+    N.f(V2C_NF_MUS_S)[m3] = mu; N.f(V2C_NF_AS)[m3] = fa; N.f(V2C_NF_BS)[m3] = fb;
+    N.f(V2C_NF_LS)[m3] = fL; N.f(V2C_NF_V0S)[m3] = fV0;
+    if (ss != 0.f) {
+      N.f(V2C_NF_RO)[m3] = __fdividef(cur[0].value(), ss); N.f(V2C_NF_ET)[m3] = __fdividef(cur[1].value(), ss);
+      N.f(V2C_NF_HT)[m3] = __fdividef(cur[2].value(), ss); N.f(V2C_NF_CP)[m3] = __fdividef(cur[3].value(), ss);
+      N.f(V2C_NF_KT)[m3] = __fdividef(cur[4].value(), ss); N.f(V2C_NF_TK)[m3] = __fdividef(cur[5].value(), ss);
+    } else {
+      N.f(V2C_NF_RO)[m3] = 0; N.f(V2C_NF_ET)[m3] = 0; N.f(V2C_NF_HT)[m3] = 0;
+      N.f(V2C_NF_CP)[m3] = 0; N.f(V2C_NF_KT)[m3] = 0; N.f(V2C_NF_TK)[m3] = 0;
+    }
+    // arrays the reference zeroes at the start (interpolation.c:58-153)
+    // and that marker2nodes itself does not fill
+    static const int zl[] = {V2C_NF_NU, V2C_NF_ND, V2C_NF_WTPHISUM, V2C_NF_WTSXXSUM,
+                             V2C_NF_WTVXSUM, V2C_NF_WTVYSUM, V2C_NF_PHISUM, V2C_NF_SXYSUM,
+                             V2C_NF_EXYSUM, V2C_NF_ESUM, V2C_NF_SXXSUM, V2C_NF_EXXSUM,
+                             V2C_NF_VXSUM, V2C_NF_VYSUM, V2C_NF_PSUM, V2C_NF_MRX0,
+                             V2C_NF_MRY0};
+#pragma unroll
+    for (int q = 0; q < (int)(sizeof(zl) / sizeof(zl[0])); q++) N.f(zl[q])[m3] = 0;
+  } else if (role == 2) {
+    // centre node (ci+1, j+1) from cell (ci, j)
+    if (ci < g.ncx && j < ncy) {
+      const long mc = (long)(ci + 1) * g.yn + (j + 1);
+      const float s1 = cur[5].value();
+      if (s1 != 0.f) {
+        float sxxen = __fdividef(cur[2].value(), s1), sppen = __fdividef(cur[4].value(), s1);
+        float exxen = __fdividef(cur[3].value(), s1);
+        float sxxe, sppe, exxe;
+        if (antid) {
+          sxxe = N.f(V2C_NF_SXX)[mc] + (sxxen - N.f(V2C_NF_SXXEE)[mc]);
+          sppe = N.f(V2C_NF_PR)[mc] + (sppen - N.f(V2C_NF_SPPEE)[mc]);
+          exxe = N.f(V2C_NF_EXX)[mc] + (exxen - N.f(V2C_NF_EXXEE)[mc]);
+        } else {
+          sxxe = sxxen; sppe = sppen; exxe = exxen;
+        }
+        if (a.S.sppe_nstress) sppe = a.S.nstress_f;
+        float nd = __fdividef(cur[0].value(), s1);
+        N.f(V2C_NF_SXXEN)[mc] = sxxen; N.f(V2C_NF_SPPEN)[mc] = sppen;
+        N.f(V2C_NF_EXXEN)[mc] = exxen; N.f(V2C_NF_SXXE)[mc] = sxxe;
+        N.f(V2C_NF_SPPE)[mc] = sppe; N.f(V2C_NF_EXXE)[mc] = exxe;
+        N.f(V2C_NF_ND_M2C)[mc] = nd;
+        N.f(V2C_NF_GD)[mc] = nd / (__fdividef(cur[1].value(), s1));
+        N.f(V2C_NF_BM)[mc] = 50e9f;
+        N.f(V2C_NF_DRO)[mc] = 0; N.f(V2C_NF_DRP)[mc] = 0;
+      } else {
+        N.f(V2C_NF_SXXEN)[mc] = 0; N.f(V2C_NF_SPPEN)[mc] = 0; N.f(V2C_NF_EXXEN)[mc] = 0;
+        N.f(V2C_NF_SXXE)[mc] = 0; N.f(V2C_NF_SPPE)[mc] = 0; N.f(V2C_NF_EXXE)[mc] = 0;
+        N.f(V2C_NF_GD)[mc] = 0; N.f(V2C_NF_BM)[mc] = 0;
+        N.f(V2C_NF_DRO)[mc] = 0; N.f(V2C_NF_DRP)[mc] = 0;
+      }
+    }
+    // centre fields of nodes no cell feeds (first column / first row)
+    if (ci == 0 || j == 0) {
+      N.f(V2C_NF_SXXEN)[m3] = 0; N.f(V2C_NF_SPPEN)[m3] = 0; N.f(V2C_NF_EXXEN)[m3] = 0;
+      N.f(V2C_NF_SXXE)[m3] = 0; N.f(V2C_NF_SPPE)[m3] = 0; N.f(V2C_NF_EXXE)[m3] = 0;
+      N.f(V2C_NF_GD)[m3] = 0; N.f(V2C_NF_BM)[m3] = 0;
+      N.f(V2C_NF_DRO)[m3] = 0; N.f(V2C_NF_DRP)[m3] = 0;
+    }
+  } else {
+    const float wx = cur[2].value();
+    if (wx != 0.f) {
+      float mrx0 = cur[1].value();
+      float mvxn = cur[0].value() / mrx0;
+      N.f(V2C_NF_MVXN)[m3] = mvxn;
+      // the boundary correction (vxvy_boundarycorrection) leaves the vx
+      // ghost row at zero; only the 13-node stencil gives it weight
+      N.f(V2C_NF_MVX)[m3] = j == g.yn - 1 ? 0.f
+                            : antid ? N.f(V2C_NF_VX)[m3] + (mvxn - N.f(V2C_NF_MVXE)[m3]) : mvxn;
+      N.f(V2C_NF_MRX)[m3] = mrx0 / wx;
+    } else {
+      N.f(V2C_NF_MVX)[m3] = 0; N.f(V2C_NF_MRX)[m3] = 0;
+    }
+    const float wy = vy3[2].value();
+    if (wy != 0.f) {
+      float mry0 = vy3[1].value();
+      float mvyn = vy3[0].value() / mry0;
+      N.f(V2C_NF_MVYN)[m3] = mvyn;
+      N.f(V2C_NF_MVY)[m3] = ci == g.xn - 1 ? 0.f  // the vy ghost column, likewise
+                            : antid ? N.f(V2C_NF_VY)[m3] + (mvyn - N.f(V2C_NF_MVYE)[m3]) : mvyn;
+      N.f(V2C_NF_MRY)[m3] = mry0 / wy;
+    } else {
+      N.f(V2C_NF_MVY)[m3] = 0; N.f(V2C_NF_MRY)[m3] = 0;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(NTH, 7) k_m2n(M2NArgs a) {
   __shared__ Smem sm;
   const Grid &g = a.g;
@@ -304,127 +442,142 @@ __global__ void __launch_bounds__(NTH, 7) k_m2n(M2NArgs a) {
 
     // ------------------------------------------------------ node tail
     if (ci < i0 || !jvalid) continue;
-    const long m3 = (long)ci * g.yn + j;
-    const Nodes &N = a.N;
-    const int antid = a.S.antid;
-    if (role == 0) {
-      const float ss = cur[7].value();
-      const bool interior = ci >= 1 && j >= 1 && ci < g.xn - 1 && j < g.yn - 1;
-      if (ss != 0.f && interior) {
-        float phin = __fdividef(cur[6].value(), ss), sxyen = __fdividef(cur[3].value(), ss);
-        float exyen = __fdividef(cur[4].value(), ss), pen = __fdividef(cur[2].value(), ss);
-        float phis, sxye, exye, pe;
-        if (antid) {
-          phis = N.f(V2C_NF_PHIS_IT)[m3] + (phin - N.f(V2C_NF_PHIE)[m3]);
-          sxye = N.f(V2C_NF_SXY)[m3] + (sxyen - N.f(V2C_NF_SXYEE)[m3]);
-          exye = N.f(V2C_NF_EXY)[m3] + (exyen - N.f(V2C_NF_EXYEE)[m3]);
-          pe = N.f(V2C_NF_PES)[m3] + (pen - N.f(V2C_NF_PEE)[m3]);
-        } else {
-          phis = phin; sxye = sxyen; exye = exyen; pe = pen;
-        }
-        if (pe < 0.f) pe = 0.f;
-        float nu_m2c = __fdividef(cur[0].value(), ss);
-        N.f(V2C_NF_PHIN)[m3] = phin;
-        N.f(V2C_NF_SXYEN)[m3] = sxyen;
-        N.f(V2C_NF_EXYEN)[m3] = exyen;
-        N.f(V2C_NF_PEN)[m3] = pen;
-        N.f(V2C_NF_PHIS)[m3] = phis;
-        N.f(V2C_NF_SXYE)[m3] = sxye;
-        N.f(V2C_NF_EXYE)[m3] = exye;
-        N.f(V2C_NF_PE)[m3] = pe;
-        N.f(V2C_NF_COHESION)[m3] = __fdividef(cur[5].value(), ss);
-        N.f(V2C_NF_NU_M2C)[m3] = nu_m2c;
-        N.f(V2C_NF_GG)[m3] = __fdividef(nu_m2c, __fdividef(cur[1].value(), ss));
-      } else {
-        N.f(V2C_NF_PHIN)[m3] = 0; N.f(V2C_NF_SXYEN)[m3] = 0; N.f(V2C_NF_EXYEN)[m3] = 0;
-        N.f(V2C_NF_PHIS)[m3] = 0; N.f(V2C_NF_SXYE)[m3] = 0; N.f(V2C_NF_EXYE)[m3] = 0;
-        N.f(V2C_NF_COHESION)[m3] = 0; N.f(V2C_NF_GG)[m3] = 0;
-      }
-    } else if (role == 1) {
-      const float ss = cur[6].value();
-      const bool interior = ci >= 1 && j >= 1 && ci < g.xn - 1 && j < g.yn - 1;
-      float mu = 0.f, fa = 0.f, fb = 0.f, fL = 0.f, fV0 = 0.f;
-      if (ss != 0.f && interior) node_friction(a, ci, j, mu, fa, fb, fL, fV0);
-      N.f(V2C_NF_MUS_S)[m3] = mu; N.f(V2C_NF_AS)[m3] = fa; N.f(V2C_NF_BS)[m3] = fb;
-      N.f(V2C_NF_LS)[m3] = fL; N.f(V2C_NF_V0S)[m3] = fV0;
-      if (ss != 0.f) {
-        N.f(V2C_NF_RO)[m3] = __fdividef(cur[0].value(), ss); N.f(V2C_NF_ET)[m3] = __fdividef(cur[1].value(), ss);
-        N.f(V2C_NF_HT)[m3] = __fdividef(cur[2].value(), ss); N.f(V2C_NF_CP)[m3] = __fdividef(cur[3].value(), ss);
-        N.f(V2C_NF_KT)[m3] = __fdividef(cur[4].value(), ss); N.f(V2C_NF_TK)[m3] = __fdividef(cur[5].value(), ss);
-      } else {
-        N.f(V2C_NF_RO)[m3] = 0; N.f(V2C_NF_ET)[m3] = 0; N.f(V2C_NF_HT)[m3] = 0;
-        N.f(V2C_NF_CP)[m3] = 0; N.f(V2C_NF_KT)[m3] = 0; N.f(V2C_NF_TK)[m3] = 0;
-      }
-      // arrays the reference zeroes at the start (interpolation.c:58-153)
-      // and that marker2nodes itself does not fill
-      static const int zl[] = {V2C_NF_NU, V2C_NF_ND, V2C_NF_WTPHISUM, V2C_NF_WTSXXSUM,
-                               V2C_NF_WTVXSUM, V2C_NF_WTVYSUM, V2C_NF_PHISUM, V2C_NF_SXYSUM,
-                               V2C_NF_EXYSUM, V2C_NF_ESUM, V2C_NF_SXXSUM, V2C_NF_EXXSUM,
-                               V2C_NF_VXSUM, V2C_NF_VYSUM, V2C_NF_PSUM, V2C_NF_MRX0,
-                               V2C_NF_MRY0};
+    node_tail(a, role, ci, j, cur, vy3);
+  }
+}
+
+// ------------------------------------------------ interpolationmod 1
+// The 13-node stencil (interpolation.c:258-538) as a gather: one thread per
+// node and role sums, in sorted-marker order cell by cell, the markers of
+// the cells whose stencil reaches the node, with that stencil's weight
+// (bilinear on basic nodes; the staggered vx, vy and centre stencils with
+// their half-cell conditions), then runs the same node tail as the tile
+// sweep.  A marker in cell (cx, cy) at offsets (u, v) reaches
+//   basic (cx + a, cy + b), a, b in {0, 1}:  (a ? u : 1-u) (b ? v : 1-v)
+//   vx (cx + a, cy + b), b in {-1, 0, 1}:    (a ? u : 1-u) times 1-|v-1/2|
+//       (b = 0), v-1/2 if v > 1/2 (b = 1), 1/2-v if v < 1/2 (b = -1)
+//   vy likewise with the axes exchanged (a in {-1, 0, 1}, b in {0, 1})
+//   centre (cx + a, cy + b), a, b in {0, 1, 2}: the product of the axis
+//       factors 1/2-u if u < 1/2 (a = 0), 1-|u-1/2| (a = 1), u-1/2 if
+//       u > 1/2 (a = 2), and the same in v.
+// Contributions the reference sends past the last node row (its node
+// index wraps into the next column's first row, a centre node that is
+// never normalised) have no effect and are not formed.
+struct Mk {
+  int idx, t;
+  float u, v;
+};
+
+__device__ __forceinline__ bool marker_active(const Grid &g, int cx, int cy, float u, float v) {
+  bool act = true;
+  if (cx == 0 || cx == g.ncx - 1) {
+    double x = g.gx[cx] + (double)u * (g.gx[cx + 1] - g.gx[cx]);
+    act = act && x > 0 && x < g.xsize;
+  }
+  if (cy == 0 || cy == g.ncy - 1) {
+    double y = g.gy[cy] + (double)v * (g.gy[cy + 1] - g.gy[cy]);
+    act = act && y > 0 && y < g.ysize;
+  }
+  return act;
+}
+
+// axis factor of a staggered (half-cell) stencil: k = 0 below the cell's
+// middle, 1 across it, 2 above it; 0 where the stencil does not reach
+__device__ __forceinline__ float half_factor(int k, float f) {
+  if (k == 0) return f < 0.5f ? 1.f - f - 0.5f : 0.f;
+  if (k == 1) return 1.f - fabsf(f - 0.5f);
+  return f > 0.5f ? f - 0.5f : 0.f;
+}
+
+template <int ROLE>
+__global__ void __launch_bounds__(128) k_m2n_mode1(M2NArgs a) {
+  const Grid &g = a.g;
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= g.nn) return;
+  const int ix = (int)(t / g.yn), iy = (int)(t - (long)ix * g.yn);
+  const int ncy = g.ncy;
+  Acc cur[8], vy3[3];
 #pragma unroll
-      for (int q = 0; q < (int)(sizeof(zl) / sizeof(zl[0])); q++) N.f(zl[q])[m3] = 0;
-    } else if (role == 2) {
-      // centre node (ci+1, j+1) from cell (ci, j)
-      if (ci < g.ncx && j < ncy) {
-        const long mc = (long)(ci + 1) * g.yn + (j + 1);
-        const float s1 = cur[5].value();
-        if (s1 != 0.f) {
-          float sxxen = __fdividef(cur[2].value(), s1), sppen = __fdividef(cur[4].value(), s1);
-          float exxen = __fdividef(cur[3].value(), s1);
-          float sxxe, sppe, exxe;
-          if (antid) {
-            sxxe = N.f(V2C_NF_SXX)[mc] + (sxxen - N.f(V2C_NF_SXXEE)[mc]);
-            sppe = N.f(V2C_NF_PR)[mc] + (sppen - N.f(V2C_NF_SPPEE)[mc]);
-            exxe = N.f(V2C_NF_EXX)[mc] + (exxen - N.f(V2C_NF_EXXEE)[mc]);
+  for (int q = 0; q < 8; q++) cur[q].zero();
+#pragma unroll
+  for (int q = 0; q < 3; q++) vy3[q].zero();
+  // cells that can reach this node: dx, dy offsets of the cell from the node
+  const int dx0 = ROLE == 2 ? -2 : -1, dx1 = ROLE == 3 ? 1 : 0;
+  const int dy0 = ROLE == 2 ? -2 : -1, dy1 = ROLE == 3 ? 1 : 0;
+  for (int dx = dx0; dx <= dx1; dx++) {
+    const int cx = ix + dx;
+    if (cx < 0 || cx >= g.ncx) continue;
+    const float iwx = 1.f / __ldg(g.wx + cx);
+    for (int dy = dy0; dy <= dy1; dy++) {
+      const int cy = iy + dy;
+      if (cy < 0 || cy >= ncy) continue;
+      // stencil position of the node relative to the cell: a = -dx, b = -dy
+      const int ax = -dx, by = -dy;
+      if (ROLE == 3 && ax < 0 && by < 0) continue;  // (1, 1): no stencil reaches
+      const float s1 = iwx / __ldg(g.wy + cy);
+      const long c = (long)cx * ncy + cy;
+      const int sb = __ldg(a.start + c), se = __ldg(a.start + c + 1);
+      for (int s = sb; s < se; s++) {
+        const int idx = __ldg(a.perm + s);
+        const float u = a.m.u_in[idx], v = a.m.v_in[idx];
+        if (!marker_active(g, cx, cy, u, v)) continue;
+        const int tt = a.m.type[idx];
+        if (ROLE == 0 || ROLE == 1) {
+          const float w = s1 * (ax ? u : 1.f - u) * (by ? v : 1.f - v);
+          if (ROLE == 0) {
+            const float mnu = a.m.mnu[idx];
+            cur[0].add(mnu * w); cur[1].add(mnu * a.R(RK_INV_GG, tt) * w);
+            cur[2].add(a.m.e[idx] * w); cur[3].add(a.m.sxy[idx] * w);
+            cur[4].add(a.m.exy[idx] * w); cur[5].add(a.m.coh[idx] * w);
+            cur[6].add(a.m.phi[idx] * w); cur[7].add(w);
           } else {
-            sxxe = sxxen; sppe = sppen; exxe = exxen;
+            const float T = a.m.tk[idx], bb = a.R(RK_BB, tt);
+            const float ro = a.S.p.densimod ? a.m.mro[idx] : a.R(RK_RO, tt);
+            cur[0].add(ro * w);
+            cur[1].add(__fdividef(bb, 1.f - bb * (T - 298.15f)) * w);
+            cur[2].add(a.R(RK_HT, tt) * w); cur[3].add(a.R(RK_CP, tt) * w);
+            cur[4].add(a.m.mkt[idx] * w); cur[5].add(T * w); cur[6].add(w);
           }
-          if (a.S.sppe_nstress) sppe = a.S.nstress_f;
-          float nd = __fdividef(cur[0].value(), s1);
-          N.f(V2C_NF_SXXEN)[mc] = sxxen; N.f(V2C_NF_SPPEN)[mc] = sppen;
-          N.f(V2C_NF_EXXEN)[mc] = exxen; N.f(V2C_NF_SXXE)[mc] = sxxe;
-          N.f(V2C_NF_SPPE)[mc] = sppe; N.f(V2C_NF_EXXE)[mc] = exxe;
-          N.f(V2C_NF_ND_M2C)[mc] = nd;
-          N.f(V2C_NF_GD)[mc] = nd / (__fdividef(cur[1].value(), s1));
-          N.f(V2C_NF_BM)[mc] = 50e9f;
-          N.f(V2C_NF_DRO)[mc] = 0; N.f(V2C_NF_DRP)[mc] = 0;
+        } else if (ROLE == 2) {
+          const float w = s1 * half_factor(ax, u) * half_factor(by, v);
+          if (w != 0.f) {
+            const float mnu = a.m.mnu[idx];
+            cur[0].add(mnu * w); cur[1].add(mnu * a.R(RK_INV_GG, tt) * w);
+            cur[2].add(a.m.sxx[idx] * w); cur[3].add(a.m.exx[idx] * w);
+            cur[4].add(a.m.p[idx] * w); cur[5].add(w);
+          }
         } else {
-          N.f(V2C_NF_SXXEN)[mc] = 0; N.f(V2C_NF_SPPEN)[mc] = 0; N.f(V2C_NF_EXXEN)[mc] = 0;
-          N.f(V2C_NF_SXXE)[mc] = 0; N.f(V2C_NF_SPPE)[mc] = 0; N.f(V2C_NF_EXXE)[mc] = 0;
-          N.f(V2C_NF_GD)[mc] = 0; N.f(V2C_NF_BM)[mc] = 0;
-          N.f(V2C_NF_DRO)[mc] = 0; N.f(V2C_NF_DRP)[mc] = 0;
+          const float ro = a.S.p.densimod ? a.m.mro[idx] : a.R(RK_RO, tt);
+          // vx node: x bilinear (ax in {0, 1}), y staggered (by + 1 in {0, 1, 2})
+          if (ax >= 0) {
+            const float w = s1 * (ax ? u : 1.f - u) * half_factor(by + 1, v);
+            if (w != 0.f) {
+              cur[0].add(a.m.vx[idx] * ro * w); cur[1].add(ro * w); cur[2].add(w);
+            }
+          }
+          // vy node: x staggered (ax + 1), y bilinear (by in {0, 1})
+          if (by >= 0) {
+            const float w = s1 * half_factor(ax + 1, u) * (by ? v : 1.f - v);
+            if (w != 0.f) {
+              vy3[0].add(a.m.vy[idx] * ro * w); vy3[1].add(ro * w); vy3[2].add(w);
+            }
+          }
         }
-      }
-      // centre fields of nodes no cell feeds (first column / first row)
-      if (ci == 0 || j == 0) {
-        N.f(V2C_NF_SXXEN)[m3] = 0; N.f(V2C_NF_SPPEN)[m3] = 0; N.f(V2C_NF_EXXEN)[m3] = 0;
-        N.f(V2C_NF_SXXE)[m3] = 0; N.f(V2C_NF_SPPE)[m3] = 0; N.f(V2C_NF_EXXE)[m3] = 0;
-        N.f(V2C_NF_GD)[m3] = 0; N.f(V2C_NF_BM)[m3] = 0;
-        N.f(V2C_NF_DRO)[m3] = 0; N.f(V2C_NF_DRP)[m3] = 0;
-      }
-    } else {
-      const float wx = cur[2].value();
-      if (wx != 0.f) {
-        float mrx0 = cur[1].value();
-        float mvxn = cur[0].value() / mrx0;
-        N.f(V2C_NF_MVXN)[m3] = mvxn;
-        N.f(V2C_NF_MVX)[m3] = antid ? N.f(V2C_NF_VX)[m3] + (mvxn - N.f(V2C_NF_MVXE)[m3]) : mvxn;
-        N.f(V2C_NF_MRX)[m3] = mrx0 / wx;
-      } else {
-        N.f(V2C_NF_MVX)[m3] = 0; N.f(V2C_NF_MRX)[m3] = 0;
-      }
-      const float wy = vy3[2].value();
-      if (wy != 0.f) {
-        float mry0 = vy3[1].value();
-        float mvyn = vy3[0].value() / mry0;
-        N.f(V2C_NF_MVYN)[m3] = mvyn;
-        N.f(V2C_NF_MVY)[m3] = antid ? N.f(V2C_NF_VY)[m3] + (mvyn - N.f(V2C_NF_MVYE)[m3]) : mvyn;
-        N.f(V2C_NF_MRY)[m3] = mry0 / wy;
-      } else {
-        N.f(V2C_NF_MVY)[m3] = 0; N.f(V2C_NF_MRY)[m3] = 0;
       }
     }
+  }
+  if (ROLE != 2) {
+    node_tail(a, ROLE, ix, iy, cur, vy3);
+  } else if (ix >= 1 && iy >= 1) {
+    node_tail(a, 2, ix - 1, iy - 1, cur, vy3);  // writes centre node (ix, iy)
+  } else {
+    // a centre node no cell has (first column or row)
+    const Nodes &N = a.N;
+    const long m3 = t;
+    N.f(V2C_NF_SXXEN)[m3] = 0; N.f(V2C_NF_SPPEN)[m3] = 0; N.f(V2C_NF_EXXEN)[m3] = 0;
+    N.f(V2C_NF_SXXE)[m3] = 0; N.f(V2C_NF_SPPE)[m3] = 0; N.f(V2C_NF_EXXE)[m3] = 0;
+    N.f(V2C_NF_GD)[m3] = 0; N.f(V2C_NF_BM)[m3] = 0;
+    N.f(V2C_NF_DRO)[m3] = 0; N.f(V2C_NF_DRP)[m3] = 0;
   }
 }
 
@@ -456,6 +609,14 @@ __global__ void k_dphis(Grid g, float *phis) {
 }  // namespace
 
 void launch_m2n(const M2NArgs &a, cudaStream_t st) {
+  if (a.S.p.interpolationmod == 1) {
+    const unsigned nb = (unsigned)((a.g.nn + 127) / 128);
+    k_m2n_mode1<0><<<nb, 128, 0, st>>>(a);
+    k_m2n_mode1<1><<<nb, 128, 0, st>>>(a);
+    k_m2n_mode1<2><<<nb, 128, 0, st>>>(a);
+    k_m2n_mode1<3><<<nb, 128, 0, st>>>(a);
+    return;
+  }
   dim3 grid((a.g.xn + a.TX - 1) / a.TX, (a.g.yn + TY - 1) / TY);
   k_m2n<<<grid, NTH, 0, st>>>(a);
 }

@@ -191,6 +191,7 @@ __device__ __forceinline__ void vel_at(const Grid &g, const float4 *Q, Pos p, fl
     A[4].add(w);                                                        \
   } while (0)
 
+template <bool BS>
 __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
   __shared__ Smem sm;
   const Grid &g = a.g;
@@ -202,7 +203,8 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
   const int ncy = g.ncy;
   const int ci_end = min(i0 + a.TX, g.xn);
   const v2c_params &P = a.S.p;
-  const int backscatter = a.do_n2m && P.antidiffinter == 1;
+  // interpolationmod 1 back-scatters through a.bs and the gather kernels
+  const int backscatter = a.do_n2m && P.antidiffinter == 1 && !BS;
   const long yn = g.yn;
 
   // role 0: PHIS, SXY, EXY, ES, w (basic)   role 1: PR, SXX, EXX, w (centre)
@@ -282,6 +284,14 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
             sm.q[Q_MRO][k] = a.R(RK_RO, t);
           }
           if (!owned) continue;
+          if (BS) {
+            const long s = cs + k, n = a.n;
+            a.bs[BS_U * n + s] = uc; a.bs[BS_V * n + s] = vc;
+            a.bs[BS_PHIS * n + s] = PHIS; a.bs[BS_SXY * n + s] = SXY;
+            a.bs[BS_EXY * n + s] = EXY; a.bs[BS_ES * n + s] = ES;
+            a.bs[BS_PR * n + s] = PR; a.bs[BS_SXX * n + s] = SXX;
+            a.bs[BS_EXX * n + s] = EXX;
+          }
           // ------------------------------------- marker update (:943-1011)
           const bool in_strict = (ix > 0 || u > 0.f) && (ix < g.ncx - 1 || u < 1.f) &&
                                  (iy > 0 || v > 0.f) && (iy < g.ncy - 1 || v < 1.f);
@@ -472,6 +482,85 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
   }
 }
 
+// ------------------------------------------------ interpolationmod 1
+// The back-scatter of interpolate_mechanical (interpolation.c:1104-1158 and
+// 1249-1358) with the full stencils, as a gather: one thread per node sums,
+// cell by cell in sorted order, the payload the tile sweep left per marker
+// — bilinear weights on basic nodes, the staggered centre stencil on
+// pressure nodes (no vx/vy back-scatter in this mode) — and normalises as
+// the tail of nodes2markers does (interpolation.c:1014-1046).  The centre
+// stencil's contributions past the last node row land, as in the
+// reference, in the next column's first row (a ghost node whose sums are
+// kept but never normalised).
+__device__ __forceinline__ float bs_half(int k, float f) {
+  if (k == 0) return f < 0.5f ? 1.f - f - 0.5f : 0.f;
+  if (k == 1) return 1.f - fabsf(f - 0.5f);
+  return f > 0.5f ? f - 0.5f : 0.f;
+}
+
+template <int ROLE>
+__global__ void __launch_bounds__(128) k_n2m_bs_mode1(N2MArgs a) {
+  const Grid &g = a.g;
+  const Nodes &N = a.N;
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= g.nn) return;
+  const int ix = (int)(t / g.yn), iy = (int)(t - (long)ix * g.yn);
+  const int ncy = g.ncy;
+  const long n = a.n;
+  const float *bs = a.bs;
+  Acc sum[5];
+#pragma unroll
+  for (int q = 0; q < 5; q++) sum[q].zero();
+  auto cell_sum = [&](int cx, int cy, int ax, int by) {
+    if (cx < 0 || cx >= g.ncx || cy < 0 || cy >= ncy) return;
+    const float s1 = (1.f / __ldg(g.wx + cx)) / __ldg(g.wy + cy);
+    const long c = (long)cx * ncy + cy;
+    const int sb = __ldg(a.start + c), se = __ldg(a.start + c + 1);
+    for (int s = sb; s < se; s++) {
+      const float u = bs[BS_U * n + s], v = bs[BS_V * n + s];
+      if (ROLE == 0) {
+        const float w = s1 * (ax ? u : 1.f - u) * (by ? v : 1.f - v);
+        sum[0].add(bs[BS_PHIS * n + s] * w); sum[1].add(bs[BS_SXY * n + s] * w);
+        sum[2].add(bs[BS_EXY * n + s] * w); sum[3].add(bs[BS_ES * n + s] * w);
+        sum[4].add(w);
+      } else {
+        const float w = s1 * bs_half(ax, u) * bs_half(by, v);
+        if (w != 0.f) {
+          sum[0].add(bs[BS_PR * n + s] * w); sum[1].add(bs[BS_SXX * n + s] * w);
+          sum[2].add(bs[BS_EXX * n + s] * w); sum[3].add(w);
+        }
+      }
+    }
+  };
+  if (ROLE == 0) {
+    for (int ax = 1; ax >= 0; ax--)
+      for (int by = 1; by >= 0; by--) cell_sum(ix - ax, iy - by, ax, by);
+    const float w = sum[4].value();
+    const float ph = sum[0].value(), sy = sum[1].value(), ey = sum[2].value(), es = sum[3].value();
+    N.f(V2C_NF_PHISUM)[t] = ph; N.f(V2C_NF_SXYSUM)[t] = sy;
+    N.f(V2C_NF_EXYSUM)[t] = ey; N.f(V2C_NF_ESUM)[t] = es; N.f(V2C_NF_WTPHISUM)[t] = w;
+    if (w != 0.f && ix >= 1 && iy >= 1 && ix < g.xn - 1 && iy < g.yn - 1) {
+      N.f(V2C_NF_PHIE)[t] = __fdividef(ph, w); N.f(V2C_NF_SXYEE)[t] = __fdividef(sy, w);
+      N.f(V2C_NF_EXYEE)[t] = __fdividef(ey, w); N.f(V2C_NF_PEE)[t] = __fdividef(es, w);
+    }
+  } else {
+    for (int ax = 2; ax >= 0; ax--)
+      for (int by = 2; by >= 0; by--) cell_sum(ix - ax, iy - by, ax, by);
+    // the first row also gets what the last cell row sends past the end of
+    // the previous columns
+    if (iy == 0)
+      for (int ax = 2; ax >= 0; ax--) cell_sum(ix - 1 - ax, ncy - 1, ax, 2);
+    const float w = sum[3].value();
+    const float ps = sum[0].value(), sx = sum[1].value(), ex = sum[2].value();
+    N.f(V2C_NF_PSUM)[t] = ps; N.f(V2C_NF_SXXSUM)[t] = sx;
+    N.f(V2C_NF_EXXSUM)[t] = ex; N.f(V2C_NF_WTSXXSUM)[t] = w;
+    if (w != 0.f && ix >= 1 && iy >= 1) {
+      N.f(V2C_NF_SPPEE)[t] = __fdividef(ps, w); N.f(V2C_NF_SXXEE)[t] = __fdividef(sx, w);
+      N.f(V2C_NF_EXXEE)[t] = __fdividef(ex, w);
+    }
+  }
+}
+
 // ----------------------------------------------------------- the move
 // moveandrotatemarkers (moveandrotatemarkers.c:1-178), one thread per
 // marker in cell order: Euler or RK4 through allinteri, stress rotation,
@@ -595,7 +684,14 @@ __global__ void __launch_bounds__(256) k_move(N2MArgs a) {
 
 void launch_n2m(const N2MArgs &a, cudaStream_t st) {
   dim3 grid((a.g.xn + a.TX - 1) / a.TX, (a.g.yn + TY - 1) / TY);
-  k_n2m<<<grid, NTH, 0, st>>>(a);
+  if (!a.bs) {
+    k_n2m<false><<<grid, NTH, 0, st>>>(a);
+  } else {
+    k_n2m<true><<<grid, NTH, 0, st>>>(a);
+    const unsigned nb = (unsigned)((a.g.nn + 127) / 128);
+    k_n2m_bs_mode1<0><<<nb, 128, 0, st>>>(a);
+    k_n2m_bs_mode1<1><<<nb, 128, 0, st>>>(a);
+  }
 }
 
 void launch_move(const N2MArgs &a, cudaStream_t st) {
