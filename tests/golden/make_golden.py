@@ -1,8 +1,9 @@
 """Generate tests/golden/ref_micro.npz: inputs and outputs of the reference's
 own routines (compiled from its sources by oracle/build_ref.sh) on two micro
 cases, for pinning the oracle restatement where the reference is absent,
-and the restart file (.prn) the reference's save_model wrote after the step
-on the first case.
+the restart file (.prn) the reference's save_model wrote after the step
+on the first case, and the Stokes matrix its preparematrix assembled on
+that case.
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -46,6 +47,16 @@ def main():
         out[f"{name}/marks_out"] = np.stack([res["marks"][k] for k in range(abi.MF_N)])
         if name == "default":
             out[f"{name}/prn"] = np.frombuffer(res["prn"], dtype=np.uint8)
+    # the Stokes matrix the reference's preparematrix assembles on the first
+    # case after marker2nodes, compute_before_solve and basic2center
+    c = micro(7)
+    dt = float(c.params["timestep"])
+    ctl = dict(abi.STOKES_DEFAULTS, mukoef=dt * 30e5, dt=dt)
+    res = B.run_reference(c, stages=(1 << 0) | (1 << 2) | (1 << 7) | B.STOKES_STAGE,
+                          nthreads=1, stokes=ctl)["stokes"]
+    out["stokes/ctl"] = np.array(json.dumps(ctl, sort_keys=True))
+    for k in ("ia", "ja", "a", "b"):
+        out[f"stokes/{k}"] = res[k]
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "ref_micro.npz")
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path))

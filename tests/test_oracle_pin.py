@@ -193,6 +193,29 @@ def test_stokes_assembly_bit_exact_vs_reference(variant):
     assert ref["ja"].size > 10 * c.nodenum
 
 
+def test_stokes_assembly_matches_golden():
+    """The reference's preparematrix on the micro case (committed fixture)
+    against the restatement, after the same marker2nodes,
+    compute_before_solve and basic2center."""
+    z = np.load(GOLDEN)
+    p = synth.default_params()
+    p.update(json.loads(str(z["default/params"])))
+    nodes = {k: z["default/nodes_in"][k].copy() for k in range(abi.NF_N)}
+    marks = {k: z["default/marks_in"][k].copy() for k in range(abi.MF_N)}
+    c = synth.Case("default", p, z["default/gx"], z["default/gy"], z["default/rt"], nodes, marks,
+                   z["default/markt"].copy(), z["default/bondm"], z["default/bondn"],
+                   z["default/bondv"])
+    ctl = json.loads(str(z["stokes/ctl"]))
+    r = oracle.Restatement(c)
+    r.marker2nodes()
+    r.compute_before_solve(ctl["dt"], 0)
+    r.basic2center()
+    rc, ours = r.stokes_assemble(**ctl)
+    assert rc == 0
+    for k in ("ia", "ja", "a", "b"):
+        assert np.array_equal(ours[k], z[f"stokes/{k}"], equal_nan=k in ("a", "b")), k
+
+
 def test_stokes_assembly_open_edge_is_refused():
     """A Stokes row on the model's edge would index past the grid in the
     reference; the restatement refuses it."""
