@@ -809,6 +809,7 @@ extern "C" int v2c_marker2nodes(v2c_ctx *ctx) {
   a.gxf = ctx->d_gxf;
   a.gyf = ctx->d_gyf;
   a.TX = pick_tx(ctx);
+  a.n = ctx->n;
   CK(cudaMemsetAsync(ctx->d_sticky, 0, sizeof(uint32_t) * ctx->nn, st));
   ctx->dsxx_valid = false;  // the scatter writes sxxe
   {

@@ -64,6 +64,7 @@ struct M2NArgs {
   unsigned long long *stat;
   const float *gxf, *gyf;  // FP32 line positions (coarse band test)
   int TX;
+  long n = 0;  // markers (chooses the sweep's occupancy)
 };
 void launch_m2n(const M2NArgs &a, cudaStream_t st);
 

@@ -294,7 +294,11 @@ __device__ __forceinline__ void node_tail(const M2NArgs &a, int role, int ci, in
   }
 }
 
-__global__ void __launch_bounds__(NTH, 7) k_m2n(M2NArgs a) {
+// MINB resident CTAs per SM: 7 (72 registers) hides more latency at 20
+// markers per cell; at 16 or fewer the lanes' shared-memory bank conflicts
+// dominate and 6 (80 registers, no spills) is faster (measured at 20 and 16)
+template <int MINB>
+__global__ void __launch_bounds__(NTH, MINB) k_m2n(M2NArgs a) {
   __shared__ Smem sm;
   const Grid &g = a.g;
   const int tid = threadIdx.x, role = tid / TY, jl = tid % TY;
@@ -618,7 +622,9 @@ void launch_m2n(const M2NArgs &a, cudaStream_t st) {
     return;
   }
   dim3 grid((a.g.xn + a.TX - 1) / a.TX, (a.g.yn + TY - 1) / TY);
-  k_m2n<<<grid, NTH, 0, st>>>(a);
+  const long ncell = (long)a.g.ncx * a.g.ncy;
+  if (a.n > 16 * ncell + ncell / 2) k_m2n<7><<<grid, NTH, 0, st>>>(a);
+  else k_m2n<6><<<grid, NTH, 0, st>>>(a);
 }
 
 void launch_sticky(const Nodes &N, const uint32_t *key, long nn, cudaStream_t st) {
