@@ -1096,7 +1096,7 @@ extern "C" int v2c_stokes_assemble(v2c_ctx *ctx, const v2c_stokes_ctl *ctl, long
   if (rows + 1 > 0x7fffffffL) return fail(ctx, V2C_ERR_CAPACITY);
   cudaStream_t st = ctx->stream;
   const long nb = ctx->bondnum;
-  DevBuf bm, bn, bv, cnt, rhs, bsum, err, dja, da;
+  DevBuf bm, bn, bv, cnt, rhs, bsum, err, dja, da, ecol, evalb;
   CK(bm.alloc<long>(ctx->nn * 4));
   CK(bn.alloc<long>(nb * 3));
   CK(bv.alloc<double>(nb * 4));
@@ -1135,6 +1135,16 @@ extern "C" int v2c_stokes_assemble(v2c_ctx *ctx, const v2c_stokes_ctl *ctl, long
   s.b = rhs.get<double>();
   s.ja = nullptr;
   s.a = nullptr;
+  s.ell_col = nullptr;
+  s.ell_val = nullptr;
+  if (ja) {
+    // the caller has room for the coefficients: the count pass keeps the
+    // rows, so the FP64 work is done once
+    CK(ecol.alloc<int32_t>(rows * STOKES_ROW_MAX));
+    CK(evalb.alloc<double>(rows * STOKES_ROW_MAX));
+    s.ell_col = ecol.get<int32_t>();
+    s.ell_val = evalb.get<double>();
+  }
   s.err = err.get<int>();
   int h_err = 0;
   int32_t total = 0;

@@ -44,9 +44,14 @@ struct StokesArgs {
   int32_t *cnt;        // [3 nodenum + 1]: coefficients per row, then row starts
   int32_t *ja;         // [nnz] (fill pass)
   double *a;           // [nnz] (fill pass)
+  // rows kept by the count pass (STOKES_ROW_MAX entries per row), so that
+  // the fill pass only moves them; null: the fill pass rebuilds each row
+  int32_t *ell_col;
+  double *ell_val;
   double *b;           // [3 nodenum]
   int *err;            // set where the reference stops or a row leaves the grid
 };
+constexpr int STOKES_ROW_MAX = 24;
 void launch_stokes_count(const StokesArgs &a, cudaStream_t st);
 void launch_stokes_fill(const StokesArgs &a, cudaStream_t st);
 

@@ -8,7 +8,9 @@
 // columns in increasing order, the terms of one column summed in list order
 // starting from zero, zero terms and zero sums left out.  Two passes: the
 // first counts each row's coefficients (and writes the right-hand side), a
-// scan turns counts into row starts, the second writes columns and values.
+// scan turns counts into row starts, the second writes columns and values;
+// when the caller gives room for the coefficients the first pass also keeps
+// each row (at most 24 entries) and the second only moves it.
 //
 // FP64 throughout, in the reference's evaluation order, and this file is
 // compiled without multiply-add contraction, so a coefficient is the
@@ -20,7 +22,7 @@ namespace v2c {
 namespace {
 
 // terms of one equation: continuity 5, Stokes 3 + 4 x 4 + 5 drunken sailor
-constexpr int MAXT = 24;
+constexpr int MAXT = STOKES_ROW_MAX;
 
 enum { ERR_OUTSIDE = 1, ERR_BOUNDARY = 2 };
 
@@ -332,7 +334,25 @@ __global__ void k_stokes_count(StokesArgs a) {
   const int n = form_row(E);
   a.cnt[r] = n;
   if (a.b) a.b[r] = E.c;
+  if (a.ell_col) {
+    for (int i = 0; i < n; i++) {
+      a.ell_col[r * MAXT + i] = (int32_t)(E.col[i] + 1);
+      a.ell_val[r * MAXT + i] = E.w[i];
+    }
+  }
   if (bad) atomicOr(a.err, bad);
+}
+
+// the rows the count pass kept, moved to their CSR positions
+__global__ void k_stokes_move(StokesArgs a) {
+  const long rows = 3 * a.g.nn;
+  const long r = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  const long s = a.cnt[r], n = a.cnt[r + 1] - s;
+  for (int i = 0; i < n; i++) {
+    a.ja[s + i] = a.ell_col[r * MAXT + i];
+    a.a[s + i] = a.ell_val[r * MAXT + i];
+  }
 }
 
 __global__ void k_stokes_fill(StokesArgs a) {
@@ -362,7 +382,9 @@ void launch_stokes_count(const StokesArgs &a, cudaStream_t st) {
 
 void launch_stokes_fill(const StokesArgs &a, cudaStream_t st) {
   const long rows = 3 * a.g.nn;
-  if (rows > 0) k_stokes_fill<<<nblk(rows, 128), 128, 0, st>>>(a);
+  if (rows <= 0) return;
+  if (a.ell_col) k_stokes_move<<<nblk(rows, 256), 256, 0, st>>>(a);
+  else k_stokes_fill<<<nblk(rows, 128), 128, 0, st>>>(a);
 }
 
 }  // namespace v2c
