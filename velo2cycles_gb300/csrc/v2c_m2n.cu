@@ -520,8 +520,17 @@ __global__ void __launch_bounds__(128) k_m2n_mode1(M2NArgs a) {
       if (ROLE == 3 && ax < 0 && by < 0) continue;  // (1, 1): no stencil reaches
       const float s1 = iwx / __ldg(g.wy + cy);
       const long c = (long)cx * ncy + cy;
-      const int sb = __ldg(a.start + c), se = __ldg(a.start + c + 1);
-      for (int s = sb; s < se; s++) {
+      // quarter classes (2 (v > 1/2) + (u > 1/2)) that can have weight:
+      // a half-cell factor k = 0 needs the lower half, k = 2 the upper
+      constexpr int UX[3] = {0x5, 0xf, 0xa}, VY[3] = {0x3, 0xf, 0xc};
+      int mask = 0xf;
+      if (ROLE == 2) mask = UX[ax] & VY[by];
+      if (ROLE == 3) mask = (ax >= 0 ? VY[by + 1] : 0) | (by >= 0 ? UX[ax + 1] : 0);
+      const int4 qs = __ldg(a.qstart + c);
+      const int qb[5] = {qs.x, qs.y, qs.z, qs.w, __ldg(a.start + c + 1)};
+      for (int q = 0; q < 4; q++) {
+        if (!((mask >> q) & 1)) continue;
+      for (int s = qb[q]; s < qb[q + 1]; s++) {
         const int idx = __ldg(a.perm + s);
         const float u = a.m.u_in[idx], v = a.m.v_in[idx];
         if (!marker_active(g, cx, cy, u, v)) continue;
@@ -567,6 +576,7 @@ __global__ void __launch_bounds__(128) k_m2n_mode1(M2NArgs a) {
             }
           }
         }
+      }
       }
     }
   }
