@@ -129,8 +129,24 @@ __device__ __forceinline__ int4 rank_segment(const uint32_t *tmp, int32_t *perm,
     const uint32_t val = (jj < L) ? tmp[jj] : 0xffffffffu;
     int rank = 0;
     if (L <= 32) {
+      // bitonic sort of the warp's keys (padding 0xffffffff sorts last:
+      // array indices stay below 2^30 - 1, so no key equals it)
+      uint32_t key = val;
 #pragma unroll
-      for (int k = 0; k < 32; k++) rank += (__shfl_sync(V2C_FULL, val, k) < val);
+      for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+          const uint32_t other = __shfl_xor_sync(V2C_FULL, key, j);
+          const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+          key = keep_min ? min(key, other) : max(key, other);
+        }
+      const bool in = lane < L;
+      const uint32_t q = key >> 30;
+      cnt.x += __popc(__ballot_sync(V2C_FULL, in && q == 0));
+      cnt.y += __popc(__ballot_sync(V2C_FULL, in && q == 1));
+      cnt.z += __popc(__ballot_sync(V2C_FULL, in && q == 2));
+      if (in) perm[lane] = (int32_t)(key & KEY_INDEX);
+      continue;
     } else {
       for (int b2 = 0; b2 < L; b2 += 32) {
         const uint32_t other = (b2 + lane < L) ? tmp[b2 + lane] : 0xffffffffu;
