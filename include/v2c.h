@@ -538,7 +538,14 @@ int v2c_mlp_infer(v2c_ctx *ctx, const double *states_dev, long n, float *out_dev
  * streams makes that first call before it begins capturing.  There is one
  * scratch per device: calls that overlap on the same device (different
  * streams or host threads without ordering between them) race on it and give
- * wrong results, so order them. */
+ * wrong results, so order them.  Cost: each cell's segment is put in index
+ * order by one warp, in registers up to 32 markers and by a bitonic network
+ * in global memory above that, O(L log^2 L) for L markers in the cell; a
+ * grid with markers piled into a few cells (for example all of them outside
+ * the grid, clamped into a corner cell) is sorted far more slowly than one
+ * with a few tens of markers per cell.  A CUDA error left pending by earlier
+ * work makes the call return V2C_ERR_CUDA before it queues anything, leaving
+ * that error in place. */
 /* 4 Mi cells: a 4001 x 1001 line grid (4 000 000 cells) fits */
 #define V2C_STATIC_SORT_MAX_CELLS 4194304
 int v2c_sort_cells_static(const double *gx_dev, long xnumx, const double *gy_dev,

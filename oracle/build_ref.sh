@@ -5,19 +5,20 @@
 #  2. oracle/_ref/v2c_ref      -- the reference's own hot-path routines,
 #     compiled from its sources with oracle/ref_harness.c.
 #
-# For (2) the reference sources are copied from $V2C_REFERENCE/src (default
-# /root/reference/src) into oracle/_ref/src, raising only the array-size
-# macros of headevps.c so larger grids and marker sets fit.  That staging
-# directory is git-ignored; it exists so the same recipe can rebuild the
-# binary on a machine without the reference tree.  When neither the tree nor
-# a staged copy is present only (1) is built.
+# For (2) the reference sources are copied from $V2C_REFERENCE/src (set
+# V2C_REFERENCE to the reference checkout, the directory that holds src/)
+# into oracle/_ref/src, raising only the array-size macros of headevps.c so
+# larger grids and marker sets fit.  That staging directory is git-ignored;
+# it exists so the same recipe can rebuild the binary on a machine without
+# the reference tree.  With V2C_REFERENCE unset the staged copy is used;
+# when neither is present only (1) is built.
 #
 # Both are compiled with -ffp-contract=off so FP64 arithmetic is evaluated
 # exactly as written on every host architecture.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
-REF="${V2C_REFERENCE:-/root/reference}"
+REF="${V2C_REFERENCE:-}"
 CC="${CC:-gcc}"
 mkdir -p "$OUT"
 
@@ -29,7 +30,7 @@ density_ductilevisc_calc.c moveandrotatemarkers.c \
 momentum_continuity_addmatrix_checkerror.c momentum_continuity_iterate.c \
 temperature_iterate.c plastic.c recalc_marker_properties.c load_save.c"
 
-if [ -d "$REF/src" ]; then
+if [ -n "$REF" ] && [ -d "$REF/src" ]; then
   mkdir -p "$OUT/src"
   for f in $FILES; do cp "$REF/src/$f" "$OUT/src/$f"; done
   # grid up to 1100 x 420 lines, 6.5 M markers; the Stokes matrix arrays

@@ -25,6 +25,30 @@ def test_oversize_grid_rejected_before_any_device_work(built_lib):
                                        None) == abi.ERR_ARG  # fits; fails only on the pointers
 
 
+def test_huge_line_counts_rejected_without_overflow(built_lib):
+    """Line counts whose cell product would overflow 64 bits, or whose
+    factors exceed an int, are refused as over capacity before any product
+    is formed."""
+    from velo2cycles_gb300._lib import lib
+    big = 1 << 40
+    assert lib().v2c_sort_cells_static(None, big, None, big, None, None, 0, None, None, None,
+                                       None) == abi.ERR_CAPACITY
+    assert lib().v2c_sort_cells_static(None, 3, None, (1 << 62), None, None, 0, None, None, None,
+                                       None) == abi.ERR_CAPACITY
+
+
+def test_wrapper_rejects_host_tensors(built_lib):
+    """Host (CPU) tensors never reach the library: the kernels would be
+    handed host addresses."""
+    torch = pytest.importorskip("torch")
+    g = torch.linspace(0, 1, 5, dtype=torch.float64)
+    x = torch.zeros(3, dtype=torch.float64)
+    i3 = torch.zeros(3, dtype=torch.int32)
+    start = torch.zeros(17, dtype=torch.int32)
+    with pytest.raises(ValueError, match="CUDA device"):
+        cellsort.sort_cells_static(g, g, x, x, i3, i3.clone(), start)
+
+
 def _expected(case):
     """cells, start, perm and max cell count from the context path."""
     m = mic.from_case(case)

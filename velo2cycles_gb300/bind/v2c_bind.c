@@ -14,7 +14,10 @@
 #include "v2c_bind.h"
 #include "v2c_bind_map.h"
 
-int v2c_bind_sync_markers = 1;
+/* 0: host marker arrays are refreshed only by v2c_bind_markers_to_host()
+ * (the host reads them only to save or post-process); 1: after every call
+ * that changes them (a full marker download per call) */
+int v2c_bind_sync_markers = 0;
 
 static v2c_ctx *v2c_bind_ctx = NULL;
 static int v2c_bind_have_markers = 0;  /* device markers current */

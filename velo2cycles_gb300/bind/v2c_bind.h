@@ -27,9 +27,12 @@
  * carry FP32 precision.  The markers live on the GPU between calls: they
  * are uploaded on the first call and after v2c_bind_markers_changed(), and
  * the host marker arrays (positions, T, strain, pressure, stresses, strain
- * rates, velocities, state, cohesion) are refreshed after every call that
- * changes them when v2c_bind_sync_markers is 1 (the default), or only by
- * v2c_bind_markers_to_host() when it is 0.  The per-marker friction
+ * rates, velocities, state, cohesion) are refreshed only by
+ * v2c_bind_markers_to_host() when v2c_bind_sync_markers is 0 (the default):
+ * call it before save_model, postproc or any other host code that reads
+ * marker arrays.  With v2c_bind_sync_markers = 1 they are refreshed after
+ * every call that changes them, a full marker download per call.  The
+ * per-marker friction
  * parameters the reference stores (mark_a, mark_b, mark_L, mark_L0,
  * mark_V0, markC0, fric_static) are recomputed from position on the GPU and
  * are not written back.

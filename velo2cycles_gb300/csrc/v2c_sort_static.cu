@@ -192,35 +192,54 @@ extern "C" int v2c_sort_cells_static(const double *gx_dev, long xnumx, const dou
                                      long ynumy, const double *x_dev, const double *y_dev,
                                      long n, int32_t *cell_dev, int32_t *perm_dev,
                                      int32_t *start_dev, void *cuda_stream) {
-  // sizes first: nothing below the limits reaches the device
+  // sizes first: nothing below the limits reaches the device.  Each factor
+  // is bounded before the product is formed, so no size overflows `long` or
+  // the int the kernels take.
   if (xnumx < 2 || ynumy < 2 || n < 0 || n > INT_MAX) return V2C_ERR_ARG;
-  const long ncell = (xnumx - 1) * (ynumy - 1);
-  if (ncell > MAX_CELLS) {
+  if (xnumx - 1 > MAX_CELLS || ynumy - 1 > MAX_CELLS / (xnumx - 1)) {
     fprintf(stderr,
-            "v2c_sort_cells_static: %ld x %ld grid lines give %ld cells, more than the %ld "
+            "v2c_sort_cells_static: %ld x %ld grid lines give more than the %ld cells "
             "(V2C_STATIC_SORT_MAX_CELLS) its fixed scratch holds; use the context path\n",
-            xnumx, ynumy, ncell, MAX_CELLS);
+            xnumx, ynumy, MAX_CELLS);
     return V2C_ERR_CAPACITY;
   }
+  const long ncell = (xnumx - 1) * (ynumy - 1);
   if (!gx_dev || !gy_dev || !start_dev || (n > 0 && (!x_dev || !y_dev || !cell_dev || !perm_dev)))
     return V2C_ERR_ARG;
+  // An error another caller left pending would be reported as this call's
+  // own by the checks after each launch below: refuse to start instead, and
+  // leave that error in place for its owner.
+  if (cudaPeekAtLastError() != cudaSuccess) {
+    fprintf(stderr, "v2c_sort_cells_static: an earlier CUDA error is pending (%s); not started\n",
+            cudaGetErrorString(cudaPeekAtLastError()));
+    return V2C_ERR_CUDA;
+  }
   int32_t *scratch = nullptr;
   if (int rc = scratch_for_current_device(&scratch)) return rc;
   int32_t *count = scratch, *bsum = scratch + MAX_CELLS;
   cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  // status of the launch just queued (nothing was pending on entry)
+  auto launched = []() { return cudaGetLastError() == cudaSuccess; };
 
   if (cudaMemsetAsync(count, 0, sizeof(int32_t) * ncell, st) != cudaSuccess) return V2C_ERR_CUDA;
-  if (n > 0)
+  if (n > 0) {
     k_assign_count<<<nblk(n, 256), 256, 0, st>>>(gx_dev, (int)xnumx, gy_dev, (int)ynumy, x_dev,
                                                  y_dev, n, cell_dev, count);
+    if (!launched()) return V2C_ERR_CUDA;
+  }
   const long nb = (ncell + SB * SE - 1) / (SB * SE);
   k_scan_block_s<<<(unsigned)nb, SB, 0, st>>>(count, ncell, start_dev, bsum);
+  if (!launched()) return V2C_ERR_CUDA;
   k_scan_sums_s<<<1, SB, 0, st>>>(bsum, (int)nb, start_dev + ncell);
+  if (!launched()) return V2C_ERR_CUDA;
   k_scan_add_s<<<nblk(ncell, 256), 256, 0, st>>>(start_dev, ncell, bsum);
+  if (!launched()) return V2C_ERR_CUDA;
   if (n > 0) {
     if (cudaMemsetAsync(count, 0, sizeof(int32_t) * ncell, st) != cudaSuccess) return V2C_ERR_CUDA;
     k_fill<<<nblk(n, 256), 256, 0, st>>>(cell_dev, n, start_dev, count, perm_dev);
+    if (!launched()) return V2C_ERR_CUDA;
     k_order_cells<<<nblk(ncell * 32, 256), 256, 0, st>>>(start_dev, ncell, perm_dev);
+    if (!launched()) return V2C_ERR_CUDA;
   }
-  return cudaGetLastError() == cudaSuccess ? V2C_OK : V2C_ERR_CUDA;
+  return V2C_OK;
 }
