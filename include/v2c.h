@@ -64,7 +64,9 @@ typedef struct v2c_params {
   int densimod;             /* [0]                                           */
   int RSFmode;              /* [1]                                           */
   int power_law_RSF;        /* [0]                                           */
-  int rkmod;                /* [0]                                           */
+  int rkmod;                /* [0] 0 Picard, 1 Lapusta average, 2 RK2, 3 RK4:
+                                the slip rate compute_before_solve's pass rk
+                                takes (calc_RSF.c:46-86)                    */
   int stickymod;            /* [1]                                           */
   int inertyn;              /* [0] radiation damping on                       */
   int pmode;                /* [0] normal stress = nstress                    */

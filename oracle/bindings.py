@@ -18,8 +18,10 @@ def restatement_path() -> str:
     return os.path.join(OUT, "liboracle.so")
 
 
-def reference_path() -> str:
-    return os.path.join(OUT, "v2c_ref")
+def reference_path(serial: bool = False) -> str:
+    """The reference routines built with OpenMP (v2c_ref), or with the
+    OpenMP pragmas ignored (v2c_ref_serial)."""
+    return os.path.join(OUT, "v2c_ref_serial" if serial else "v2c_ref")
 
 
 def _stale() -> bool:
@@ -61,6 +63,7 @@ class _State(ctypes.Structure):
         ("bondnum", ctypes.c_long),
         ("nthreads", ctypes.c_int),
         ("phantom", ctypes.c_int),
+        ("cap", ctypes.c_long),
     ]
 
 
@@ -129,14 +132,20 @@ def _lib():
 class Restatement:
     """Runs the C restatement on a copy of a synth.Case (arrays updated in place)."""
 
-    def __init__(self, case, nthreads: int = 1, phantom: bool = False):
+    def __init__(self, case, nthreads: int = 1, phantom: bool = False, cap: int = 0):
+        """cap: room for markers beyond case.n (immobile markers append
+        markers in the move); marks/markt show the current markers."""
         self.case = case
         self.lib = _lib()
         c = case
         self._keep = []
+        cap = max(int(cap), c.n)
         self.nodes = {f: np.ascontiguousarray(c.nodes[f], dtype=np.float64) for f in range(abi.NF_N)}
-        self.marks = {f: np.ascontiguousarray(c.marks[f], dtype=np.float64) for f in range(abi.MF_N)}
-        self.markt = np.ascontiguousarray(c.markt, dtype=np.int8)
+        self._marks = {f: np.zeros(max(cap, 1)) for f in range(abi.MF_N)}
+        self._markt = np.zeros(max(cap, 1), dtype=np.int8)
+        for f in range(abi.MF_N):
+            self._marks[f][:c.n] = c.marks[f]
+        self._markt[:c.n] = c.markt
         self.gx = np.ascontiguousarray(c.gx, dtype=np.float64)
         self.gy = np.ascontiguousarray(c.gy, dtype=np.float64)
         self.rt = np.ascontiguousarray(c.rt, dtype=np.float64)
@@ -149,9 +158,10 @@ class Restatement:
         for f in range(abi.NF_N):
             st.N[f] = _dp(self.nodes[f])
         for f in range(abi.MF_N):
-            st.M[f] = _dp(self.marks[f])
-        st.t = self.markt.ctypes.data_as(ctypes.POINTER(ctypes.c_byte))
+            st.M[f] = _dp(self._marks[f])
+        st.t = self._markt.ctypes.data_as(ctypes.POINTER(ctypes.c_byte))
         st.n = c.n
+        st.cap = cap
         st.bondm = self.bondm.ctypes.data_as(ctypes.POINTER(ctypes.c_long))
         st.bondn = self.bondn.ctypes.data_as(ctypes.POINTER(ctypes.c_long))
         st.bondv = _dp(self.bondv)
@@ -159,6 +169,18 @@ class Restatement:
         st.nthreads = nthreads
         st.phantom = int(phantom)
         self.st = st
+
+    @property
+    def n(self) -> int:
+        return int(self.st.n)
+
+    @property
+    def marks(self) -> dict:
+        return {f: a[:self.st.n] for f, a in self._marks.items()}
+
+    @property
+    def markt(self) -> np.ndarray:
+        return self._markt[:self.st.n]
 
     def set_params(self, **kw):
         d = self.st.p.to_dict()
@@ -328,6 +350,14 @@ STOKES_STAGE = 1 << 13
 STOKES_KEYS = ("mukoef", "dt", "gxkoef", "gykoef", "timebond", "drunkensailor")
 
 
+def picard_passes(npass: int) -> int:
+    """Stage bits asking for npass Picard passes (rk = 0 .. npass-1) of
+    compute_before_solve + compute_after_solve after marker2nodes and
+    interpolate_center2basic_old (with STAGE_BEFORE and STAGE_AFTER)."""
+    assert 0 < npass < 16
+    return npass << 16
+
+
 def write_case(path: str, case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0,
                timestep=None, oldornew=0, dts=None, heatdif=None, stokes=None) -> None:
     """timestep: v2c_timestep_ctl values as a dict (abi.TIMESTEP_DEFAULTS when
@@ -395,9 +425,11 @@ def read_result(path: str, nodenum: int):
 
 
 def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeout=3600,
-                  timestep=None, oldornew=0, dts=None, heatdif=None, stokes=None):
+                  timestep=None, oldornew=0, dts=None, heatdif=None, stokes=None,
+                  serial=False):
     """Run the reference routines on `case`; returns the arrays after the
-    stages plus per-stage seconds summed over the timed steps."""
+    stages plus per-stage seconds summed over the timed steps.  serial: the
+    build with the OpenMP pragmas ignored."""
     if not reference_available():
         build()
     if not reference_available():
@@ -407,7 +439,7 @@ def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeo
         write_case(cp, case, stages, nthreads, nsteps, warmup, timestep, oldornew, dts, heatdif,
                    stokes)
         env = dict(os.environ, OMP_NUM_THREADS=str(max(1, nthreads)))
-        r = subprocess.run([reference_path(), cp, rp], env=env, capture_output=True,
+        r = subprocess.run([reference_path(serial), cp, rp], env=env, capture_output=True,
                            timeout=timeout, cwd=d)
         if r.returncode != 0:
             raise RuntimeError(f"v2c_ref failed ({r.returncode}): {r.stderr.decode()[-2000:]}")

@@ -1,5 +1,5 @@
 #!/bin/sh
-# Build recipe for the two CPU checkers (test infrastructure only):
+# Build recipe for the CPU checkers (test infrastructure only):
 #
 #  1. oracle/_ref/liboracle.so -- the C restatement oracle/v2c_oracle.c.
 #  2. oracle/_ref/v2c_ref      -- the reference's own hot-path routines,
@@ -49,6 +49,14 @@ if [ -f "$OUT/src/headevps.c" ]; then
   case "$(uname -m)" in x86_64) MODEL="-mcmodel=medium" ;; esac
   $CC -std=gnu99 -O3 -fopenmp -fcommon -w -ffp-contract=off $MODEL \
       -I"$OUT/src" -I"$HERE/../include" -o "$OUT/v2c_ref" "$HERE/ref_harness.c" -lm
+  # 3. oracle/_ref/v2c_ref_serial -- the same sources with the OpenMP
+  #    pragmas ignored (libgomp linked only for omp_get_wtime): the routines
+  #    as written for one thread.  moveandrotatemarkers appends spawned
+  #    markers through a reduction variable, which under OpenMP starts from
+  #    0 in every thread; this build pins the restatement's serial reading.
+  $CC -std=gnu99 -O3 -fopenmp-simd -fcommon -w -ffp-contract=off $MODEL \
+      -I"$OUT/src" -I"$HERE/../include" -o "$OUT/v2c_ref_serial" "$HERE/ref_harness.c" \
+      -lgomp -lm
 else
   echo "build_ref.sh: reference sources not found; built the restatement only" >&2
 fi

@@ -84,7 +84,8 @@ static int ref_load_case(const char *path, ref_case *C) {
       memcpy(rock_row(r), rt + (long)r * V2C_MAXTMR, sizeof(double) * V2C_MAXTMR);
     }
   }
-  double *scratch = (double *)malloc(sizeof(double) * ((n > nn ? n : nn) + 1));
+  /* a move can at most double the markers (one spawn per immobile one) */
+  double *scratch = (double *)malloc(sizeof(double) * ((2 * n > nn ? 2 * n : nn) + 1));
   C->scratch = scratch;
   /* fields the reference has no array for are read into scratch */
   for (int k = 0; k < V2C_NF_N; k++) rd(node_array(k) ? node_array(k) : scratch, sizeof(double), nn, f);

@@ -94,7 +94,10 @@ int main(int argc, char **argv) {
   ref_case C;
   int rc = ref_load_case(argv[1], &C);
   if (rc) return rc;
-  int nthreads = C.nthreads, stages = C.stages, nsteps = C.nsteps, warmup = C.warmup;
+  int nthreads = C.nthreads, stages = C.stages & 0xffff, nsteps = C.nsteps, warmup = C.warmup;
+  /* stage bits 16-19: number of Picard passes of compute_before_solve /
+   * compute_after_solve (0: one pass at rk = 0 with the other stages) */
+  const int npass = (C.stages >> 16) & 0xf;
   omp_set_num_threads(nthreads > 0 ? nthreads : 1);
   if (!freopen("/dev/null", "w", stdout)) return 5;
 
@@ -114,11 +117,22 @@ int main(int argc, char **argv) {
   }
     STAGE(0, 0, marker2nodes());
     STAGE(1, 1, interpolate_center2basic_old(timestep));
+    if (npass > 0) {
+      /* Picard passes rk = 0 .. npass-1 of the node routines (the order of
+       * momentum_continuity_iterate.c:67-91 without the Stokes solve): each
+       * pass's compute_after_solve leaves the slip rate the next pass's
+       * compute_before_solve takes (calc_RSF.c:58-86) */
+      for (int rk = 0; rk < npass; rk++) {
+        STAGE(2, 2, compute_before_solve(timestep, rk));
+        STAGE(3, 3, deltas = compute_after_solve(timestep, rk));
+      }
+    } else {
     STAGE(2, 2, compute_before_solve(timestep, 0));
     STAGE(7, 7, interpolate_basic2center());
     STAGE(9, 7, recompute_stress_strainrate(timestep, 0));
     STAGE(8, 7, interpolate_center2basic(timestep));
     STAGE(3, 3, deltas = compute_after_solve(timestep, 0));
+    }
     STAGE(10, 7, copyarrays(0));
     if (stages & (1 << 11)) {
       /* solve_temperature (temperature_iterate.c:2-412) with the solver

@@ -937,7 +937,11 @@ int v2c_oracle_marker_temperature(v2c_oracle_state *s, double heatdif) {
   return 0;
 }
 
-/* calc_vpvisc, calc_RSF.c:33-169 (rkmod 0 and 1) */
+/* calc_vpvisc, calc_RSF.c:33-169.  The state rate dphidt it selects per
+ * rkmod is never used by the reference (it is only printed on error), nor
+ * are the RK_sliprs/RK_phidts histories rkmod 3 stores (calc_RSF.c:72-76,
+ * read only into that dphidt at :84-86): the slip rate V is what each
+ * pass takes. */
 static double vpvisc(v2c_oracle_state *s, int rk, double dt, long m3, double nP,
                      double W, int *err) {
   const v2c_params *p = &s->p;
@@ -961,6 +965,10 @@ static double vpvisc(v2c_oracle_state *s, int rk, double dt, long m3, double nP,
       V = N[V2C_NF_RK_SLIPRS_SOLVED][m3];
       if (p->RSFmode == 1) dphidt = N[V2C_NF_RK_PHIDTS_SOLVED][m3];
     }
+  }
+  if (rk == 3 && p->rkmod == 3) {
+    V = N[V2C_NF_RK_SLIPRS_SOLVED][m3];
+    if (p->RSFmode == 1) dphidt = N[V2C_NF_RK_PHIDTS_SOLVED][m3];  /* (the reference's 1/6 average) */
   }
   (void)dphidt;
   N[V2C_NF_PES][m3] = N[V2C_NF_PE][m3] + V / W * dt;
@@ -1414,20 +1422,28 @@ static void allinteri(const v2c_oracle_state *s, double x, double y, double *VX,
   *VY += ((1.0 - e) * (1.0 - n) * vy[m3] + (1.0 - e) * n * vy[m3 + 1] + e * (1.0 - n) * vy[m3 + yn] + e * n * vy[m3 + yn + 1]) * xrat;
 }
 
-/* moveandrotatemarkers.c:1-178 for mobile markers (type < 100).  Immobile
- * marker spawning (:90-136) and the compaction it triggers (:143-173) are
- * not restated: a type >= 100 marker returns V2C_ERR_UNSUPPORTED. */
+/* moveandrotatemarkers.c:1-178.  Immobile markers (type >= 100) keep their
+ * anchor in markk (x) and markv (y); one that moves inside the model spawns
+ * a mobile marker of type - 100 there, appended after the last marker with
+ * its temperature, strain, stresses, pressure and strain rates reset, and
+ * goes back to its anchor, as it does when it strays more than ystpy from
+ * it (:90-136).  Then out-of-model mobile markers, in index order, take the
+ * appended markers from the last one back (:141-171).  This is the routine
+ * as written for one thread: the reference's OpenMP build makes the append
+ * index marknum1 a reduction variable, whose private copies start from 0,
+ * so there the spawned markers overwrite markers 0, 1, ... instead. */
 int v2c_oracle_move(v2c_oracle_state *s) {
   const v2c_params *p = &s->p;
   double **M = s->M;
   double dt = p->timestep;
+  const long cap = s->cap > s->n ? s->cap : s->n;
+  long marknum1 = s->n;
   for (long mm1 = 0; mm1 < s->n; mm1++) {
     int mm2 = s->t[mm1];
     double x = M[V2C_MF_X][mm1], y = M[V2C_MF_Y][mm1];
     if (!(((x >= 0 && y >= 0 && x <= p->xsize && y <= p->ysize) || p->outgrid != 1) &&
           !RT(s, V2C_RT_IM, mm2)))
       continue;
-    if (mm2 >= 100) return V2C_ERR_UNSUPPORTED;
     double vx0, vy0, sp0, ee0, vx1, vy1, sp1, ee1, vx2, vy2, sp2, ee2, vx3, vy3, sp3, ee3, vx4, vy4, sp4, ee4;
     if (p->markmod == 1) {
       allinteri(s, x, y, &vx0, &vy0, &sp0, &ee0);
@@ -1453,6 +1469,37 @@ int v2c_oracle_move(v2c_oracle_state *s) {
     }
     x += (dt * vx0);
     y += (dt * vy0);
+    if (mm2 >= 100) {
+      /* immobile marker (:88-135) */
+      if (x >= 0 && y >= 0 && x <= p->xsize && y <= p->ysize) {
+        if (marknum1 >= cap) return V2C_ERR_CAPACITY;  /* "Space out in markx[]" */
+        const long k = marknum1++;
+        s->t[k] = (signed char)(mm2 - 100);
+        M[V2C_MF_X][k] = x;
+        M[V2C_MF_Y][k] = y;
+        M[V2C_MF_K][k] = 0;
+        M[V2C_MF_D][k] = -1.0;
+        M[V2C_MF_V][k] = 0;
+        M[V2C_MF_E][k] = 0;
+        M[V2C_MF_XX][k] = 0;
+        M[V2C_MF_XY][k] = 0;
+        M[V2C_MF_P][k] = 0;
+        M[V2C_MF_EXX][k] = 0;
+        M[V2C_MF_EXY][k] = 0;
+        x = M[V2C_MF_K][mm1];
+        y = M[V2C_MF_V][mm1];
+      }
+      double dx = x - M[V2C_MF_K][mm1];
+      double dy = y - M[V2C_MF_V][mm1];
+      dy = pow(dx * dx + dy * dy, 0.5);
+      if (dy > p->ystpy) {
+        x = M[V2C_MF_K][mm1];
+        y = M[V2C_MF_V][mm1];
+      }
+      M[V2C_MF_X][mm1] = x;
+      M[V2C_MF_Y][mm1] = y;
+      continue;
+    }
     M[V2C_MF_X][mm1] = x;
     M[V2C_MF_Y][mm1] = y;
     sp0 *= dt;
@@ -1477,6 +1524,25 @@ int v2c_oracle_move(v2c_oracle_state *s) {
       M[V2C_MF_E][mm1] = 0;
     }
   }
+  /* out-of-model mobile markers take the appended ones, last first */
+  for (long mm1 = 0; marknum1 > s->n && mm1 < s->n; mm1++) {
+    const double x = M[V2C_MF_X][mm1], y = M[V2C_MF_Y][mm1];
+    if ((x < 0 || y < 0 || x > p->xsize || y > p->ysize) && s->t[mm1] < 100) {
+      marknum1--;
+      s->t[mm1] = s->t[marknum1];
+      M[V2C_MF_K][mm1] = 0;
+      M[V2C_MF_D][mm1] = -1.0;
+      M[V2C_MF_E][mm1] = 0;
+      M[V2C_MF_XX][mm1] = 0;
+      M[V2C_MF_XY][mm1] = 0;
+      M[V2C_MF_P][mm1] = 0;
+      M[V2C_MF_EXX][mm1] = 0;
+      M[V2C_MF_EXY][mm1] = 0;
+      M[V2C_MF_X][mm1] = M[V2C_MF_X][marknum1];
+      M[V2C_MF_Y][mm1] = M[V2C_MF_Y][marknum1];
+    }
+  }
+  s->n = marknum1;
   return 0;
 }
 

@@ -38,6 +38,8 @@ typedef struct v2c_oracle_state {
                                    zero marker one past the end, as the
                                    reference's loop bound m3<=marknum does
                                    (interpolation.c:937)                   */
+  long cap;                     /* marker arrays' capacity (>= n; 0: n):
+                                   immobile markers append new markers     */
 } v2c_oracle_state;
 
 long v2c_oracle_nxsearch(const double *g, long n, double x);

@@ -10,7 +10,7 @@ import oracle
 from velo2cycles_gb300 import abi, mic, synth
 from velo2cycles_gb300._lib import V2CError
 
-from .parity import M2N_OUT, N2M_OUT, VISCOUS, node_errors, marker_errors, nxsearch_np
+from .parity import M2N_OUT, N2M_OUT, node_errors, marker_errors, nxsearch_np, oracle_for, over
 
 pytestmark = pytest.mark.gpu
 
@@ -26,8 +26,7 @@ def _subset(c, keep):
 
 def _check(m, ref, fields):
     errs = node_errors(m.download_nodes(fields), ref.nodes, fields)
-    ids = {v: k for k, v in abi.node_field_names().items()}
-    bad = {k: v for k, v in errs.items() if not v <= (1e-5 if ids.get(k) in VISCOUS else 1e-6)}
+    bad = over(errs, 1e-6)
     assert not bad, bad
 
 
@@ -37,7 +36,7 @@ def test_no_markers(built_lib, oracle_built):
     both sides (plastic.c:2-56 checks nu <= 0 at every interior node)."""
     c = _subset(synth.make_case("tiny", seed=1), np.zeros(0, dtype=np.int64))
     m = mic.from_case(c, max_markers=16)
-    ref = oracle.Restatement(c.copy())
+    ref = oracle_for(c)
     dt = c.params["timestep"]
     m.marker2nodes(); ref.marker2nodes()
     _check(m, ref, M2N_OUT)
@@ -62,7 +61,7 @@ def test_empty_cells_and_crowded_cell(built_lib, oracle_built):
     x[:400] = 0.5 * (c.gx[20] + c.gx[21]) + np.linspace(-1, 1, 400)
     y[:400] = 0.5 * (c.gy[8] + c.gy[9])
     m = mic.from_case(c)
-    ref = oracle.Restatement(c.copy())
+    ref = oracle_for(c)
     m.marker2nodes(); ref.marker2nodes()
     _check(m, ref, M2N_OUT)
     m.nodes2markers(); ref.nodes2markers()
@@ -75,7 +74,7 @@ def test_all_markers_outside(built_lib, oracle_built):
     c = synth.make_case("tiny", seed=3)
     c.marks[abi.MF_X][:] = -10.0
     m = mic.from_case(c)
-    ref = oracle.Restatement(c.copy())
+    ref = oracle_for(c)
     m.marker2nodes(); ref.marker2nodes()
     _check(m, ref, M2N_OUT)
     m.close()
@@ -104,7 +103,7 @@ def test_multi_step_drift(built_lib, oracle_built):
     within ten times the one-step tolerance of the FP64 oracle."""
     c = synth.make_case("small", seed=5)
     m = mic.from_case(c)
-    ref = oracle.Restatement(c.copy())
+    ref = oracle_for(c)
     dts = 10.0 ** np.random.default_rng(0).uniform(6, 9, 6)
     for dt in dts:
         m.set_params(timestep=float(dt))

@@ -61,8 +61,9 @@ def test_forms_reach_the_oracle_root(ctx, precision):
     assert out[abi.RO_RES].max() <= 1e-10
     V = out[abi.RO_V]
     live = V > 1e-40
+    # the converged residual recomputed in FP64 at the returned slip rate
     res = B.rsf_residual(S[:, live], V[live])
-    assert res.max() <= 1.5e-10, res.max()
+    assert res.max() <= 1e-10, res.max()
     rel = np.abs(V / ref[abi.RO_V] - 1)
     assert np.quantile(rel, 0.999) < 1e-8, np.quantile(rel, 0.999)
     tau_rel = np.abs(out[abi.RO_TAU] / ref[abi.RO_TAU] - 1)

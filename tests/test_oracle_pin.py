@@ -19,7 +19,7 @@ import oracle
 from oracle import bindings as B
 from velo2cycles_gb300 import abi, synth
 
-from .parity import stokes_case, temperature_case
+from .parity import immobile_case, stokes_case, temperature_case
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ref_micro.npz")
 
@@ -142,6 +142,73 @@ def test_picard_node_sequence_bit_exact_vs_reference(name, seed):
     inner = (m // yn >= 1) & (m % yn >= 1) & (m // yn < c.gx.size - 1) & (m % yn < yn - 1)
     assert np.array_equal(r.nodes[abi.NF_RK_SLIPRS_FINAL][inner],
                           r.nodes[abi.NF_RK_SLIPRS_SOLVED][inner], equal_nan=True)
+
+
+def picard_case(name, seed, rkmod, **kw):
+    """A case whose solved slip and state rates differ from the final ones,
+    so that every pass's choice between them shows in the results."""
+    c = synth.make_case(name, seed, rkmod=rkmod, **kw)
+    rng = np.random.default_rng(seed)
+    for f in (abi.NF_RK_SLIPRS_SOLVED, abi.NF_RK_PHIDTS_SOLVED):
+        base = c.nodes[abi.NF_RK_SLIPRS_FINAL if f == abi.NF_RK_SLIPRS_SOLVED
+                       else abi.NF_RK_PHIDTS_FINAL]
+        c.nodes[f] = base * rng.uniform(0.3, 3.0, base.size)
+    return c
+
+
+@needs_ref
+@pytest.mark.parametrize("rkmod", [0, 1, 2, 3])
+@pytest.mark.parametrize("variant", [{}, dict(RSFmode=0), dict(timesum=0.0)],
+                         ids=["rsf", "RSFmode=0", "timesum=0"])
+def test_picard_passes_bit_exact_vs_reference(rkmod, variant):
+    """Four passes rk = 0..3 of compute_before_solve + compute_after_solve
+    under each rkmod (calc_RSF.c:46-86: rk 0 takes the final slip rate,
+    later passes the solved one, except rk 3 under rkmod 1 and 2, which
+    takes none), each pass feeding the next its solved rates."""
+    c = picard_case("small", 31, rkmod, **variant)
+    stages = (1 << B.STAGE_M2N) | (1 << B.STAGE_BEFORE) | (1 << B.STAGE_AFTER)
+    ref = B.run_reference(c, stages=stages | B.picard_passes(4), nthreads=1)
+    r = oracle.Restatement(c.copy(), phantom=True)
+    dt = c.params["timestep"]
+    r.marker2nodes()
+    for rk in range(4):
+        r.compute_before_solve(dt, rk)
+        d = r.compute_after_solve(dt, rk)
+    assert not _compare(r, ref["nodes"], ref["marks"])
+    assert d == ref["deltas"]
+
+
+@needs_ref
+@pytest.mark.parametrize("n_imm,n_out", [(40, 25), (10, 30), (30, 0)])
+def test_immobile_markers_bit_exact_vs_reference(n_imm, n_out):
+    """moveandrotatemarkers with immobile markers: spawned markers appended in
+    index order, anchors kept, out-of-model markers refilled from the last
+    appended one back, the new marker count.  Against the reference built
+    for one thread (v2c_ref_serial; see the next test for the OpenMP build)."""
+    c = immobile_case(5, n_imm=n_imm, n_out=n_out)
+    ref = B.run_reference(c, stages=1 << B.STAGE_MOVE, nthreads=1, serial=True)
+    r = oracle.Restatement(c.copy(), cap=2 * c.n)
+    assert r.move() == 0
+    assert r.n == ref["n"] == c.n + max(0, n_imm - n_out)
+    assert np.array_equal(r.markt, ref["markt"])
+    assert not _compare(r, ref["nodes"], ref["marks"])
+
+
+@needs_ref
+def test_openmp_build_appends_from_zero():
+    """The reference's OpenMP build appends the spawned markers through the
+    reduction variable marknum1 (moveandrotatemarkers.c:5), whose private
+    copy starts from 0: the spawned markers overwrite markers 0, 1, ...
+    rather than landing after the last one.  The restatement (and the GPU)
+    follow the routine as written for one thread."""
+    c = immobile_case(5, n_imm=12, n_out=0)
+    ref = B.run_reference(c, stages=1 << B.STAGE_MOVE, nthreads=1)
+    imm = np.flatnonzero(c.markt >= 100)
+    assert ref["n"] == c.n + imm.size
+    # the first markers now hold the spawned types, the appended slots
+    # nothing the move wrote
+    assert np.array_equal(ref["markt"][:imm.size], c.markt[imm] - 100)
+    assert np.all(ref["marks"][abi.MF_X][c.n:] == 0)
 
 
 @needs_ref

@@ -145,9 +145,8 @@ def test_reference_restart_drives_gpu_step(tmp_path, built_lib, oracle_built):
     """The state the reference saved after its step, loaded from the file,
     runs the GPU marker2nodes + nodes2markers pass like the oracle does on
     the same state (tolerances of the MIC parity tests)."""
-    import oracle
     from velo2cycles_gb300 import mic
-    from .parity import M2N_OUT, VISCOUS, node_errors
+    from .parity import M2N_OUT, node_errors, oracle_for, over
 
     z = np.load(GOLDEN)
     got = prn.read(_write_bytes(tmp_path, "ref.prn", z["default/prn"].tobytes()))
@@ -162,10 +161,8 @@ def test_reference_restart_drives_gpu_step(tmp_path, built_lib, oracle_built):
     m = mic.from_case(case)
     m.marker2nodes()
     out = m.download_nodes(M2N_OUT)
-    ref = oracle.Restatement(case.copy())
+    ref = oracle_for(case)
     ref.marker2nodes()
-    errs = node_errors(out, ref.nodes, M2N_OUT)
-    names = {v: k for k, v in abi.node_field_names().items()}
-    bad = {k: v for k, v in errs.items() if not v <= (1e-5 if names.get(k) in VISCOUS else 1e-6)}
+    bad = over(node_errors(out, ref.nodes, M2N_OUT))
     assert not bad, bad
     m.close()

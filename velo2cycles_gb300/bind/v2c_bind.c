@@ -146,10 +146,17 @@ static void v2c_bind_nodes_down(const int *fields, int nf) {
 
 void v2c_bind_markers_to_host(void) {
   if (!v2c_bind_ctx || !v2c_bind_have_markers) return;
+  if (v2c_bind_slipv_n < marknum) {  /* markers appended by immobile ones */
+    double *p = (double *)realloc(v2c_bind_slipv, sizeof(double) * marknum);
+    if (!p) { printf("v2c_bind: out of host memory\n"); errcheck = 1; return; }
+    memset(p + v2c_bind_slipv_n, 0, sizeof(double) * (marknum - v2c_bind_slipv_n));
+    v2c_bind_slipv = p;
+    v2c_bind_slipv_n = marknum;
+  }
   /* the fields the GPU keeps; markd/markw only where a marker was reset */
   double *f[V2C_MF_N];
   memset(f, 0, sizeof(f));
-  static const int keep[] = {V2C_MF_X, V2C_MF_Y, V2C_MF_K, V2C_MF_D, V2C_MF_E, V2C_MF_P,
+  static const int keep[] = {V2C_MF_X, V2C_MF_Y, V2C_MF_K, V2C_MF_V, V2C_MF_D, V2C_MF_E, V2C_MF_P,
                              V2C_MF_W, V2C_MF_EXX, V2C_MF_EXY, V2C_MF_XX, V2C_MF_XY,
                              V2C_MF_VX, V2C_MF_VY, V2C_MF_C, V2C_MF_PHI};
   for (int k = 0; k < V2C_BIND_LEN(keep); k++) f[keep[k]] = v2c_bind_marker_array(keep[k]);
@@ -249,6 +256,16 @@ double v2c_bind_nodes2markers(void) {
 void v2c_bind_moveandrotatemarkers(void) {
   if (!v2c_bind_setup() || !v2c_bind_nodes_up()) return;
   if (!v2c_bind_ok(v2c_moveandrotatemarkers(v2c_bind_ctx), "v2c_moveandrotatemarkers")) return;
+  /* immobile markers append markers: the new count, as the reference sets
+   * marknum at the end of its routine (moveandrotatemarkers.c:176) */
+  v2c_status st;
+  if (v2c_bind_ok(v2c_get_status(v2c_bind_ctx, &st), "v2c_get_status")) {
+    if (st.n_markers > MAXMRK) {
+      printf("Space out in markx[]");
+      exit(0);
+    }
+    marknum = st.n_markers;
+  }
   if (v2c_bind_sync_markers) v2c_bind_markers_to_host();
 }
 

@@ -2,6 +2,7 @@
 // and the step entry points that replace the reference's global-array
 // routines.
 #include <math.h>
+#include <cmath>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -72,6 +73,15 @@ struct v2c_ctx {
   // uploads; valid per component while it matches the FP32 field
   double *d_vel64 = nullptr;
   bool vel64_ok[2] = {false, false};
+  // FP64 copies of the uploaded node temperatures TK and TK2 (the marker
+  // temperature update reads them); TK's is stale once marker2nodes writes TK
+  double *d_tk64 = nullptr;
+  bool tk64_ok[2] = {false, false};
+  // immobile markers (type >= 100): their count, and the compaction
+  // scratch, allocated the first time markers with such a type arrive
+  long n_immobile = 0;
+  ImmBufs imm{};
+  void *imm_mem = nullptr;
   int bc_n = 0;
   void *bc_mem = nullptr;
   BcRows bc{};
@@ -201,6 +211,14 @@ Scal make_scal(const v2c_params &p, const std::vector<double> &rt) {
   split(p.timestep, s.dt_hi, s.dt_lo);
   split(p.faultwidth, s.W_hi, s.W_lo);
   split(p.nstress, s.sn_hi, s.sn_lo);
+  if (p.timestep > 0) {
+    split(log(p.timestep), s.lndt_hi, s.lndt_lo);
+  } else {
+    s.lndt_hi = -INFINITY;
+    s.lndt_lo = 0.f;
+  }
+  s.eps2_lo = (float)(p.eps2 - (double)s.eps2_f);
+  s.tdeep_lo = (float)(p.tdeep - (double)s.tdeep_f);
   s.sppe_nstress = (p.timesum == 0 && p.reloadfromDP == 0 && p.compressiblemode == 1);
   s.timesum_pos = p.timesum > 0;
   s.timesum_zero = p.timesum == 0;
@@ -217,7 +235,7 @@ int fail(v2c_ctx *ctx, int code) {
 int check_params(const v2c_params *p) {
   if (p->xnumx < 4 || p->ynumy < 4) return V2C_ERR_ARG;
   if (p->interpolationmod != 1 && p->interpolationmod != 2) return V2C_ERR_UNSUPPORTED;
-  if (p->rkmod == 3) return V2C_ERR_UNSUPPORTED;
+  if (p->rkmod < 0 || p->rkmod > 3) return V2C_ERR_UNSUPPORTED;
   if (p->newton_guess < V2C_GUESS_PLAIN || p->newton_guess > V2C_GUESS_OFF) return V2C_ERR_ARG;
   if (p->newton_precision != V2C_NEWTON_SPLIT && p->newton_precision != V2C_NEWTON_FP64)
     return V2C_ERR_ARG;
@@ -290,7 +308,7 @@ extern "C" int v2c_create(const v2c_params *p, long max_markers, void *cuda_stre
   mm[k++] = (void *)m.field; ctx->n_marker_mem = k;
   AM(cell_in, int32_t) AM(cell_out, int32_t) AM(u_in, float) AM(u_out, float)
   AM(v_in, float) AM(v_out, float) AM(id, int32_t) AM(type, int8_t) AM(flags, uint8_t)
-  AM(tk, float) AM(e, float) AM(p, float) AM(sxx, float) AM(sxy, float) AM(exx, float)
+  AM(tk, float) AM(tk_lo, float) AM(mv, float) AM(mv_lo, float) AM(e, float) AM(p, float) AM(sxx, float) AM(sxy, float) AM(exx, float)
   AM(exy, float) AM(vx, float) AM(vy, float) AM(phi, float) AM(coh, float) AM(slipv, float)
   AM(mnu, float) AM(mkt, float) AM(mro, float)
 #undef AM
@@ -319,6 +337,8 @@ extern "C" int v2c_destroy(v2c_ctx *ctx) {
   for (double *v : ctx->d_cyc_v64)
     if (v) cudaFree(v);
   if (ctx->d_vel64) cudaFree(ctx->d_vel64);
+  if (ctx->d_tk64) cudaFree(ctx->d_tk64);
+  if (ctx->imm_mem) cudaFree(ctx->imm_mem);
   if (ctx->d_bs) cudaFree(ctx->d_bs);
   if (ctx->d_slip) cudaFree(ctx->d_slip);
   if (ctx->d_mslip) cudaFree(ctx->d_mslip);
@@ -388,7 +408,7 @@ extern "C" int v2c_set_rock_table(v2c_ctx *ctx, const double *rt) {
     double nu = R(V2C_RT_NU, t), dh = R(V2C_RT_DH, t), dv = R(V2C_RT_DV, t);
     double ss = R(V2C_RT_SS, t), mm = R(V2C_RT_MM, t), gg = R(V2C_RT_GG, t);
     F(RK_GG, t) = (float)gg;
-    F(RK_INV_GG, t) = gg != 0 ? (float)(1.0 / gg) : 0.f;
+    F(RK_INV_GG, t) = (float)(1.0 / gg);  // inf for G = 0, as nu/G is in the reference
     F(RK_NU, t) = (float)nu;
     F(RK_LNNU, t) = nu > 0 ? (float)log(nu) : 0.f;
     F(RK_DH, t) = (float)dh; F(RK_DV, t) = (float)dv;
@@ -400,6 +420,21 @@ extern "C" int v2c_set_rock_table(v2c_ctx *ctx, const double *rt) {
     F(RK_KF, t) = (float)R(V2C_RT_KF, t); F(RK_KP, t) = (float)R(V2C_RT_KP, t);
     F(RK_N0, t) = (float)R(V2C_RT_N0, t); F(RK_N1, t) = (float)R(V2C_RT_N1, t);
     F(RK_IM, t) = (float)R(V2C_RT_IM, t);
+    // float pairs of the Arrhenius exponent's constants
+    auto pair = [&](int khi, int klo, double d) {
+      F(khi, t) = (float)d;
+      F(klo, t) = std::isfinite(d) ? (float)(d - (double)(float)d) : 0.f;
+    };
+    pair(RK_DH, RK_DH_LO, dh);
+    pair(RK_DV, RK_DV_LO, dv);
+    // diffusion-creep viscosity 0.5 k1 e1, k1 = nu / ss^(mm-1)
+    // (density_ductilevisc_calc.c:116-127), as ln(0.5 k1) + (E+PV)/RT
+    const double lnk = (nu > 0 && ss > 0) ? log(0.5) + log(nu) - (mm - 1.0) * log(ss) : 0.0;
+    pair(RK_LNK, RK_LNK_LO, lnk);
+    pair(RK_LNG, RK_LNG_LO, gg > 0 ? log(gg) : -INFINITY);
+    pair(RK_SS, RK_SS_LO, ss);
+    pair(RK_EM, RK_EM_LO, mm != 0 ? (mm - 1.0) / mm : 0.0);
+    pair(RK_MM1, RK_MM1_LO, mm - 1.0);
     int kind;
     // branch selection of ductilevisc (density_ductilevisc_calc.c:44-66)
     if (t == 1) kind = VISC_STICKY;
@@ -566,14 +601,47 @@ int build_bc(v2c_ctx *ctx) {
 }  // namespace
 
 // ============================================================ marker arrays
+// the compaction scratch of immobile markers, one allocation for the
+// context's capacity (ImmBufs in v2c_kernels.h)
+static int alloc_immobile(v2c_ctx *ctx) {
+  const long cap = ctx->cap > 0 ? ctx->cap : 1;
+  const long nb = scan_blocks(cap) + 1;
+  const size_t words = (size_t)cap * 7 + 2 * (size_t)(cap + 1) + (size_t)nb + 2;
+  void *mem = nullptr;
+  if (cudaMalloc(&mem, sizeof(int32_t) * words) != cudaSuccess) return V2C_ERR_CUDA;
+  int32_t *w = static_cast<int32_t *>(mem);
+  ImmBufs &b = ctx->imm;
+  b.spawn = w; w += cap;
+  b.out = w; w += cap;
+  b.sp_cell = w; w += cap;
+  b.sp_u = reinterpret_cast<float *>(w); w += cap;
+  b.sp_v = reinterpret_cast<float *>(w); w += cap;
+  b.src = w; w += cap;
+  b.inv = w; w += cap;
+  b.spawn_rank = w; w += cap + 1;
+  b.out_rank = w; w += cap + 1;
+  b.blocksum = w; w += nb;
+  b.totals = w;
+  ctx->imm_mem = mem;
+  return V2C_OK;
+}
+
 extern "C" int v2c_upload_markers(v2c_ctx *ctx, const double *const *fields,
                                   const signed char *markt, long n) {
   if (!ctx || !fields || !markt || n < 0) return V2C_ERR_ARG;
   if (!fields[V2C_MF_X] || !fields[V2C_MF_Y]) return fail(ctx, V2C_ERR_ARG);
   if (n > ctx->cap) return fail(ctx, V2C_ERR_CAPACITY);
   if (!ctx->have_grid) return fail(ctx, V2C_ERR_STATE);
-  for (long i = 0; i < n; i++)
-    if (markt[i] < 0 || markt[i] >= 100) return fail(ctx, V2C_ERR_UNSUPPORTED);
+  long n_imm = 0;
+  for (long i = 0; i < n; i++) {
+    if (markt[i] < 0) return fail(ctx, V2C_ERR_UNSUPPORTED);
+    n_imm += markt[i] >= 100;
+  }
+  if (n_imm > 0 && !ctx->imm_mem) {
+    int rc = alloc_immobile(ctx);
+    if (rc) return fail(ctx, rc);
+  }
+  ctx->n_immobile = n_imm;
   cudaStream_t st = ctx->stream;
   Markers &m = ctx->m;
   Grid g = make_grid(ctx);
@@ -583,16 +651,21 @@ extern "C" int v2c_upload_markers(v2c_ctx *ctx, const double *const *fields,
   launch_assign(g, ctx->d_stage64, ctx->d_stage64b, n, m, ctx->d_stat, st);
   CK(cudaMemcpyAsync(m.type, markt, n, cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(m.flags, 0, n, st));
-  struct F { int id; float *dst; } ff[] = {
-      {V2C_MF_K, m.tk}, {V2C_MF_E, m.e}, {V2C_MF_P, m.p}, {V2C_MF_XX, m.sxx},
-      {V2C_MF_XY, m.sxy}, {V2C_MF_EXX, m.exx}, {V2C_MF_EXY, m.exy}, {V2C_MF_VX, m.vx},
-      {V2C_MF_VY, m.vy}, {V2C_MF_PHI, m.phi}, {V2C_MF_C, m.coh}, {V2C_MF_SLIPV, m.slipv}};
+  // the temperature and markv as float pairs, the other fields in FP32
+  struct F { int id; float *dst; float *lo; } ff[] = {
+      {V2C_MF_K, m.tk, m.tk_lo}, {V2C_MF_V, m.mv, m.mv_lo}, {V2C_MF_E, m.e, nullptr},
+      {V2C_MF_P, m.p, nullptr},
+      {V2C_MF_XX, m.sxx, nullptr}, {V2C_MF_XY, m.sxy, nullptr}, {V2C_MF_EXX, m.exx, nullptr},
+      {V2C_MF_EXY, m.exy, nullptr}, {V2C_MF_VX, m.vx, nullptr}, {V2C_MF_VY, m.vy, nullptr},
+      {V2C_MF_PHI, m.phi, nullptr}, {V2C_MF_C, m.coh, nullptr}, {V2C_MF_SLIPV, m.slipv, nullptr}};
   for (auto &f : ff) {
     if (fields[f.id]) {
       CK(cudaMemcpyAsync(ctx->d_stage64, fields[f.id], sizeof(double) * n, cudaMemcpyHostToDevice, st));
-      launch_f64_to_f32(ctx->d_stage64, f.dst, n, st);
+      if (f.lo) launch_f64_to_pair(ctx->d_stage64, f.dst, f.lo, n, st);
+      else launch_f64_to_f32(ctx->d_stage64, f.dst, n, st);
     } else {
       CK(cudaMemsetAsync(f.dst, 0, sizeof(float) * n, st));
+      if (f.lo) CK(cudaMemsetAsync(f.lo, 0, sizeof(float) * n, st));
     }
   }
   CK(cudaMemsetAsync(m.mnu, 0, sizeof(float) * n, st));
@@ -603,8 +676,8 @@ extern "C" int v2c_upload_markers(v2c_ctx *ctx, const double *const *fields,
   const int32_t *perm = ctx->sb.perm;
   float *tmpf = (float *)ctx->d_stage64;
   int32_t *tmpi = (int32_t *)ctx->d_stage64;
-  float *fl[] = {m.u_in, m.v_in, m.tk, m.e, m.p, m.sxx, m.sxy, m.exx, m.exy, m.vx,
-                 m.vy, m.phi, m.coh, m.slipv};
+  float *fl[] = {m.u_in, m.v_in, m.tk, m.tk_lo, m.mv, m.mv_lo, m.e, m.p, m.sxx, m.sxy, m.exx,
+                 m.exy, m.vx, m.vy, m.phi, m.coh, m.slipv};
   for (float *f : fl) {
     launch_gather_f32(f, perm, tmpf, n, st);
     CK(cudaMemcpyAsync(f, tmpf, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
@@ -640,13 +713,16 @@ extern "C" int v2c_download_markers(v2c_ctx *ctx, double *const *fields, signed 
       CK(cudaMemcpyAsync(fields[V2C_MF_Y], ctx->d_stage64b, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
   }
-  struct F { int id; const float *src; } ff[] = {
-      {V2C_MF_K, m.tk}, {V2C_MF_E, m.e}, {V2C_MF_P, m.p}, {V2C_MF_XX, m.sxx},
-      {V2C_MF_XY, m.sxy}, {V2C_MF_EXX, m.exx}, {V2C_MF_EXY, m.exy}, {V2C_MF_VX, m.vx},
-      {V2C_MF_VY, m.vy}, {V2C_MF_PHI, m.phi}, {V2C_MF_C, m.coh}, {V2C_MF_SLIPV, m.slipv}};
+  struct F { int id; const float *src; const float *lo; } ff[] = {
+      {V2C_MF_K, m.tk, m.tk_lo}, {V2C_MF_V, m.mv, m.mv_lo}, {V2C_MF_E, m.e, nullptr},
+      {V2C_MF_P, m.p, nullptr},
+      {V2C_MF_XX, m.sxx, nullptr}, {V2C_MF_XY, m.sxy, nullptr}, {V2C_MF_EXX, m.exx, nullptr},
+      {V2C_MF_EXY, m.exy, nullptr}, {V2C_MF_VX, m.vx, nullptr}, {V2C_MF_VY, m.vy, nullptr},
+      {V2C_MF_PHI, m.phi, nullptr}, {V2C_MF_C, m.coh, nullptr}, {V2C_MF_SLIPV, m.slipv, nullptr}};
   for (auto &f : ff) {
     if (!fields[f.id]) continue;
-    launch_unpermute_f32(f.src, m.id, ctx->d_stage64, n, st);
+    if (f.lo) launch_unpermute_pair(f.src, f.lo, m.id, ctx->d_stage64, n, st);
+    else launch_unpermute_f32(f.src, m.id, ctx->d_stage64, n, st);
     CK(cudaMemcpyAsync(fields[f.id], ctx->d_stage64, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
   }
@@ -659,11 +735,10 @@ extern "C" int v2c_download_markers(v2c_ctx *ctx, double *const *fields, signed 
     launch_unpermute_u8(m.flags, m.id, (uint8_t *)ctx->d_stage64b, n, st);
     CK(cudaMemcpyAsync(fl.data(), ctx->d_stage64b, n, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    for (long i = 0; i < n; i++)
-      if (fl[i] & MFLAG_RESET) {
-        if (fields[V2C_MF_D]) fields[V2C_MF_D][i] = -1.0;
-        if (fields[V2C_MF_W]) fields[V2C_MF_W][i] = -1.0;
-      }
+    for (long i = 0; i < n; i++) {
+      if ((fl[i] & (MFLAG_RESET | MFLAG_DNEG)) && fields[V2C_MF_D]) fields[V2C_MF_D][i] = -1.0;
+      if ((fl[i] & MFLAG_RESET) && fields[V2C_MF_W]) fields[V2C_MF_W][i] = -1.0;
+    }
   }
   CK(cudaStreamSynchronize(st));
   return V2C_OK;
@@ -680,8 +755,17 @@ extern "C" int v2c_download_cells(v2c_ctx *ctx, int32_t *cell, long n) {
 // ============================================================== node arrays
 // node fields live in FP32 on the device; they are converted on the way in
 // and out (the conversion kernels run on the context stream)
-// keep the FP64 copy of an uploaded velocity field (staged at dev64)
-static int keep_vel64(v2c_ctx *ctx, int field, const double *dev64) {
+// keep the FP64 copy of an uploaded velocity or temperature field (staged
+// at dev64)
+static int keep_node64(v2c_ctx *ctx, int field, const double *dev64) {
+  if (field == V2C_NF_TK || field == V2C_NF_TK2) {
+    const int k = field == V2C_NF_TK ? 0 : 1;
+    if (!ctx->d_tk64) CK(cudaMalloc(&ctx->d_tk64, sizeof(double) * 2 * ctx->nn));
+    CK(cudaMemcpyAsync(ctx->d_tk64 + k * ctx->nn, dev64, sizeof(double) * ctx->nn,
+                       cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->tk64_ok[k] = true;
+    return V2C_OK;
+  }
   if (field != V2C_NF_VX && field != V2C_NF_VY) return V2C_OK;
   const int k = field == V2C_NF_VX ? 0 : 1;
   if (!ctx->d_vel64) CK(cudaMalloc(&ctx->d_vel64, sizeof(double) * 2 * ctx->nn));
@@ -696,7 +780,7 @@ extern "C" int v2c_upload_node_field(v2c_ctx *ctx, int field, const double *src)
   ctx->dsxx_valid = false;
   CK(cudaMemcpyAsync(ctx->d_node64, src, sizeof(double) * ctx->nn, cudaMemcpyHostToDevice,
                      ctx->stream));
-  if (int rc = keep_vel64(ctx, field, ctx->d_node64)) return fail(ctx, rc);
+  if (int rc = keep_node64(ctx, field, ctx->d_node64)) return fail(ctx, rc);
   launch_node_to_f32(ctx->d_node64, ctx->d_node + (long)field * ctx->nn, ctx->nn, ctx->stream);
   ctx->launches += 1;
   CK(cudaGetLastError());
@@ -745,7 +829,7 @@ extern "C" int v2c_upload_node_fields(v2c_ctx *ctx, int count, const int *fields
   launch_fields_to_f32(ctx->d_nstage, ctx->nn, fields, count, ctx->d_node, ctx->stream);
   ctx->launches += 1;
   for (int k = 0; k < count; k++)
-    if (int rc2 = keep_vel64(ctx, fields[k], ctx->d_nstage + (long)k * ctx->nn)) return fail(ctx, rc2);
+    if (int rc2 = keep_node64(ctx, fields[k], ctx->d_nstage + (long)k * ctx->nn)) return fail(ctx, rc2);
   CK(cudaGetLastError());
   return V2C_OK;
 }
@@ -812,6 +896,7 @@ extern "C" int v2c_marker2nodes(v2c_ctx *ctx) {
   a.n = ctx->n;
   CK(cudaMemsetAsync(ctx->d_sticky, 0, sizeof(uint32_t) * ctx->nn, st));
   ctx->dsxx_valid = false;  // the scatter writes sxxe
+  ctx->tk64_ok[0] = false;  // and the node temperature
   {
     PhysArgs ph;
     ph.g = a.g; ph.N = a.N; ph.m = a.m; ph.R = a.R; ph.S = a.S; ph.n = ctx->n;
@@ -990,12 +1075,28 @@ static int n2m_move(v2c_ctx *ctx, int do_n2m, int do_move) {
     ctx->launches += a.bs ? 3 : 1;
   }
   if (do_move) {
+    const bool imm = ctx->n_immobile > 0 && ctx->n > 0;
+    if (imm) {
+      CK(cudaMemsetAsync(ctx->imm.spawn, 0, sizeof(int32_t) * ctx->n, st));
+      CK(cudaMemsetAsync(ctx->imm.out, 0, sizeof(int32_t) * ctx->n, st));
+      a.imm = ctx->imm;
+      a.has_imm = 1;
+    }
     {
       Prof pr(ctx, V2C_PROF_MOVE);
       launch_move(a, st);
       ctx->launches += ctx->n > 0 ? 2 : 1;
     }
     CK(cudaGetLastError());
+    if (imm) {
+      // spawned markers appended, out-of-model slots refilled (one stream
+      // synchronisation for the new marker count)
+      long added = 0;
+      rc = launch_immobile_compact(ctx->m, ctx->n, ctx->cap, ctx->imm, &added, st);
+      if (rc) return fail(ctx, rc);
+      ctx->n += added;
+      ctx->launches += 8;
+    }
     swap_positions(ctx);
     // next step's order: counting sort of the new cells
     Prof pr(ctx, V2C_PROF_SORT);
@@ -1056,6 +1157,11 @@ extern "C" int v2c_marker_temperature(v2c_ctx *ctx, double heatdif) {
   a.heatdif = (float)heatdif;
   a.dt = (float)ctx->p.timestep;
   a.tdeep = (float)ctx->p.tdeep;
+  a.tdeep64 = ctx->p.tdeep;
+  if (ctx->d_tk64 && ctx->tk64_ok[0] && ctx->tk64_ok[1]) {
+    a.tk64 = ctx->d_tk64;
+    a.tk2_64 = ctx->d_tk64 + ctx->nn;
+  }
   // the sort's slot buffers hold nothing between sorts (one entry per marker)
   a.dtk1 = reinterpret_cast<float *>(ctx->sb.tmp);
   a.wt = reinterpret_cast<float *>(ctx->sb.slot);
@@ -1258,7 +1364,9 @@ extern "C" int v2c_cycle_step(v2c_ctx *ctx, int regime, double dt, int use_graph
   if (!ctx->d_cyc_v[regime] || !ctx->d_slip) return fail(ctx, V2C_ERR_STATE);
   ctx->p.timestep = dt;
   cudaStream_t st = ctx->stream;
-  if (!use_graph) {
+  // immobile markers change the marker count inside the step (a host
+  // synchronisation), which a captured graph cannot hold: run eagerly
+  if (!use_graph || ctx->n_immobile > 0) {
     rc = cycle_enqueue(ctx, regime, dt);
     if (rc) return rc;
     ctx->p.timesum += dt;

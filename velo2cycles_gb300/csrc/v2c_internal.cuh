@@ -27,10 +27,20 @@ namespace v2c {
 
 // ------------------------------------------------------------ rock table
 // FP32 copies and derived constants of the per-type coefficients.
+// The _LO entries are the low words of float pairs (hi + lo, ~48 bits) for
+// the constants of the Arrhenius exponent, whose rounding to FP32 alone would
+// change the viscosity by several parts in 1e6 (see ductile_visc32).
 enum {
   RK_GG = 0, RK_INV_GG, RK_NU, RK_LNNU, RK_DH, RK_DV, RK_LNSS, RK_MM,
   RK_RO, RK_BB, RK_AA, RK_CP, RK_KT, RK_HT, RK_KF, RK_KP, RK_LN_N0, RK_LN_N1,
-  RK_N0, RK_N1, RK_KIND, RK_IM, RK_N
+  RK_N0, RK_N1, RK_KIND, RK_IM,
+  RK_DH_LO, RK_DV_LO,      // activation energy and volume, low words
+  RK_LNK, RK_LNK_LO,       // ln(0.5 nu / ss^(mm-1)), the diffusion-creep prefactor
+  RK_LNG, RK_LNG_LO,       // ln G
+  RK_SS, RK_SS_LO,         // ss
+  RK_EM, RK_EM_LO,         // (mm-1)/mm
+  RK_MM1, RK_MM1_LO,       // mm-1
+  RK_N
 };
 enum { VISC_NEWTON = 0, VISC_POWER = 1, VISC_STICKY = 2, VISC_UNDEF = 3 };
 
@@ -48,10 +58,19 @@ struct Markers {
   int32_t *id;
   int8_t *type;
   uint8_t *flags;  // bit0: out-of-grid reset (markd = markw = -1)
+  // tk + tk_lo is the temperature as a float pair: the power-law viscosity
+  // depends on exp(E/RT) with E/RT up to ~50, so a temperature rounded to
+  // FP32 (6e-8) alone would move it by ~3e-6
   float *tk, *e, *p, *sxx, *sxy, *exx, *exy, *vx, *vy, *phi, *coh, *slipv;
+  float *tk_lo;
+  // markv as a float pair: the y anchor of an immobile marker (type >= 100,
+  // whose markk holds the x anchor), moveandrotatemarkers.c:127-133
+  float *mv, *mv_lo;
   float *mnu, *mkt, *mro;  // per-step results of the marker physics kernel
 };
-enum { MFLAG_RESET = 1 };
+// RESET: out-of-grid reset, markd = markw = -1; DNEG: markd = -1 only (a
+// marker appended or refilled by the immobile-marker rule)
+enum { MFLAG_RESET = 1, MFLAG_DNEG = 2 };
 
 // ------------------------------------------------------------------ grid
 struct Grid {
@@ -87,6 +106,8 @@ struct Scal {
   float zdeep_lo_f;   // (float)zdeep - 1 - 1e-6 |zdeep|: coarse depth test
   float eps2_f, nstress_f, nubeg_f, nuend_f, faultwidth_f;
   float dt_hi, dt_lo, W_hi, W_lo, sn_hi, sn_lo;  // float-float timestep, faultwidth, nstress
+  float lndt_hi, lndt_lo;  // ln timestep as a float pair (-inf when timestep <= 0)
+  float eps2_lo, tdeep_lo; // low words of the temperatures markers are reset to
   int sppe_nstress;   // timesum == 0 && reloadfromDP == 0 && compressiblemode == 1
   int timesum_pos;    // timesum > 0
   int timesum_zero;   // timesum == 0

@@ -138,6 +138,28 @@ void launch_before_solve(const Grid &g, const Nodes &N, const Scal &S, double dt
 void launch_after_solve(const Grid &g, const Nodes &N, const Scal &S, double dt, int rk,
                         double *red, cudaStream_t st);
 
+// Immobile markers (moveandrotatemarkers.c:88-171): what the move kernel
+// records per reference marker number, and the scratch of the compaction
+// that appends the spawned markers and refills out-of-model slots.
+struct ImmBufs {
+  int32_t *spawn;          // [cap] 1: the immobile marker spawned (by id)
+  int32_t *out;            // [cap] 1: the mobile marker ends outside the model (by id)
+  int32_t *spawn_rank;     // [cap + 1] exclusive scan of spawn, total last
+  int32_t *out_rank;       // [cap + 1] exclusive scan of out, total last
+  int32_t *sp_cell;        // [cap] spawn position (by id)
+  float *sp_u, *sp_v;
+  int32_t *src;            // [cap] id of the immobile marker of each spawn rank
+  int32_t *inv;            // [cap] array index of each id
+  int32_t *blocksum;       // scan scratch (scan_blocks(cap) entries)
+  int32_t *totals;         // [2] A (spawned), O (out of model)
+};
+// After launch_move: ranks, refills and appends; returns through *added the
+// markers appended after the last one (the caller checks it against the
+// capacity first through `cap`; V2C_ERR_CAPACITY leaves nothing changed).
+// Synchronises the stream once (the new marker count).
+int launch_immobile_compact(const Markers &m, long n, long cap, ImmBufs &b, long *added,
+                            cudaStream_t st);
+
 // nodes2markers + move sweep
 struct N2MArgs {
   Grid g;
@@ -158,6 +180,10 @@ struct N2MArgs {
   // payload (BS_N fields, SoA by sorted position) here and per-node gather
   // kernels sum it; null for interpolationmod 2
   float *bs = nullptr;
+  // the move records spawns and out-of-model markers here when the markers
+  // include immobile ones (has_imm; device pointers, passed by value)
+  ImmBufs imm{};
+  int has_imm = 0;
 };
 enum { BS_U = 0, BS_V, BS_PHIS, BS_SXY, BS_EXY, BS_ES, BS_PR, BS_SXX, BS_EXX, BS_N };
 // float4 coefficient sets per cell: 4 quarters x (VX, VY, ESP)
@@ -176,6 +202,10 @@ struct TempArgs {
   const int32_t *start;
   long n, ncell;
   float heatdif, dt, tdeep;
+  double tdeep64;
+  // FP64 copies of the node temperatures TK (solved) and TK2 (before), as
+  // uploaded; null: the FP32 node fields are used
+  const double *tk64 = nullptr, *tk2_64 = nullptr;
   float *dtk1, *wt;  // per sorted position (scratch)
   float *tol;        // per node (scratch)
 };
@@ -192,6 +222,10 @@ int calc_timestep_device(const Grid &g, const Nodes &N, const Scal &S, const v2c
 void launch_assign(const Grid &g, const double *x, const double *y, long n, Markers m,
                    unsigned long long *stat, cudaStream_t st);
 void launch_f64_to_f32(const double *src, float *dst, long n, cudaStream_t st);
+// FP64 values as float pairs hi + lo, and back (out[id[i]] = hi[i] + lo[i])
+void launch_f64_to_pair(const double *src, float *hi, float *lo, long n, cudaStream_t st);
+void launch_unpermute_pair(const float *hi, const float *lo, const int32_t *id, double *out,
+                           long n, cudaStream_t st);
 void launch_gather_f32(const float *src, const int32_t *perm, float *dst, long n, cudaStream_t st);
 void launch_gather_i32(const int32_t *src, const int32_t *perm, int32_t *dst, long n, cudaStream_t st);
 void launch_gather_i8(const int8_t *src, const int32_t *perm, int8_t *dst, long n, cudaStream_t st);

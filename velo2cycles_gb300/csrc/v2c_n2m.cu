@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
           float phi = a.m.phi[idx], mexx = a.m.exx[idx], mexy = a.m.exy[idx];
           float msxx = a.m.sxx[idx], msxy = a.m.sxy[idx], mp = a.m.p[idx];
           float mvx = a.m.vx[idx], mvy = a.m.vy[idx], me = a.m.e[idx];
-          bool changed = false;
+          bool changed = false, tk_set = false;
           if (a.do_n2m) {
             if (in_strict && t < 50 && tk <= 0.f) {
               if (P.antidiffinter == 1) {
@@ -311,7 +311,10 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
                 msxx = SXXE; msxy = SXYE; mp = SPPE; mexx = EXXE; mexy = EXYE;
                 mvx = MVX; mvy = MVY; phi = PHISE; me = ESE;
               }
-              if (!P.tempmod) tk = a.S.eps2_f;
+              if (!P.tempmod) {
+                tk = a.S.eps2_f;
+                tk_set = true;
+              }
               changed = true;
             }
             if (in_grid && t < 50 && tk > 0.f) {
@@ -332,6 +335,7 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
             a.m.sxx[idx] = msxx; a.m.sxy[idx] = msxy; a.m.p[idx] = mp;
             a.m.vx[idx] = mvx; a.m.vy[idx] = mvy; a.m.e[idx] = me;
             a.m.tk[idx] = tk;
+            if (tk_set) a.m.tk_lo[idx] = a.S.eps2_lo;
           }
         }
         if (!backscatter) continue;
@@ -638,6 +642,33 @@ __global__ void __launch_bounds__(256) k_move(N2MArgs a) {
         if (p.Y > 0.5f * nwy && nv_ <= 0.5f) nv_ = nextafterf(0.5f, 1.f);
         if (p.Y > nwy && nv_ <= 1.f) nv_ = nextafterf(1.f, 2.f);
       }
+      if (t >= 100) {
+        // immobile marker (moveandrotatemarkers.c:88-135): inside the model
+        // it spawns a mobile marker there and goes back to its anchor
+        // (markk, markv), as it does when it strays more than ystpy from it
+        const bool inside = (nix > 0 || nu_ >= 0.f) && (nix < g.ncx - 1 || nu_ <= 1.f) &&
+                            (niy > 0 || nv_ >= 0.f) && (niy < g.ncy - 1 || nv_ <= 1.f);
+        const double ax = (double)a.m.tk[idx] + (double)a.m.tk_lo[idx];
+        const double ay = (double)a.m.mv[idx] + (double)a.m.mv_lo[idx];
+        double x = g.gx[nix] + (double)nu_ * (g.gx[nix + 1] - g.gx[nix]);
+        double y = g.gy[niy] + (double)nv_ * (g.gy[niy + 1] - g.gy[niy]);
+        if (inside && a.has_imm) {
+          const int id = a.m.id[idx];
+          a.imm.spawn[id] = 1;
+          a.imm.sp_cell[id] = nix * ncy + niy;
+          a.imm.sp_u[id] = nu_;
+          a.imm.sp_v[id] = nv_;
+          x = ax;
+          y = ay;
+        }
+        const double dx = x - ax, dy = y - ay;
+        if (x == ax && y == ay || sqrt(dx * dx + dy * dy) > P.ystpy) {
+          nix = nsearch64(g.gx, g.xn, ax);
+          niy = nsearch64(g.gy, g.yn, ay);
+          nu_ = offset32((ax - g.gx[nix]) / (g.gx[nix + 1] - g.gx[nix]));
+          nv_ = offset32((ay - g.gy[niy]) / (g.gy[niy + 1] - g.gy[niy]));
+        }
+      } else {
       // stress rotation, moveandrotatemarkers.c:58-76
       float msxx = a.m.sxx[idx], msxy = a.m.sxy[idx];
       sp0 *= dt;
@@ -657,23 +688,42 @@ __global__ void __launch_bounds__(256) k_move(N2MArgs a) {
       a.m.sxy[idx] = msxy;
       // markers coming from depth, out-of-grid reset (:79-87); the FP64
       // position only when the FP32 one is within 1 m of zdeep
-      float tk = a.m.tk[idx];
-      const float tk0 = tk;
+      // (the temperature pair's high word decides tk < tdeep; the two can
+      // differ only for a temperature within half an FP32 ulp of tdeep, where
+      // resetting or not leaves the same temperature to that half ulp)
+      float tk = a.m.tk[idx], tk_lo = 0.f;
+      bool reset = false;
       if (vy0 < 0.f && tk < a.S.tdeep_f &&
           __ldg(a.gyf + niy) + nv_ * __ldg(g.wy + niy) > a.S.zdeep_lo_f) {
         const double ynew = g.gy[niy] + (double)nv_ * (g.gy[niy + 1] - g.gy[niy]);
-        if (ynew > P.zdeep) tk = a.S.tdeep_f;
+        if (ynew > P.zdeep) {
+          tk = a.S.tdeep_f;
+          tk_lo = a.S.tdeep_lo;
+          reset = true;
+        }
       }
       const bool out = (nix == 0 && nu_ < 0.f) || (nix == g.ncx - 1 && nu_ > 1.f) ||
                        (niy == 0 && nv_ < 0.f) || (niy == g.ncy - 1 && nv_ > 1.f);
       if (out) {
         tk = 0.f;
+        tk_lo = 0.f;
+        reset = true;
         a.m.e[idx] = 0.f;
         a.m.flags[idx] |= MFLAG_RESET;
         atomicAdd(a.stat + ST_OUT_OF_GRID, 1ull);
       }
-      if (tk != tk0) a.m.tk[idx] = tk;
+      if (reset) {
+        a.m.tk[idx] = tk;
+        a.m.tk_lo[idx] = tk_lo;
+      }
+      }
     }
+    // mobile markers outside the model after the move: the slots that
+    // markers spawned by immobile ones refill (moveandrotatemarkers.c:141-171)
+    if (a.has_imm && t < 100 &&
+        !((nix > 0 || nu_ >= 0.f) && (nix < g.ncx - 1 || nu_ <= 1.f) &&
+          (niy > 0 || nv_ >= 0.f) && (niy < g.ncy - 1 || nv_ <= 1.f)))
+      a.imm.out[a.m.id[idx]] = 1;
     a.m.cell_out[idx] = nix * ncy + niy;
     a.m.u_out[idx] = nu_;
     a.m.v_out[idx] = nv_;

@@ -18,6 +18,7 @@
 // range.
 #include <math.h>
 
+#include "v2c_ff.cuh"
 #include "v2c_kernels.h"
 
 namespace v2c {
@@ -36,6 +37,31 @@ __device__ __forceinline__ float asinh_exp(float w) {
 __device__ __forceinline__ float log_sinh(float s) {
   if (s > 10.f) return s - 0.693147180559945f + log1pf(-expf(-2.f * s));
   return logf(sinhf(s));
+}
+
+// Float-float forms of the exponents of the slip-rate law.  Its exponent
+// sums terms of a few hundred that cancel (ln V, (mu + b phi)/a, ln sinh of
+// tau/(a sigma)), and the slip rate is e^exponent: in FP32 the sum's
+// rounding alone (~1e-5) would be the slip rate's relative error.
+
+// ln sinh x for x > 0 as a float pair (the correction terms in FP32: below
+// 2e-9 for x > 10, and log1p of sinh(x)/x - 1 < 0.05 for x < 0.5)
+__device__ __forceinline__ ff ff_log_sinh(ff x) {
+  if (x.hi > 10.f)
+    return ff_add_f(ff_sub(x, ff_ln2()), log1pf(-expf(-2.f * x.hi)));
+  if (x.hi > 0.5f)
+    return ff_log(ff_scale(ff_sub(ff_exp(x), ff_exp(ff_neg(x))), 0.5f));
+  const float x2 = x.hi * x.hi;
+  return ff_add_f(ff_log(x), log1pf(x2 * (1.f / 6.f + x2 * (1.f / 120.f + x2 * (1.f / 5040.f)))));
+}
+
+// e^E for a float pair E (the low word as a first-order factor)
+__device__ __forceinline__ float exp_ff(ff E) { return expf(E.hi) * (1.f + E.lo); }
+
+// asinh(e^w) for a float-pair w (calc_RSF.c:128), to FP32 precision
+__device__ __forceinline__ float asinh_exp_ff(ff w) {
+  if (w.hi > 9.f) return (w.hi + 0.693147180559945f) + (w.lo + 0.25f * __expf(-2.f * w.hi));
+  return asinhf(exp_ff(w));
 }
 
 // ageing-law state after dt at slip rate V (calc_RSF.c:96-103)
@@ -219,7 +245,9 @@ __global__ void k_before(Grid g, Nodes N, Scal S, float dt, int rk, unsigned lon
   long m2 = m3 % g.yn, m1 = m3 / g.yn;
   if (!(m1 >= 1 && m2 >= 1 && m1 < g.xn - 1 && m2 < g.yn - 1)) return;
   const float W = (float)p.faultwidth;
-  const float nP = (p.pmode == 0 || p.timesum == 0) ? (float)p.nstress : N.f(V2C_NF_SPPES)[m3];
+  const bool nP_const = p.pmode == 0 || p.timesum == 0;
+  const ff nP_ff = nP_const ? ff{S.sn_hi, S.sn_lo} : ff_f(N.f(V2C_NF_SPPES)[m3]);
+  const float nP = nP_ff.hi;
   const float sxxs = N.f(V2C_NF_SXXS)[m3], sxy = N.f(V2C_NF_SXY)[m3];
   const float sigin = sqrtf(sxxs * sxxs + sxy * sxy);
   float nu;
@@ -228,7 +256,10 @@ __global__ void k_before(Grid g, Nodes N, Scal S, float dt, int rk, unsigned lon
     // calc_vpvisc
     float V = 0.f;
     if (rk == 0) V = (p.RSFmode == 1 || p.timesum > 0) ? N.f(V2C_NF_RK_SLIPRS_FINAL)[m3] : 0.f;
-    if ((p.rkmod == 0 && rk > 0) || (rk > 0 && rk < 3)) V = N.f(V2C_NF_RK_SLIPRS_SOLVED)[m3];
+    // later passes take the last solved rate (calc_RSF.c:58-86; the state
+    // rates and the rkmod 3 histories it also selects are never used)
+    if ((p.rkmod == 0 && rk > 0) || (rk > 0 && rk < 3) || (rk == 3 && p.rkmod == 3))
+      V = N.f(V2C_NF_RK_SLIPRS_SOLVED)[m3];
     N.f(V2C_NF_PES)[m3] = N.f(V2C_NF_PE)[m3] + V / W * dt;
     float newstate = 0.f, syield;
     if (p.RSFmode == 1) {
@@ -236,10 +267,14 @@ __global__ void k_before(Grid g, Nodes N, Scal S, float dt, int rk, unsigned lon
       newstate = new_state(ph, V, dt, L, V0);
       const float rad = (p.inertyn == 0) ? 4.3303e+06f * V : 0.f;
       const float a = N.f(V2C_NF_AS)[m3], b = N.f(V2C_NF_BS)[m3], mu = N.f(V2C_NF_MUS_S)[m3];
+      // exponents in float-float (see ff_log_sinh)
+      const ff lnVV0 = ff_log(ff_div(ff_f(V), ff_f(V0)));
       if (p.power_law_RSF > 0)
-        syield = expf(logf(nP * mu) + a / mu * logf(V / V0) + (newstate * b) / mu) + rad;
+        syield = exp_ff(ff_add(ff_add(ff_log(ff_mul_f(nP_ff, mu)), ff_mul(ff_div(ff_f(a), ff_f(mu)), lnVV0)),
+                               ff_div(ff_mul_f(ff_f(newstate), b), ff_f(mu)))) + rad;
       else
-        syield = nP * a * asinh_exp(logf(V / (2.f * V0)) + (mu + newstate * b) / a) + rad;
+        syield = nP * a * asinh_exp_ff(ff_add(ff_sub(lnVV0, ff_ln2()),
+                                              ff_div(ff_add_f(ff_mul_f(ff_f(newstate), b), mu), ff_f(a)))) + rad;
     } else {
       syield = nP * N.f(V2C_NF_MUS_S)[m3] + N.f(V2C_NF_COHESION)[m3];
     }
@@ -275,7 +310,9 @@ __global__ void k_after(Grid g, Nodes N, Scal S, float dt, float *part) {
     long m2 = m3 % g.yn, m1 = m3 / g.yn;
     if (m1 >= 1 && m2 >= 1 && m1 < g.xn - 1 && m2 < g.yn - 1) {
       const float W = (float)p.faultwidth;
-      const float nps = (p.pmode == 0 || p.timesum == 0) ? (float)p.nstress : N.f(V2C_NF_SPPES)[m3];
+      const bool nps_const = p.pmode == 0 || p.timesum == 0;
+      const ff nps_ff = nps_const ? ff{S.sn_hi, S.sn_lo} : ff_f(N.f(V2C_NF_SPPES)[m3]);
+      const float nps = nps_ff.hi;
       const float sxxs = N.f(V2C_NF_SXXS)[m3], sxy = N.f(V2C_NF_SXY)[m3];
       const float sigin = sqrtf(sxxs * sxxs + sxy * sxy);
       const float a = N.f(V2C_NF_AS)[m3], b = N.f(V2C_NF_BS)[m3], mu = N.f(V2C_NF_MUS_S)[m3];
@@ -283,10 +320,19 @@ __global__ void k_after(Grid g, Nodes N, Scal S, float dt, float *part) {
       float V;
       if (p.RSFmode == 1) {
         if (sigin > 0.f) {
+          // the slip rate's exponent in float-float from the FP32 node
+          // values (see ff_log_sinh)
+          const ff sig = ff_sqrt(ff_add(ff_mul(ff_f(sxxs), ff_f(sxxs)), ff_mul(ff_f(sxy), ff_f(sxy))));
+          const ff bpa = ff_div(ff_mul_f(ff_f(ph), b), ff_f(a));  // b phi / a
           if (p.power_law_RSF > 0)
-            V = expf(logf(V0) + (mu / a) * logf(sigin / (nps * mu)) + (-ph * b) / a);
+            V = exp_ff(ff_sub(ff_add(ff_log(ff_f(V0)),
+                                     ff_mul(ff_div(ff_f(mu), ff_f(a)),
+                                            ff_log(ff_div(sig, ff_mul_f(nps_ff, mu))))),
+                              bpa));
           else
-            V = expf(logf(2.f * V0) + log_sinh(sigin / (a * nps)) - (mu + b * ph) / a);
+            V = exp_ff(ff_sub(ff_add(ff_log(ff_f(2.f * V0)),
+                                     ff_log_sinh(ff_div(sig, ff_mul_f(nps_ff, a)))),
+                              ff_add(ff_div(ff_f(mu), ff_f(a)), bpa)));
           const float ex = N.f(V2C_NF_EXXPL)[m3], ey = N.f(V2C_NF_EXY)[m3];
           const float Vslip = sqrtf(ex * ex + ey * ey) * W;
           V = (V <= Vslip) ? V : Vslip;

@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(PT, 5) k_phys(PhysArgs a) {
         const float mkt = conductivity32(a.R, t, T, mpb);
         const float sxx = a.m.sxx[i], sxy = a.m.sxy[i];
         sigin = sqrtf(sxx * sxx + sxy * sxy);
-        mnu = ductile_visc32(a.R, a.S, t, sigin, T, mpb);
+        mnu = ductile_visc32(a.R, a.S, t, sigin, T, a.m.tk_lo[i], mpb);
         const float phi0 = a.m.phi[i];
         phi = marker_friction(a, ix, iy, u, v, ax.X, ay.X, t, phi0, fr);
         if (!collect) {

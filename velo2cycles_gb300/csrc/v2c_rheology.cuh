@@ -8,6 +8,7 @@
 // exp((E+PV)/RT) reaches exp(150) in the reference and overflows FP32, while
 // the ratios the iteration actually needs stay O(1).
 #pragma once
+#include "v2c_ff.cuh"
 #include "v2c_internal.cuh"
 
 namespace v2c {
@@ -31,8 +32,34 @@ __device__ __forceinline__ float conductivity32(const Rock &R, int t, float T, f
 
 // ductilevisc.  Returns NaN for a type that fits no branch (the reference
 // leaves its result undefined there).
+//
+// Precision.  The viscosity is e^s0 times an O(1) ratio, with s0 = ln of
+// the diffusion-creep viscosity, up to ~60: an FP32 s0 alone (ulp 4e-6)
+// would carry several parts in 1e6.  s0 = ln(0.5 k1) + (E + PV)/(RT) is
+// therefore formed as a float pair from the float-pair temperature
+// (T, Tlo) and the per-type constant pairs of the rock table.
+//
+// The creep iteration.  The reference iterates on the dislocation-creep
+// viscosity with an approximate derivative, so it converges linearly (about
+// a dozen steps, up to ~30), and its result is the iterate where the
+// relative change of mnu0 first drops below 1e-6 in log10.  Run directly in
+// FP32, every step carries a rounding error of a few 1e-7 of the iterate:
+// the iterates drift by up to ~2e-6 from the FP64 ones, and the stopping
+// test, which compares changes of ~2e-6, stops a step early or late for a
+// few per cent of the markers.  Here, with d = eta_disl / eta_diff and
+// B(d) = g + d (1 + g) the reference's prefactor term, its residual is
+// f2(d) = d - (q B(d))^em (q = ss/sigin, em = (mm-1)/mm, g = G dt/eta_diff):
+//   1. d*, close to the root of f2, by an FP32 Newton with the exact
+//      derivative;
+//   2. R0 = f2(d*) in float-float, from float pairs of q, g and em;
+//   3. the reference's iteration replayed from its start d0 = q^(mm-1)
+//      (float-float) in the deviation e = d - d*:
+//        f2(d* + e) = R0 + e - (q B*)^em expm1(em log1p(e (1 + g)/B*)),
+//      every term of which FP32 holds to a few 1e-7 of e rather than of d,
+//      as it does the steps and the change that the stopping test reads.
+// The viscosity is e^s0 d/(1 + d) at the step the replay stops.
 __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, int t,
-                                                float sigin, float T, float mpb) {
+                                                float sigin, float T, float Tlo, float mpb) {
   int kind = (int)R(RK_KIND, t);
   if (kind == VISC_STICKY) {
     float nu = R(RK_NU, t);
@@ -43,51 +70,104 @@ __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, in
   if (kind != VISC_POWER) return __int_as_float(0x7fc00000);
 
   const float mm = R(RK_MM, t);
-  const float LN_HALF = -0.693147180559945f;
-  float le1 = (R(RK_DH, t) + R(RK_DV, t) * mpb) / (8.314f * T);
-  if (le1 > 150.f) le1 = 150.f;
+  // (E + PV)/(RT), density_ductilevisc_calc.c:116-120, capped at 150
+  const ff num = ff_add(ff{R(RK_DH, t), R(RK_DH_LO, t)},
+                        ff_mul_f(ff{R(RK_DV, t), R(RK_DV_LO, t)}, mpb));
+  const ff den = ff_mul(ff{T, Tlo}, ff{8.31400012969970703125f, -1.2969971407983394e-07f});
+  ff le1 = den.hi != 0.f ? ff_div(num, den) : ff_f(num.hi / den.hi);
+  if (le1.hi > 150.f || (le1.hi == 150.f && le1.lo > 0.f)) le1 = ff_f(150.f);
   // ln of the diffusion-creep viscosity 0.5 k1 e1, k1 = nu / ss^(mm-1)
-  float s0 = LN_HALF + R(RK_LNNU, t) - (mm - 1.f) * R(RK_LNSS, t) + le1;
-  float lnv = s0;  // sigin == 0: eta = eta_diff
+  const ff s0 = ff_add(ff{R(RK_LNK, t), R(RK_LNK_LO, t)}, le1);
+  float lnr = 0.f;  // ln(eta / eta_diff); sigin == 0: eta = eta_diff
   if (sigin > 0.f) {
-    // eta_disl / eta_diff = (ss / sigin)^(mm-1)
-    const float d0 = exp2f((mm - 1.f) * (R(RK_LNSS, t) - logf(sigin)) * 1.44269504089f);
-    const float g = __expf(__logf(R(RK_GG, t) * S.dt) - s0);  // G dt / eta_diff
-    const float invS = __expf(-s0);
-    const float em = (mm - 1.f) / mm;
-    const float c0 = exp2f(__log2f(d0) / mm);     // coeff / eta_diff^(1/mm)
-    const float emc0 = em * c0;
-    const float p2fac = 2.f * s0 * invS;
-    // |log10(m_k / m_k-1)| < 1e-6  <=>  10^-1e-6 < m_k / m_k-1 < 10^1e-6
-    const float RLO = 0.99999769741f, RHI = 1.00000230259f;
+    const ff em_ff{R(RK_EM, t), R(RK_EM_LO, t)};
+    const float em = em_ff.hi;
+    const ff q_ff = ff_div(ff{R(RK_SS, t), R(RK_SS_LO, t)}, ff_f(sigin));  // ss / sigin
+    const float q = q_ff.hi;
+    // G dt / eta_diff (0 without elasticity or time step)
+    ff g_ff = ff_f(0.f);
+    if (R(RK_LNG, t) > -INFINITY && S.lndt_hi > -INFINITY)
+      g_ff = ff_exp(ff_sub(ff_add(ff{R(RK_LNG, t), R(RK_LNG_LO, t)}, ff{S.lndt_hi, S.lndt_lo}), s0));
+    const float g = g_ff.hi, g1p = 1.f + g;
+    // the reference's start, eta_disl / eta_diff = q^(mm-1) at the marker's
+    // stress, in float-float: an FP32 start would change where the replay
+    // stops in ~0.1 % of the markers
+    const ff lnq = ff_log(q_ff);
+    const ff d0_ff = ff_exp(ff_mul(ff{R(RK_MM1, t), R(RK_MM1_LO, t)}, lnq));
+    const float d0 = d0_ff.hi;
+    // 1. d*: Newton on f2 with its exact derivative (fast intrinsics: only
+    //    its closeness to the root matters, R0 below is exact at it)
+    float ds = d0;
+    for (int it = 0; it < 16; it++) {
+      const float B = fmaf(ds, g1p, g);
+      const float f1c = exp2f(em * __log2f(q * B));  // (q B)^em
+      const float fp = 1.f - em * __fdividef(f1c, B) * g1p;
+      float dn = ds - __fdividef(ds - f1c, fp);
+      if (!(dn > 0.f)) dn = 0.5f * ds;
+      const bool conv = fabsf(dn - ds) <= 1e-6f * ds;
+      ds = dn;
+      if (conv) break;
+    }
+    // 2. R0 = f2(d*) and (q B*)^em in float-float
+    const ff Bs_ff = ff_add(ff_mul_f(ff_add_f(g_ff, 1.f), ds), g_ff);
+    const ff c0f1s_ff = ff_exp(ff_mul(em_ff, ff_add(lnq, ff_log(Bs_ff))));
+    const ff R0 = ff_add_f(ff_neg(c0f1s_ff), ds);
+    const float c0f1s = c0f1s_ff.hi, Bs = Bs_ff.hi, r0 = R0.hi;
+    // 3. the reference's iteration in e = d - d*
+    const float invS = __expf(-s0.hi);
+    const float p2fac = 2.f * s0.hi * invS;
     // the extra derivative term p2 (below) is at most invS e^max(p2fac,0)
-    // (dold >= 0); under half an ulp of gm it cannot change gm + p2 in FP32
+    // (d >= 0); under half an ulp of gm it cannot change gm + p2 in FP32
     const float p2max = invS * __expf(fmaxf(p2fac, 0.f));
-    float dnew = d0, m_prev = 1.f;
+    // |log10(m_k / m_k-1)| < 1e-6  <=>  10^-1e-6 - 1 < m_k / m_k-1 - 1 < 10^1e-6 - 1
+    const float TLO = -2.30258242e-6f, THI = 2.30258771e-6f;
+    const ff e0 = ff_add_f(d0_ff, -ds);
+    float e = e0.hi + e0.lo, e_prev = 0.f, d_prev = 1.f;
+    // per-step constants: B(d)/B* - 1 = x = e (1 + g)/B*; c0 B^em / B
+    // = (c0 B*^em / B*) (1 + g1)/(1 + x)
+    const float inv_Bs = __fdividef(1.f, Bs);
+    const float kx = g1p * inv_Bs, kc = c0f1s * inv_Bs;
+    // (1 + x)^em - 1 = em x (1 + c1 x (1 + c2 x (1 + c3 x))) + O(x^5), for
+    // |x| < 1/32 within 3e-8 of itself (the steps near the stop)
+    const float c1 = 0.5f * (em - 1.f), c2 = (em - 2.f) * (1.f / 3.f), c3 = 0.25f * (em - 3.f);
     for (int counter = 1; counter <= 50; counter++) {
-      const float dold = dnew;
-      const float m = __fdividef(dnew, dnew + 1.f);    // mnu0 / eta_diff
+      const float e_old = e;
+      const float d_old = ds + e_old;
+      const float m = __fdividef(d_old, d_old + 1.f);   // mnu0 / eta_diff
       const float gm = g + m;
-      const float base = (1.f + dold) * gm;            // prefactor (G dt + mnu0) / eta_diff
-      const float f1 = exp2f(em * __log2f(base));      // base^((mm-1)/mm)
-      const float f2 = dold - c0 * f1;
+      // B(d)/B* - 1: below -1 the reference's iteration has gone to a
+      // negative prefactor, whose power is NaN there and is NaN here (log1pf)
+      const float x = e_old * kx;
+      const float g1 = fabsf(x) < 0.03125f
+                           ? em * x * fmaf(c1 * x, fmaf(c2 * x, fmaf(c3, x, 1.f), 1.f), 1.f)
+                           : expm1f(em * log1pf(x));  // (B(d)/B*)^em - 1
+      const float f2 = (e_old - c0f1s * g1) + r0;       // f2(d* + e)
+      const float cfB = __fdividef(kc * (1.f + g1), 1.f + x);  // c0 B^em / B
       // pow(eta_diff, 2/(eta_diff+eta_disl_old)) / eta_diff, the reference's
       // extra term of the derivative (density_ductilevisc_calc.c:190-191)
       const float p2 = (invS > 1e-30f && !(p2max < gm * 0x1p-25f))
-                           ? __expf(__fdividef(p2fac, 1.f + dold)) * invS : 0.f;
-      const float df = 1.f - emc0 * __fdividef(f1, base) * (gm + p2);  // base^(-1/mm) = f1/base
-      dnew = dold - __fdividef(f2, df);
-      // m / m_prev within (RLO, RHI), m and m_prev positive
-      if (counter > 3 && m > RLO * m_prev && m < RHI * m_prev) break;
-      m_prev = m;
+                           ? __expf(__fdividef(p2fac, 1.f + d_old)) * invS : 0.f;
+      const float df = 1.f - em * cfB * (gm + p2);
+      e = e_old - __fdividef(f2, df);
+      // relative change of mnu0 from the previous step: (d - d_prev) /
+      // (d_prev (1 + d)), tested without the division (the denominator > 0)
+      const float D = d_prev * (1.f + d_old), dd = e_old - e_prev;
+      if (counter > 3 && dd > TLO * D && dd < THI * D) break;
+      e_prev = e_old;
+      d_prev = d_old;
     }
-    lnv = s0 - log1pf(1.f / dnew);
+    // d/(1 + d) at the last step, d = d* + e as a float pair
+    float dlo;
+    const float dhi = two_sum(ds, e, dlo);
+    const float inv = __fdividef(1.f, dhi);
+    lnr = -log1pf(inv * (1.f - dlo * inv));
   }
   // limits nubeg/nuend then the per-type limits, in that order
+  const ff lnv = ff_add_f(s0, lnr);
   float nu;
-  if (lnv < S.ln_nubeg) nu = S.nubeg_f;
-  else if (lnv > S.ln_nuend) nu = S.nuend_f;
-  else nu = expf(lnv);
+  if (lnv.hi < S.ln_nubeg) nu = S.nubeg_f;
+  else if (lnv.hi > S.ln_nuend) nu = S.nuend_f;
+  else nu = expf(lnv.hi) * (1.f + lnv.lo);
   if (nu < R(RK_N0, t)) nu = R(RK_N0, t);
   if (nu > R(RK_N1, t)) nu = R(RK_N1, t);
   return nu;

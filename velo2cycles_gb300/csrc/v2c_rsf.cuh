@@ -352,9 +352,11 @@ __device__ __forceinline__ RsfResult rsf_solve_split(const RsfIn &in, const Rsf3
   const ff floor_u = ff_from_double(RSF_LOG_FLOOR);
   ff u = (u32 <= floor32 + 1e-6f) ? floor_u : ff_f(u32);
   // the ratio |F|/(F+T*) needs a few significant digits: F and F+T* come
-  // from the float-float evaluation (absolute error ~1e-13 of F+T*), the
-  // ratio is taken in FP32
-  const float rtolf = (float)rtol;
+  // from the float-float evaluation, the ratio is taken in FP32.  Accepted
+  // at 3/4 of the tolerance: the float-float ratio and the FP64 one at the
+  // same slip rate differ by up to ~1.3e-11 (measured on 20 000 states of
+  // the C3 distributions), and the returned root must meet rtol in FP64.
+  const float rtolf = 0.75f * (float)rtol;
   for (int k = 0; k < 4; k++) {
     ff lhs, phi, A, Vs;
     const ff F = rsf_eval_ff(q, u, lhs, phi, A, Vs);

@@ -202,6 +202,22 @@ __global__ void k_f64_to_f32(const double *src, float *dst, long n) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i < n) dst[i] = (float)src[i];
 }
+// FP64 -> float pair hi + lo (hi the nearest float, lo the nearest float to
+// the remainder)
+__global__ void k_f64_to_pair(const double *src, float *hi, float *lo, long n) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double d = src[i];
+    const float h = (float)d;
+    hi[i] = h;
+    lo[i] = (float)(d - (double)h);
+  }
+}
+__global__ void k_unperm_pair(const float *hi, const float *lo, const int32_t *id, double *out,
+                              long n) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) out[id[i]] = (double)hi[i] + (double)lo[i];
+}
 template <class T>
 __global__ void k_gather(const T *src, const int32_t *perm, T *dst, long n) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -260,6 +276,13 @@ void launch_sort(const int32_t *cell, const float *u, const float *v, long n, lo
 
 void launch_f64_to_f32(const double *src, float *dst, long n, cudaStream_t st) {
   if (n > 0) k_f64_to_f32<<<nblk(n, 256), 256, 0, st>>>(src, dst, n);
+}
+void launch_f64_to_pair(const double *src, float *hi, float *lo, long n, cudaStream_t st) {
+  if (n > 0) k_f64_to_pair<<<nblk(n, 256), 256, 0, st>>>(src, hi, lo, n);
+}
+void launch_unpermute_pair(const float *hi, const float *lo, const int32_t *id, double *out,
+                           long n, cudaStream_t st) {
+  if (n > 0) k_unperm_pair<<<nblk(n, 256), 256, 0, st>>>(hi, lo, id, out, n);
 }
 void launch_gather_f32(const float *src, const int32_t *perm, float *dst, long n, cudaStream_t st) {
   if (n > 0) k_gather<float><<<nblk(n, 256), 256, 0, st>>>(src, perm, dst, n);

@@ -14,6 +14,12 @@
 //      node only, temperature_iterate.c:306-335);
 //   3. per marker: the antidiffusion, minus that node value times the
 //      marker's weight at the node.
+// Marker temperatures are float pairs (tk + tk_lo) and are updated in FP64
+// (a few FP64 operations per marker, outside the MIC step): the viscosity
+// amplifies a temperature error about fifty-fold.  The node temperatures
+// are read from their FP64 copies when the host uploaded TK and TK2 since
+// the last marker2nodes, so a marker that takes the solved temperature, or
+// its change TK - TK2, takes it at FP64 precision.
 #include <math.h>
 
 #include "v2c_kernels.h"
@@ -57,14 +63,23 @@ __global__ void k_temp_markers(TempArgs a) {
     // interpolate_temperature (interpolation.c:1492-1533) in the marker's cell
     const long m3 = (long)ix * yn + iy;
     const float d0 = (1.f - u) * (1.f - v), d1 = (1.f - u) * v, d2 = u * (1.f - v), d3 = u * v;
-    const float TK = d0 * tk[m3] + d1 * tk[m3 + 1] + d2 * tk[m3 + yn] + d3 * tk[m3 + yn + 1];
-    const float TK2 = d0 * tk2[m3] + d1 * tk2[m3 + 1] + d2 * tk2[m3 + yn] + d3 * tk2[m3 + yn + 1];
-    if (t >= 50) {
-      a.m.tk[idx] = TK;
-      continue;
+    double TK, TK2;
+    if (a.tk64 && a.tk2_64) {
+      const double *p = a.tk64, *q = a.tk2_64;
+      TK = (double)d0 * p[m3] + (double)d1 * p[m3 + 1] + (double)d2 * p[m3 + yn] +
+           (double)d3 * p[m3 + yn + 1];
+      TK2 = (double)d0 * q[m3] + (double)d1 * q[m3 + 1] + (double)d2 * q[m3 + yn] +
+            (double)d3 * q[m3 + yn + 1];
+    } else {
+      TK = d0 * tk[m3] + d1 * tk[m3 + 1] + d2 * tk[m3 + yn] + d3 * tk[m3 + yn + 1];
+      TK2 = d0 * tk2[m3] + d1 * tk2[m3 + 1] + d2 * tk2[m3 + yn] + d3 * tk2[m3 + yn + 1];
     }
-    float mk = a.m.tk[idx];
-    if (mk <= 0.f) mk = TK2 < a.tdeep ? a.tdeep : TK2;  // newly arrived marker
+    double mk;
+    if (t >= 50) {
+      mk = TK;
+    } else {
+    mk = (double)a.m.tk[idx] + (double)a.m.tk_lo[idx];
+    if (mk <= 0.0) mk = TK2 < a.tdeep64 ? a.tdeep64 : TK2;  // newly arrived marker
     if (a.heatdif != 0.f) {
       const float wx = __ldg(g.wx + ix), wy = __ldg(g.wy + iy);
       // node order of the reference's loop: m1 outer, m2 inner
@@ -73,13 +88,16 @@ __global__ void k_temp_markers(TempArgs a) {
                           cp[m3 + yn] * ro[m3 + yn] * d2 + cp[m3 + yn + 1] * ro[m3 + yn + 1] * d3;
       float e = -a.heatdif * mkt / mrocp * 2.f * (1.f / (wx * wx) + 1.f / (wy * wy)) * a.dt;
       if (e < -150.f) e = -150.f;
-      const float dtk1 = -(TK2 - mk) * expm1f(e);  // dtk (1 - exp(e))
+      const float dtk1 = -(float)(TK2 - mk) * expm1f(e);  // dtk (1 - exp(e))
       mk += dtk1;
       a.dtk1[s] = dtk1;
       a.wt[s] = d0 / (wx * wy);
     }
     mk += TK - TK2;
-    a.m.tk[idx] = mk;
+    }
+    const float hi = (float)mk;
+    a.m.tk[idx] = hi;
+    a.m.tk_lo[idx] = (float)(mk - (double)hi);
   }
 }
 
@@ -114,7 +132,11 @@ __global__ void k_temp_anti(TempArgs a) {
     const float t = a.tol[(long)ix * g.yn + iy];
     if (t != 0.f) {
       const float u = a.m.u_in[idx], v = a.m.v_in[idx];
-      a.m.tk[idx] -= t * ((1.f - u) * (1.f - v));
+      const double mk = (double)a.m.tk[idx] + (double)a.m.tk_lo[idx] -
+                        (double)(t * ((1.f - u) * (1.f - v)));
+      const float hi = (float)mk;
+      a.m.tk[idx] = hi;
+      a.m.tk_lo[idx] = (float)(mk - (double)hi);
     }
   }
 }

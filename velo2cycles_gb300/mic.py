@@ -89,13 +89,19 @@ class MarkerInCell:
         t = np.ascontiguousarray(markt, dtype=np.int8)
         call("v2c_upload_markers", self.h, arr, t.ctypes.data_as(ctypes.POINTER(ctypes.c_byte)), n)
         self.n = n
+        # immobile markers (type >= 100) append markers in the move
+        self._immobile = bool((t >= 100).any())
+
+    def _refresh_n(self):
+        if getattr(self, "_immobile", False):
+            self.n = int(self.status()["n_markers"])
 
     def download_markers(self, fields=None, into: dict | None = None):
         """FP64 marker arrays in reference numbering.  markd/markw given in
         `into` are updated in place (set to -1 for markers reset after
         leaving the grid)."""
         fields = list(range(abi.MF_N)) if fields is None else list(fields)
-        device_fields = {abi.MF_X, abi.MF_Y, abi.MF_K, abi.MF_E, abi.MF_P, abi.MF_XX,
+        device_fields = {abi.MF_X, abi.MF_Y, abi.MF_K, abi.MF_V, abi.MF_E, abi.MF_P, abi.MF_XX,
                          abi.MF_XY, abi.MF_EXX, abi.MF_EXY, abi.MF_VX, abi.MF_VY, abi.MF_PHI,
                          abi.MF_C, abi.MF_SLIPV}
         out = {} if into is None else into
@@ -213,6 +219,7 @@ class MarkerInCell:
     def cycle_step(self, regime: int, dt: float, use_graph: bool = True):
         """One seismic-cycle step (see v2c_cycle_step); timesum advances."""
         call("v2c_cycle_step", self.h, int(regime), float(dt), int(bool(use_graph)))
+        self._refresh_n()
         self.params["timestep"] = float(dt)
         self.params["timesum"] = float(self.params["timesum"]) + float(dt)
 
@@ -239,9 +246,11 @@ class MarkerInCell:
 
     def moveandrotatemarkers(self):
         call("v2c_moveandrotatemarkers", self.h)
+        self._refresh_n()
 
     def nodes2markers_move(self):
         call("v2c_nodes2markers_move", self.h)
+        self._refresh_n()
 
     def synchronize(self):
         call("v2c_synchronize", self.h)
