@@ -234,6 +234,16 @@ int v2c_download_markers(v2c_ctx *ctx, double *const *fields,
 /* Cell index of every marker (reference numbering) as found on the device:
  * ix*(ynumy-1)+iy with ix = nxsearch(x), iy = nysearch(y). */
 int v2c_download_cells(v2c_ctx *ctx, int32_t *cell, long n);
+/* The per-marker properties the last v2c_marker2nodes evaluated
+ * (recalc_marker_properties.c:1-83): ductile viscosity mnu (ductilevisc,
+ * density_ductilevisc_calc.c:29-223) and thermal conductivity mkt, n
+ * doubles each in reference numbering (either pointer may be NULL).
+ * Markers outside the model, which the reference skips, read 0.  Valid
+ * from marker2nodes until the markers are uploaded or moved
+ * (V2C_ERR_STATE otherwise); synchronous.  The reference keeps these as
+ * locals of its marker loop (interpolation.c:229-240) and has no
+ * accessor. */
+int v2c_download_marker_properties(v2c_ctx *ctx, double *mnu, double *mkt, long n);
 
 /* ============================================================= node arrays
  * One node field (V2C_NF_*) of nodenum doubles, converted to / from the

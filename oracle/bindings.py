@@ -97,6 +97,9 @@ def _lib():
         lib.v2c_oracle_stokes_assemble.argtypes = [
             P(_State), P(abi.StokesCtl), ctypes.c_long, P(ctypes.c_int), P(ctypes.c_int),
             P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_long)]
+        lib.v2c_oracle_marker_properties.restype = ctypes.c_int
+        lib.v2c_oracle_marker_properties.argtypes = [P(_State), P(ctypes.c_double),
+                                                     P(ctypes.c_double), P(ctypes.c_double)]
         lib.v2c_oracle_copyarrays.restype = ctypes.c_int
         lib.v2c_oracle_copyarrays.argtypes = [P(_State)]
         lib.v2c_oracle_center2basic.restype = ctypes.c_int
@@ -189,6 +192,14 @@ class Restatement:
 
     def marker2nodes(self):
         return self.lib.v2c_oracle_marker2nodes(ctypes.byref(self.st))
+
+    def marker_properties(self):
+        """(viscosity, conductivity, pressure in bar) of every current
+        marker as marker2nodes evaluates them; 0 outside the model."""
+        n = self.n
+        nu, kt, pb = np.zeros(n), np.zeros(n), np.zeros(n)
+        self.lib.v2c_oracle_marker_properties(ctypes.byref(self.st), _dp(nu), _dp(kt), _dp(pb))
+        return nu, kt, pb
 
     def center2basic_old(self):
         return self.lib.v2c_oracle_center2basic_old(ctypes.byref(self.st))

@@ -524,6 +524,37 @@ static int bc_corrections(v2c_oracle_state *s) {
 
 /* ============================================================ marker2nodes
  * interpolation.c:55-926 */
+/* recalc_marker_properties.c:1-83 for every marker strictly inside the
+ * model (interpolation.c:219-240): the ductile viscosity, the thermal
+ * conductivity and the pressure in bar each marker is evaluated at, in
+ * marker order; markers outside read 0.  The marker state is not changed
+ * (the friction update of calc_frictionpara is left out). */
+int v2c_oracle_marker_properties(const v2c_oracle_state *s, double *mnu, double *mkt,
+                                 double *mpb_out) {
+  const v2c_params *p = &s->p;
+  double *const *M = s->M;
+  for (long mm1 = 0; mm1 < s->n; mm1++) {
+    double x = M[V2C_MF_X][mm1], y = M[V2C_MF_Y][mm1];
+    double nu = 0, kt = 0, mpb = 0;
+    if (x > 0 && y > 0 && x < p->xsize && y < p->ysize) {
+      int mm2 = s->t[mm1];
+      double mtk = M[V2C_MF_K][mm1];
+      mpb = 1e-5 * interp_pressure(s, x, y);
+      kt = RT(s, V2C_RT_KT, mm2);
+      kt = (kt + RT(s, V2C_RT_KF, mm2) / (mtk + 77.0)) * exp(RT(s, V2C_RT_KP, mm2) * mpb);
+      if (kt < 0)
+        kt = -kt / (1.0 + RT(s, V2C_RT_KF, mm2) * (mtk - RT(s, V2C_RT_KP, mm2)) /
+                              RT(s, V2C_RT_KP, mm2));
+      nu = v2c_oracle_ductilevisc(s, mm2, M[V2C_MF_XY][mm1], M[V2C_MF_XX][mm1],
+                                  M[V2C_MF_EXY][mm1], M[V2C_MF_EXX][mm1], mtk, mpb);
+    }
+    if (mnu) mnu[mm1] = nu;
+    if (mkt) mkt[mm1] = kt;
+    if (mpb_out) mpb_out[mm1] = mpb;
+  }
+  return V2C_OK;
+}
+
 int v2c_oracle_marker2nodes(v2c_oracle_state *s) {
   const v2c_params *p = &s->p;
   long xn = p->xnumx, yn = p->ynumy, nn = nnodes(s);

@@ -63,6 +63,10 @@ int v2c_oracle_move(v2c_oracle_state *s);
 int v2c_oracle_calc_timestep(const v2c_oracle_state *s, int oldornew,
                              const v2c_timestep_ctl *c, v2c_timestep_info *info);
 
+/* per-marker viscosity, conductivity and pressure (bar) of
+ * recalc_marker_properties, 0 outside the model */
+int v2c_oracle_marker_properties(const v2c_oracle_state *s, double *mnu, double *mkt,
+                                 double *mpb);
 /* per-marker ductile viscosity, density_ductilevisc_calc.c:29-223 */
 double v2c_oracle_ductilevisc(const v2c_oracle_state *s, int mm2, double SXY,
                               double SXX, double EXY, double EXX, double mtk,

@@ -288,13 +288,13 @@ def stokes_case(seed, name="tiny", variant="default"):
 
 
 def rel_err(a: np.ndarray, b: np.ndarray, signed: bool = True, log: bool = False,
-            abs_floor: float = 0.0) -> float:
+            abs_floor=0.0) -> float:
     """Largest per-entry error of a against the reference b (module
     docstring): max |a - b| / max(|b|, floor), floor = max(abs_floor,
-    FLOOR_FRAC * RMS(b)) for a signed field, abs_floor otherwise; for a
-    log field the relative error of the logarithm.  Entries where the floor
-    and b are both zero must match exactly; NaN/inf must sit at the same
-    entries."""
+    FLOOR_FRAC * RMS(b)) for a signed field, abs_floor otherwise (a scalar,
+    or an array of per-entry floors); for a log field the relative error of
+    the logarithm.  Entries where the floor and b are both zero must match
+    exactly; NaN/inf must sit at the same entries."""
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     fin = np.isfinite(b)
@@ -303,6 +303,8 @@ def rel_err(a: np.ndarray, b: np.ndarray, signed: bool = True, log: bool = False
     if not fin.any():
         return 0.0
     aa, bb = a[fin], b[fin]
+    if np.ndim(abs_floor):
+        abs_floor = np.asarray(abs_floor, dtype=np.float64)[fin]
     if log:
         if (aa < 0).any() or (bb < 0).any():
             return float("inf")
@@ -311,7 +313,7 @@ def rel_err(a: np.ndarray, b: np.ndarray, signed: bool = True, log: bool = False
         return float(np.abs(la - lb).max())
     floor = abs_floor
     if signed:
-        floor = max(floor, FLOOR_FRAC * float(np.sqrt(np.mean(bb * bb))))
+        floor = np.maximum(floor, FLOOR_FRAC * float(np.sqrt(np.mean(bb * bb))))
     den = np.maximum(np.abs(bb), floor)
     d = np.abs(aa - bb)
     zero = den == 0
@@ -331,8 +333,54 @@ def node_err(f: int, a, b, ref: dict | None = None) -> float:
     return rel_err(a, b, f in SIGNED_NODE or f in RATE_NODE, f in LOG_NODE, floor)
 
 
-def marker_err(f: int, a, b) -> float:
-    return rel_err(a, b, f in SIGNED_MARK, f in LOG_MARK)
+def marker_err(f: int, a, b, floor=0.0) -> float:
+    return rel_err(a, b, f in SIGNED_MARK, f in LOG_MARK, floor)
+
+
+# node fields each marker field takes in nodes2markers (interpolation.c:
+# 943-1011): the current field, and the previous one that the marker's change
+# is measured from without antidiffusion
+N2M_SOURCES = {
+    abi.MF_XX: (abi.NF_SXX, abi.NF_SXXE), abi.MF_XY: (abi.NF_SXY, abi.NF_SXYE),
+    abi.MF_EXX: (abi.NF_EXX, abi.NF_EXXE), abi.MF_EXY: (abi.NF_EXY, abi.NF_EXYE),
+    abi.MF_P: (abi.NF_PR, abi.NF_SPPE), abi.MF_VX: (abi.NF_VX, abi.NF_MVX),
+    abi.MF_VY: (abi.NF_VY, abi.NF_MVY), abi.MF_PHI: (abi.NF_PHIS_IT, abi.NF_PHIS),
+    abi.MF_E: (abi.NF_PES, abi.NF_PE)}
+
+
+def n2m_floors(ref) -> dict:
+    """Per-marker floors of the marker fields nodes2markers writes, taken on
+    the state it starts from (call before the oracle's nodes2markers): the
+    largest magnitude among the node values of the 4 x 4 block of node lines
+    around the marker's cell (every stencil of interpolate_mechanical lies
+    in it) in the node fields the marker field is interpolated from.  The
+    interpolation is a weighted sum of those FP32 node values; where they
+    differ in sign or by orders of magnitude (a shear band two cells wide
+    beside a quiet far field) its FP32 evaluation -- weights, products,
+    sums -- is exact only to a few 1e-8 of them, not of the result, and
+    that is the scale its error is measured against."""
+    x, y = ref.marks[abi.MF_X], ref.marks[abi.MF_Y]
+    gx, gy = ref.gx, ref.gy
+    xn, yn = gx.size, gy.size
+    ix, iy = nxsearch_np(gx, x), nxsearch_np(gy, y)
+    idx = [np.clip(ix + dx, 0, xn - 1) * yn + np.clip(iy + dy, 0, yn - 1)
+           for dx in range(-1, 3) for dy in range(-1, 3)]
+    out = {}
+    for f, srcs in N2M_SOURCES.items():
+        m = np.zeros(x.size)
+        for k in srcs:
+            a = np.abs(np.asarray(ref.nodes[k], dtype=np.float64))
+            for q in idx:
+                m = np.maximum(m, a[q])
+        out[f] = m
+    return out
+
+
+def rotated_floors(fl: dict) -> dict:
+    """The floors after the move's stress rotation, which mixes xx and xy."""
+    out = dict(fl)
+    out[abi.MF_XX] = out[abi.MF_XY] = np.maximum(fl[abi.MF_XX], fl[abi.MF_XY])
+    return out
 
 
 def node_errors(got: dict, ref: dict, fields) -> dict:
@@ -360,9 +408,12 @@ def over(errs: dict, tol: float = 1e-6) -> dict:
     return {k: v for k, v in errs.items() if not v <= tolerance(k, tol)}
 
 
-def marker_errors(got: dict, ref: dict, fields) -> dict:
+def marker_errors(got: dict, ref: dict, fields, floors: dict | None = None) -> dict:
+    """per-field rel_err of marker fields; floors: per-marker floors
+    (n2m_floors) of the fields that have them"""
     names = abi.marker_field_names()
-    return {names[f]: marker_err(f, got[f], ref[f]) for f in fields}
+    fl = floors or {}
+    return {names[f]: marker_err(f, got[f], ref[f], fl.get(f, 0.0)) for f in fields}
 
 
 def nxsearch_np(g: np.ndarray, x: np.ndarray) -> np.ndarray:

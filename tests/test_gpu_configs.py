@@ -9,7 +9,9 @@ moveandrotatemarkers -- on
     16 markers per cell (6.4 M), the C2 marker-field distributions;
 against the FP64 oracle on the state as the device holds it
 (parity.device_view), every node and marker field the stages write,
-per entry (parity.rel_err) at 1e-6; cells bit-exact before and after the
+per entry (parity.rel_err) at 1e-6 -- marker fields against the
+magnitude of the node values they are interpolated from (parity.n2m_floors)
+-- ; cells bit-exact before and after the
 move; positions within 3e-7 cell widths.
 """
 import numpy as np
@@ -18,7 +20,7 @@ import pytest
 from velo2cycles_gb300 import abi, mic, synth
 
 from .parity import (C2B_OUT, M2N_OUT, MOVE_MARK, N2M_MARK, N2M_OUT, RSF_OUT, marker_errors,
-                     node_errors, nxsearch_np, oracle_for, over)
+                     n2m_floors, node_errors, nxsearch_np, oracle_for, over, rotated_floors)
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-6
@@ -58,17 +60,21 @@ def test_full_step_per_stage(config):
     f = C2B_OUT + RSF_OUT
     bad, report["node RSF"] = _check(m.download_nodes(f), ref.nodes, f, node_errors)
     assert not bad, (name, "center2basic_old + node RSF", bad)
+    # marker fields against the magnitude of the node values they are
+    # interpolated from (parity.n2m_floors)
+    fl = n2m_floors(ref)
     m.nodes2markers(); ref.nodes2markers()
     bad, report["nodes2markers"] = _check(m.download_nodes(N2M_OUT), ref.nodes, N2M_OUT,
                                           node_errors)
     assert not bad, (name, "nodes2markers nodes", bad)
     bad, report["markers"] = _check(m.download_markers(N2M_MARK), ref.marks, N2M_MARK,
-                                    marker_errors)
+                                    lambda a, b, f: marker_errors(a, b, f, fl))
     assert not bad, (name, "nodes2markers markers", bad)
     m.moveandrotatemarkers(); ref.move()
     mk = m.download_markers(MOVE_MARK)
     fields = [k for k in MOVE_MARK if k not in (abi.MF_X, abi.MF_Y)]
-    bad, report["move"] = _check(mk, ref.marks, fields, marker_errors)
+    rfl = rotated_floors(fl)
+    bad, report["move"] = _check(mk, ref.marks, fields, lambda a, b, f: marker_errors(a, b, f, rfl))
     assert not bad, (name, "move", bad)
     for k, g in ((abi.MF_X, c.gx), (abi.MF_Y, c.gy)):
         w = np.diff(g)[nxsearch_np(g, ref.marks[k])]

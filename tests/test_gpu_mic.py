@@ -7,7 +7,9 @@ offset), so the comparison measures the device's arithmetic.  Tolerances,
 per entry (parity.rel_err: relative; for fields that cross zero with the
 field's RMS as a floor; slip rates through the relative error of ln V):
   * cell indices: bit-exact against nxsearch/nysearch on the FP64 positions;
-  * node and marker fields: 1e-6;
+  * node and marker fields: 1e-6 (marker fields that nodes2markers
+    interpolates, against the magnitude of the node values they come from:
+    parity.n2m_floors);
   * positions after the move: 3e-7 cell widths (the FP32 offset resolves
     2^-24 = 6e-8 of a cell).
 What FP32 storage adds on top (oracle against oracle) is bounded in
@@ -19,7 +21,7 @@ import pytest
 from velo2cycles_gb300 import abi, mic, synth
 
 from .parity import (B2C_C2B_OUT, C2B_OUT, COPY_OUT, M2N_OUT, RECOMPUTE_OUT, immobile_case,
-                     marker_err,
+                     marker_err, n2m_floors, rotated_floors,
                      temperature_case, MOVE_MARK, N2M_MARK, N2M_OUT, RSF_OUT, device_view,
                      node_errors, marker_errors, nxsearch_np, oracle_for, over)
 
@@ -64,6 +66,22 @@ def test_marker2nodes(case):
     st = m.status()
     assert st["n_nan"] == 0
     m.close()
+
+
+def test_marker_properties(case):
+    """Per-marker viscosity and conductivity of marker2nodes
+    (recalc_marker_properties.c) against the oracle's, entry by entry: the
+    viscosities span 1e17-1e26 Pa s, and the node averages that carry them
+    would hide a marker far below its node's largest."""
+    m = mic.from_case(case)
+    m.marker2nodes()
+    nu, kt = m.download_marker_properties()
+    m.close()
+    nu_r, kt_r, _ = oracle_for(case).marker_properties()
+    inside = nu_r > 0
+    assert np.array_equal(nu > 0, inside)
+    assert np.abs(nu[inside] / nu_r[inside] - 1).max() <= TOL
+    assert np.abs(kt[inside] / kt_r[inside] - 1).max() <= TOL
 
 
 def test_center2basic_and_node_rsf(case):
@@ -200,12 +218,13 @@ def test_marker_temperature(heatdif, built_lib, oracle_built):
 def test_nodes2markers(case):
     m = mic.from_case(case)
     ref = oracle_for(case)
+    fl = n2m_floors(ref)
     m.nodes2markers()
     ref.nodes2markers()
     got = m.download_nodes(N2M_OUT)
     _check_nodes(node_errors(got, ref.nodes, N2M_OUT))
     mk = m.download_markers(N2M_MARK)
-    errs = marker_errors(mk, ref.marks, N2M_MARK)
+    errs = marker_errors(mk, ref.marks, N2M_MARK, fl)
     bad = over(errs, TOL)
     assert not bad, f"marker fields over tolerance: {bad}"
     m.close()
@@ -270,12 +289,13 @@ def test_flag_variants_full_step(variant, built_lib, oracle_built):
     m.compute_before_solve(dt, 0); ref.compute_before_solve(dt, 0)
     m.compute_after_solve(dt, 0); ref.compute_after_solve(dt, 0)
     _check_nodes(node_errors(m.download_nodes(C2B_OUT + RSF_OUT), ref.nodes, C2B_OUT + RSF_OUT))
+    fl = n2m_floors(ref)
     m.nodes2markers(); ref.nodes2markers()
     _check_nodes(node_errors(m.download_nodes(N2M_OUT), ref.nodes, N2M_OUT))
     m.moveandrotatemarkers(); ref.move()
     mk = m.download_markers(N2M_MARK + MOVE_MARK)
     fields = [f for f in N2M_MARK if f not in (abi.MF_X, abi.MF_Y)]
-    errs = marker_errors(mk, ref.marks, fields)
+    errs = marker_errors(mk, ref.marks, fields, rotated_floors(fl))
     bad = over(errs, TOL)
     assert not bad, bad
     wx = np.diff(c.gx)[nxsearch_np(c.gx, ref.marks[abi.MF_X])]

@@ -37,6 +37,7 @@ _SIGS = {
     "v2c_upload_markers": [c_ctx, P(c_dp), P(ctypes.c_byte), ctypes.c_long],
     "v2c_download_markers": [c_ctx, P(c_dp), P(ctypes.c_byte), ctypes.c_long],
     "v2c_download_cells": [c_ctx, P(ctypes.c_int32), ctypes.c_long],
+    "v2c_download_marker_properties": [c_ctx, c_dp, c_dp, ctypes.c_long],
     "v2c_upload_node_field": [c_ctx, ctypes.c_int, c_dp],
     "v2c_download_node_field": [c_ctx, ctypes.c_int, c_dp],
     "v2c_interpolate_basic2center": [c_ctx],

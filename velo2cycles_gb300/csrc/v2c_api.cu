@@ -57,6 +57,9 @@ struct v2c_ctx {
   void *marker_mem[32] = {};
   int n_marker_mem = 0;
   bool have_markers = false;
+  // m.mnu / m.mkt hold the properties of the current marker slots (set by
+  // marker2nodes, cleared when markers are uploaded or moved)
+  bool props_valid = false;
   // sort
   SortBufs sb{};
   bool sorted = false;
@@ -695,6 +698,7 @@ extern "C" int v2c_upload_markers(v2c_ctx *ctx, const double *const *fields,
   CK(cudaGetLastError());
   ctx->have_markers = true;
   ctx->sorted = true;
+  ctx->props_valid = false;
   return V2C_OK;
 }
 
@@ -741,6 +745,21 @@ extern "C" int v2c_download_markers(v2c_ctx *ctx, double *const *fields, signed 
     }
   }
   CK(cudaStreamSynchronize(st));
+  return V2C_OK;
+}
+
+extern "C" int v2c_download_marker_properties(v2c_ctx *ctx, double *mnu, double *mkt, long n) {
+  if (!ctx || n != ctx->n) return V2C_ERR_ARG;
+  if (!ctx->have_markers || !ctx->props_valid) return fail(ctx, V2C_ERR_STATE);
+  cudaStream_t st = ctx->stream;
+  const float *src[2] = {ctx->m.mnu, ctx->m.mkt};
+  double *dst[2] = {mnu, mkt};
+  for (int k = 0; k < 2; k++) {
+    if (!dst[k]) continue;
+    launch_unpermute_f32(src[k], ctx->m.id, ctx->d_stage64, n, st);
+    CK(cudaMemcpyAsync(dst[k], ctx->d_stage64, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
   return V2C_OK;
 }
 
@@ -916,6 +935,7 @@ extern "C" int v2c_marker2nodes(v2c_ctx *ctx) {
     launch_m2n(a, st);
     ctx->launches += ctx->p.interpolationmod == 1 ? 4 : 1;
   }
+  ctx->props_valid = true;
   {
     Prof pr(ctx, V2C_PROF_M2N_TAIL);
     launch_sticky(a.N, ctx->d_sticky, ctx->nn, st);
@@ -976,7 +996,7 @@ extern "C" int v2c_interpolate_center2basic(v2c_ctx *ctx, double dt) {
   if (!ctx->have_grid) return fail(ctx, V2C_ERR_STATE);
   {
     Prof pr(ctx, V2C_PROF_B2C);
-    launch_c2b(make_grid(ctx), make_nodes(ctx), (float)dt, ctx->dsxx_valid ? 1 : 0, ctx->stream);
+    launch_c2b(make_grid(ctx), make_nodes(ctx), dt, ctx->dsxx_valid ? 1 : 0, ctx->stream);
   }
   ctx->launches += 1;
   CK(cudaGetLastError());
@@ -989,7 +1009,7 @@ extern "C" int v2c_recompute_stress_strainrate(v2c_ctx *ctx, double dt) {
   {
     Prof pr(ctx, V2C_PROF_B2C);
     const bool v64 = ctx->d_vel64 && ctx->vel64_ok[0] && ctx->vel64_ok[1];
-    launch_recompute(make_grid(ctx), make_nodes(ctx), make_scal(ctx->p, ctx->h_rt), (float)dt,
+    launch_recompute(make_grid(ctx), make_nodes(ctx), make_scal(ctx->p, ctx->h_rt), dt,
                      v64 ? ctx->d_vel64 : nullptr, v64 ? ctx->d_vel64 + ctx->nn : nullptr,
                      ctx->stream);
   }
@@ -1075,6 +1095,7 @@ static int n2m_move(v2c_ctx *ctx, int do_n2m, int do_move) {
     ctx->launches += a.bs ? 3 : 1;
   }
   if (do_move) {
+    ctx->props_valid = false;
     const bool imm = ctx->n_immobile > 0 && ctx->n > 0;
     if (imm) {
       CK(cudaMemsetAsync(ctx->imm.spawn, 0, sizeof(int32_t) * ctx->n, st));
@@ -1363,6 +1384,7 @@ extern "C" int v2c_cycle_step(v2c_ctx *ctx, int regime, double dt, int use_graph
   if (regime < 0 || regime > 1 || !(dt > 0)) return fail(ctx, V2C_ERR_ARG);
   if (!ctx->d_cyc_v[regime] || !ctx->d_slip) return fail(ctx, V2C_ERR_STATE);
   ctx->p.timestep = dt;
+  ctx->props_valid = false;  // the step moves the markers
   cudaStream_t st = ctx->stream;
   // immobile markers change the marker count inside the step (a host
   // synchronisation), which a captured graph cannot hold: run eagerly

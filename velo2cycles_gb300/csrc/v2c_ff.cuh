@@ -126,6 +126,15 @@ __device__ __forceinline__ ff ff_sqrt(ff a) {
   return ff_scale(ff{hh, l}, pow2i(h));
 }
 
+// the float nearest to a float pair
+__device__ __forceinline__ float ff_round(ff a) { return __fadd_rn(a.hi, a.lo); }
+// b - c of two floats, exactly, as a float pair
+__device__ __forceinline__ ff ff_diff(float b, float c) {
+  ff r;
+  r.hi = two_sum(b, -c, r.lo);
+  return r;
+}
+
 // ln 2 as a float pair
 __device__ __forceinline__ ff ff_ln2() { return ff{0.693147182464599609375f, -1.9046542e-09f}; }
 

@@ -128,6 +128,14 @@ struct Acc {
   __device__ __forceinline__ float value() const { return s + c; }
 };
 
+// The centre-node weight factor 1 - 2|f - 1/2| of an in-cell offset f
+// (interpolation.c:620-622), written as 2f below the middle and 2(1 - f)
+// above it: the same value, exact in FP32 (1 - f is exact for f >= 1/2),
+// where the literal form loses the low bits of a marker near the cell edge
+// -- whose weight is then tiny but whose viscosity may be 1e6 times its
+// neighbours' and decide the node's average.
+__device__ __forceinline__ float tent(float f) { return f < 0.5f ? 2.f * f : 2.f * (1.f - f); }
+
 // --------------------------------------------------- cell-local geometry
 // Offsets of the grid lines i-1 .. i+2 relative to line i, in FP32.
 struct Axis {

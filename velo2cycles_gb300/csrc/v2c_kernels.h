@@ -123,10 +123,10 @@ void launch_fields_to_f32(const double *stage, long nn, const int *fields, int c
                           cudaStream_t st);
 
 void launch_c2b_old(const Grid &g, const Nodes &N, cudaStream_t st);
-void launch_c2b(const Grid &g, const Nodes &N, float dt, int use_dsxx, cudaStream_t st);
+void launch_c2b(const Grid &g, const Nodes &N, double dt, int use_dsxx, cudaStream_t st);
 void launch_b2c(const Grid &g, const Nodes &N, unsigned long long *stat, cudaStream_t st);
 // vx64, vy64: FP64 node velocities for the strain rates (nullptr: the FP32 fields)
-void launch_recompute(const Grid &g, const Nodes &N, const Scal &S, float dt, const double *vx64,
+void launch_recompute(const Grid &g, const Nodes &N, const Scal &S, double dt, const double *vx64,
                       const double *vy64, cudaStream_t st);
 void launch_copyarrays(const Grid &g, const Nodes &N, cudaStream_t st);
 // accumulated slip of every marker: acc[i] += dt * slipv[i]

@@ -29,6 +29,7 @@
 // 1 basic-node thermal group, 2 centre node, 3 vx and vy nodes.
 #include <math.h>
 
+#include "v2c_ff.cuh"
 #include "v2c_kernels.h"
 #include "v2c_internal.cuh"
 
@@ -156,13 +157,32 @@ __device__ __forceinline__ void node_friction(const M2NArgs &a, int ci, int j, f
     A[6].add(w);                                                      \
   } while (0)
 
+// A compensated sum as a float pair.
+__device__ __forceinline__ ff acc_ff(const Acc &a) {
+  ff r;
+  r.hi = two_sum(a.s, a.c, r.lo);
+  return r;
+}
+// num / den of two compensated sums, rounded once
+__device__ __forceinline__ float ratio(const Acc &num, const ff &den) {
+  return ff_round(ff_div(acc_ff(num), den));
+}
+// the antidiffusion form cur + (n - prev) (interpolation.c:730-736, 758-763,
+// 784-806) from the float-pair node average n: cur and prev are consecutive
+// states of one field that agree in their leading digits, so cur - prev is
+// formed exactly and the sum is rounded once.
+__device__ __forceinline__ float antid_rn(const ff &n, float cur, float prev) {
+  return ff_round(ff_add(n, ff_diff(cur, prev)));
+}
+
 // The node tail of marker2nodes (interpolation.c:714-824) for node row j
 // of column ci, from the compensated sums of one role: 0 basic node (ci, j)
 // stress/state group (cur[0..7]: nu, nu/G, e, sxy, exy, C, phi, w), 1 its
 // thermal group (cur[0..6]: ro, et, ht, cp, kt, tk, w), 2 the centre node
 // (ci+1, j+1) of cell (ci, j) (cur[0..5]: nu, nu/G, sxx, exx, p, w) and the
 // centre fields of (ci, j) when no cell feeds it, 3 vx node (ci, j)
-// (cur[0..2]: vx*ro, ro, w) and vy node (ci, j) (vy3[0..2]).
+// (cur[0..2]: vx*ro, ro, w) and vy node (ci, j) (vy3[0..2]).  The averages
+// are float-pair quotients of the float-pair sums, rounded once to FP32.
 __device__ __forceinline__ void node_tail(const M2NArgs &a, int role, int ci, int j,
                                           const Acc (&cur)[8], const Acc (&vy3)[3]) {
   const Grid &g = a.g;
@@ -171,49 +191,51 @@ __device__ __forceinline__ void node_tail(const M2NArgs &a, int role, int ci, in
   const Nodes &N = a.N;
   const int antid = a.S.antid;
   if (role == 0) {
-    const float ss = cur[7].value();
+    const ff ssf = acc_ff(cur[7]);
+    const float ss = ff_round(ssf);
     const bool interior = ci >= 1 && j >= 1 && ci < g.xn - 1 && j < g.yn - 1;
     if (ss != 0.f && interior) {
-      float phin = __fdividef(cur[6].value(), ss), sxyen = __fdividef(cur[3].value(), ss);
-      float exyen = __fdividef(cur[4].value(), ss), pen = __fdividef(cur[2].value(), ss);
+      const ff phin = ff_div(acc_ff(cur[6]), ssf), sxyen = ff_div(acc_ff(cur[3]), ssf);
+      const ff exyen = ff_div(acc_ff(cur[4]), ssf), pen = ff_div(acc_ff(cur[2]), ssf);
       float phis, sxye, exye, pe;
       if (antid) {
-        phis = N.f(V2C_NF_PHIS_IT)[m3] + (phin - N.f(V2C_NF_PHIE)[m3]);
-        sxye = N.f(V2C_NF_SXY)[m3] + (sxyen - N.f(V2C_NF_SXYEE)[m3]);
-        exye = N.f(V2C_NF_EXY)[m3] + (exyen - N.f(V2C_NF_EXYEE)[m3]);
-        pe = N.f(V2C_NF_PES)[m3] + (pen - N.f(V2C_NF_PEE)[m3]);
+        phis = antid_rn(phin, N.f(V2C_NF_PHIS_IT)[m3], N.f(V2C_NF_PHIE)[m3]);
+        sxye = antid_rn(sxyen, N.f(V2C_NF_SXY)[m3], N.f(V2C_NF_SXYEE)[m3]);
+        exye = antid_rn(exyen, N.f(V2C_NF_EXY)[m3], N.f(V2C_NF_EXYEE)[m3]);
+        pe = antid_rn(pen, N.f(V2C_NF_PES)[m3], N.f(V2C_NF_PEE)[m3]);
       } else {
-        phis = phin; sxye = sxyen; exye = exyen; pe = pen;
+        phis = ff_round(phin); sxye = ff_round(sxyen); exye = ff_round(exyen); pe = ff_round(pen);
       }
       if (pe < 0.f) pe = 0.f;
-      float nu_m2c = __fdividef(cur[0].value(), ss);
-      N.f(V2C_NF_PHIN)[m3] = phin;
-      N.f(V2C_NF_SXYEN)[m3] = sxyen;
-      N.f(V2C_NF_EXYEN)[m3] = exyen;
-      N.f(V2C_NF_PEN)[m3] = pen;
+      N.f(V2C_NF_PHIN)[m3] = ff_round(phin);
+      N.f(V2C_NF_SXYEN)[m3] = ff_round(sxyen);
+      N.f(V2C_NF_EXYEN)[m3] = ff_round(exyen);
+      N.f(V2C_NF_PEN)[m3] = ff_round(pen);
       N.f(V2C_NF_PHIS)[m3] = phis;
       N.f(V2C_NF_SXYE)[m3] = sxye;
       N.f(V2C_NF_EXYE)[m3] = exye;
       N.f(V2C_NF_PE)[m3] = pe;
-      N.f(V2C_NF_COHESION)[m3] = __fdividef(cur[5].value(), ss);
-      N.f(V2C_NF_NU_M2C)[m3] = nu_m2c;
-      N.f(V2C_NF_GG)[m3] = __fdividef(nu_m2c, __fdividef(cur[1].value(), ss));
+      N.f(V2C_NF_COHESION)[m3] = ratio(cur[5], ssf);
+      N.f(V2C_NF_NU_M2C)[m3] = ratio(cur[0], ssf);
+      // nu_m2c / (sum nu/G w / sum w) = sum nu w / sum nu/G w
+      N.f(V2C_NF_GG)[m3] = ratio(cur[0], acc_ff(cur[1]));
     } else {
       N.f(V2C_NF_PHIN)[m3] = 0; N.f(V2C_NF_SXYEN)[m3] = 0; N.f(V2C_NF_EXYEN)[m3] = 0;
       N.f(V2C_NF_PHIS)[m3] = 0; N.f(V2C_NF_SXYE)[m3] = 0; N.f(V2C_NF_EXYE)[m3] = 0;
       N.f(V2C_NF_COHESION)[m3] = 0; N.f(V2C_NF_GG)[m3] = 0;
     }
   } else if (role == 1) {
-    const float ss = cur[6].value();
+    const ff ssf = acc_ff(cur[6]);
+    const float ss = ff_round(ssf);
     const bool interior = ci >= 1 && j >= 1 && ci < g.xn - 1 && j < g.yn - 1;
     float mu = 0.f, fa = 0.f, fb = 0.f, fL = 0.f, fV0 = 0.f;
     if (ss != 0.f && interior) node_friction(a, ci, j, mu, fa, fb, fL, fV0);
     N.f(V2C_NF_MUS_S)[m3] = mu; N.f(V2C_NF_AS)[m3] = fa; N.f(V2C_NF_BS)[m3] = fb;
     N.f(V2C_NF_LS)[m3] = fL; N.f(V2C_NF_V0S)[m3] = fV0;
     if (ss != 0.f) {
-      N.f(V2C_NF_RO)[m3] = __fdividef(cur[0].value(), ss); N.f(V2C_NF_ET)[m3] = __fdividef(cur[1].value(), ss);
-      N.f(V2C_NF_HT)[m3] = __fdividef(cur[2].value(), ss); N.f(V2C_NF_CP)[m3] = __fdividef(cur[3].value(), ss);
-      N.f(V2C_NF_KT)[m3] = __fdividef(cur[4].value(), ss); N.f(V2C_NF_TK)[m3] = __fdividef(cur[5].value(), ss);
+      N.f(V2C_NF_RO)[m3] = ratio(cur[0], ssf); N.f(V2C_NF_ET)[m3] = ratio(cur[1], ssf);
+      N.f(V2C_NF_HT)[m3] = ratio(cur[2], ssf); N.f(V2C_NF_CP)[m3] = ratio(cur[3], ssf);
+      N.f(V2C_NF_KT)[m3] = ratio(cur[4], ssf); N.f(V2C_NF_TK)[m3] = ratio(cur[5], ssf);
     } else {
       N.f(V2C_NF_RO)[m3] = 0; N.f(V2C_NF_ET)[m3] = 0; N.f(V2C_NF_HT)[m3] = 0;
       N.f(V2C_NF_CP)[m3] = 0; N.f(V2C_NF_KT)[m3] = 0; N.f(V2C_NF_TK)[m3] = 0;
@@ -231,25 +253,25 @@ __device__ __forceinline__ void node_tail(const M2NArgs &a, int role, int ci, in
     // centre node (ci+1, j+1) from cell (ci, j)
     if (ci < g.ncx && j < ncy) {
       const long mc = (long)(ci + 1) * g.yn + (j + 1);
-      const float s1 = cur[5].value();
+      const ff s1f = acc_ff(cur[5]);
+      const float s1 = ff_round(s1f);
       if (s1 != 0.f) {
-        float sxxen = __fdividef(cur[2].value(), s1), sppen = __fdividef(cur[4].value(), s1);
-        float exxen = __fdividef(cur[3].value(), s1);
+        const ff sxxen = ff_div(acc_ff(cur[2]), s1f), sppen = ff_div(acc_ff(cur[4]), s1f);
+        const ff exxen = ff_div(acc_ff(cur[3]), s1f);
         float sxxe, sppe, exxe;
         if (antid) {
-          sxxe = N.f(V2C_NF_SXX)[mc] + (sxxen - N.f(V2C_NF_SXXEE)[mc]);
-          sppe = N.f(V2C_NF_PR)[mc] + (sppen - N.f(V2C_NF_SPPEE)[mc]);
-          exxe = N.f(V2C_NF_EXX)[mc] + (exxen - N.f(V2C_NF_EXXEE)[mc]);
+          sxxe = antid_rn(sxxen, N.f(V2C_NF_SXX)[mc], N.f(V2C_NF_SXXEE)[mc]);
+          sppe = antid_rn(sppen, N.f(V2C_NF_PR)[mc], N.f(V2C_NF_SPPEE)[mc]);
+          exxe = antid_rn(exxen, N.f(V2C_NF_EXX)[mc], N.f(V2C_NF_EXXEE)[mc]);
         } else {
-          sxxe = sxxen; sppe = sppen; exxe = exxen;
+          sxxe = ff_round(sxxen); sppe = ff_round(sppen); exxe = ff_round(exxen);
         }
         if (a.S.sppe_nstress) sppe = a.S.nstress_f;
-        float nd = __fdividef(cur[0].value(), s1);
-        N.f(V2C_NF_SXXEN)[mc] = sxxen; N.f(V2C_NF_SPPEN)[mc] = sppen;
-        N.f(V2C_NF_EXXEN)[mc] = exxen; N.f(V2C_NF_SXXE)[mc] = sxxe;
+        N.f(V2C_NF_SXXEN)[mc] = ff_round(sxxen); N.f(V2C_NF_SPPEN)[mc] = ff_round(sppen);
+        N.f(V2C_NF_EXXEN)[mc] = ff_round(exxen); N.f(V2C_NF_SXXE)[mc] = sxxe;
         N.f(V2C_NF_SPPE)[mc] = sppe; N.f(V2C_NF_EXXE)[mc] = exxe;
-        N.f(V2C_NF_ND_M2C)[mc] = nd;
-        N.f(V2C_NF_GD)[mc] = nd / (__fdividef(cur[1].value(), s1));
+        N.f(V2C_NF_ND_M2C)[mc] = ratio(cur[0], s1f);
+        N.f(V2C_NF_GD)[mc] = ratio(cur[0], acc_ff(cur[1]));
         N.f(V2C_NF_BM)[mc] = 50e9f;
         N.f(V2C_NF_DRO)[mc] = 0; N.f(V2C_NF_DRP)[mc] = 0;
       } else {
@@ -267,27 +289,29 @@ __device__ __forceinline__ void node_tail(const M2NArgs &a, int role, int ci, in
       N.f(V2C_NF_DRO)[m3] = 0; N.f(V2C_NF_DRP)[m3] = 0;
     }
   } else {
-    const float wx = cur[2].value();
-    if (wx != 0.f) {
-      float mrx0 = cur[1].value();
-      float mvxn = cur[0].value() / mrx0;
-      N.f(V2C_NF_MVXN)[m3] = mvxn;
+    const ff wxf = acc_ff(cur[2]);
+    if (ff_round(wxf) != 0.f) {
+      const ff mrx0 = acc_ff(cur[1]);
+      const ff mvxn = ff_div(acc_ff(cur[0]), mrx0);
+      N.f(V2C_NF_MVXN)[m3] = ff_round(mvxn);
       // the boundary correction (vxvy_boundarycorrection) leaves the vx
       // ghost row at zero; only the 13-node stencil gives it weight
       N.f(V2C_NF_MVX)[m3] = j == g.yn - 1 ? 0.f
-                            : antid ? N.f(V2C_NF_VX)[m3] + (mvxn - N.f(V2C_NF_MVXE)[m3]) : mvxn;
-      N.f(V2C_NF_MRX)[m3] = mrx0 / wx;
+                            : antid ? antid_rn(mvxn, N.f(V2C_NF_VX)[m3], N.f(V2C_NF_MVXE)[m3])
+                                    : ff_round(mvxn);
+      N.f(V2C_NF_MRX)[m3] = ff_round(ff_div(mrx0, wxf));
     } else {
       N.f(V2C_NF_MVX)[m3] = 0; N.f(V2C_NF_MRX)[m3] = 0;
     }
-    const float wy = vy3[2].value();
-    if (wy != 0.f) {
-      float mry0 = vy3[1].value();
-      float mvyn = vy3[0].value() / mry0;
-      N.f(V2C_NF_MVYN)[m3] = mvyn;
+    const ff wyf = acc_ff(vy3[2]);
+    if (ff_round(wyf) != 0.f) {
+      const ff mry0 = acc_ff(vy3[1]);
+      const ff mvyn = ff_div(acc_ff(vy3[0]), mry0);
+      N.f(V2C_NF_MVYN)[m3] = ff_round(mvyn);
       N.f(V2C_NF_MVY)[m3] = ci == g.xn - 1 ? 0.f  // the vy ghost column, likewise
-                            : antid ? N.f(V2C_NF_VY)[m3] + (mvyn - N.f(V2C_NF_MVYE)[m3]) : mvyn;
-      N.f(V2C_NF_MRY)[m3] = mry0 / wy;
+                            : antid ? antid_rn(mvyn, N.f(V2C_NF_VY)[m3], N.f(V2C_NF_MVYE)[m3])
+                                    : ff_round(mvyn);
+      N.f(V2C_NF_MRY)[m3] = ff_round(ff_div(mry0, wyf));
     } else {
       N.f(V2C_NF_MVY)[m3] = 0; N.f(V2C_NF_MRY)[m3] = 0;
     }
@@ -387,7 +411,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_m2n(M2NArgs a) {
           // the whole cell (ci, j) to its centre node
           CLASS_RUN(qu.x, up_e) {
             const float u = sm.p[P_U][q], v = sm.p[P_V][q];
-            const float w = s1up * (1.f - 2.f * fabsf(u - 0.5f)) * (1.f - 2.f * fabsf(v - 0.5f));
+            const float w = s1up * tent(u) * tent(v);
             cur[0].add(sm.p[P_NU][q] * w); cur[1].add(sm.p[P_NUG][q] * w);
             cur[2].add(sm.p[P_SXX][q] * w); cur[3].add(sm.p[P_EXX][q] * w);
             cur[4].add(sm.p[P_P][q] * w); cur[5].add(w);

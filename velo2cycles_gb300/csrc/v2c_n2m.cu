@@ -191,7 +191,52 @@ __device__ __forceinline__ void vel_at(const Grid &g, const float4 *Q, Pos p, fl
     A[4].add(w);                                                        \
   } while (0)
 
-template <bool BS>
+// Marker values without antidiffusion (interpolation.c:985-1011), in a
+// kernel instance of their own (PLAIN) so that the common antidiffusion
+// path keeps its registers: the previous node fields interpolated (change = false: a marker's first
+// values), or the change of the node fields since then (change = true),
+// interpolated as one field of node differences -- the same bilinear form,
+// so the same value in exact arithmetic, but the FP32 node differences of
+// two states that agree in their leading digits are exact where the
+// separate interpolations would each round at the size of the field.
+struct Plain {
+  float phi, exx, exy, sxx, sxy, p, vx, vy, e;
+};
+__device__ __forceinline__ void plain_values(const Grid &g, const Nodes &N, Axis ax, Axis ay,
+                                                 float uc, float vc, bool change, Plain &o) {
+  const long yn = g.yn;
+  float e, n;
+  long m3 = stencil_basic(g, ax, ay, e, n);
+  if (change) {
+    o.exy = bil_diff(N.f(V2C_NF_EXY), N.f(V2C_NF_EXYE), m3, yn, e, n);
+    o.sxy = bil_diff(N.f(V2C_NF_SXY), N.f(V2C_NF_SXYE), m3, yn, e, n);
+    o.e = bil_diff(N.f(V2C_NF_PES), N.f(V2C_NF_PE), m3, yn, e, n);
+    o.phi = bil_diff(N.f(V2C_NF_PHIS_IT), N.f(V2C_NF_PHIS), m3, yn, e, n);
+  } else {
+    o.exy = bil(N.f(V2C_NF_EXYE), m3, yn, e, n);
+    o.sxy = bil(N.f(V2C_NF_SXYE), m3, yn, e, n);
+    o.e = bil(N.f(V2C_NF_PE), m3, yn, e, n);
+    o.phi = bil(N.f(V2C_NF_PHIS), m3, yn, e, n);
+  }
+  m3 = stencil_centre(g, ax, ay, uc > 0.5f, vc > 0.5f, e, n);
+  if (change) {
+    o.exx = bil_diff(N.f(V2C_NF_EXX), N.f(V2C_NF_EXXE), m3, yn, e, n);
+    o.sxx = bil_diff(N.f(V2C_NF_SXX), N.f(V2C_NF_SXXE), m3, yn, e, n);
+    o.p = bil_diff(N.f(V2C_NF_PR), N.f(V2C_NF_SPPE), m3, yn, e, n);
+  } else {
+    o.exx = bil(N.f(V2C_NF_EXXE), m3, yn, e, n);
+    o.sxx = bil(N.f(V2C_NF_SXXE), m3, yn, e, n);
+    o.p = bil(N.f(V2C_NF_SPPE), m3, yn, e, n);
+  }
+  m3 = stencil_vx(g, ax, ay, vc < 0.5f, g.xn - 2, e, n);
+  o.vx = change ? bil_diff(N.f(V2C_NF_VX), N.f(V2C_NF_MVX), m3, yn, e, n)
+                : bil(N.f(V2C_NF_MVX), m3, yn, e, n);
+  m3 = stencil_vy(g, ax, ay, uc < 0.5f, g.yn - 2, e, n);
+  o.vy = change ? bil_diff(N.f(V2C_NF_VY), N.f(V2C_NF_MVY), m3, yn, e, n)
+                : bil(N.f(V2C_NF_MVY), m3, yn, e, n);
+}
+
+template <bool BS, bool PLAIN>
 __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
   __shared__ Smem sm;
   const Grid &g = a.g;
@@ -204,7 +249,7 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
   const int ci_end = min(i0 + a.TX, g.xn);
   const v2c_params &P = a.S.p;
   // interpolationmod 1 back-scatters through a.bs and the gather kernels
-  const int backscatter = a.do_n2m && P.antidiffinter == 1 && !BS;
+  const int backscatter = a.do_n2m && !PLAIN && !BS;
   const long yn = g.yn;
 
   // role 0: PHIS, SXY, EXY, ES, w (basic)   role 1: PR, SXX, EXX, w (centre)
@@ -253,29 +298,14 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
           const float SXY = bil(N.f(V2C_NF_SXY), mb, yn, eb, nb);
           const float ES = bil(N.f(V2C_NF_PES), mb, yn, eb, nb);
           const float PHIS = bil(N.f(V2C_NF_PHIS_IT), mb, yn, eb, nb);
-          float EXYE = 0.f, SXYE = 0.f, ESE = 0.f, PHISE = 0.f;
-          if (owned && P.antidiffinter != 1) {
-            EXYE = bil(N.f(V2C_NF_EXYE), mb, yn, eb, nb);
-            SXYE = bil(N.f(V2C_NF_SXYE), mb, yn, eb, nb);
-            ESE = bil(N.f(V2C_NF_PE), mb, yn, eb, nb);
-            PHISE = bil(N.f(V2C_NF_PHIS), mb, yn, eb, nb);
-          }
           const long mc = stencil_centre(g, ax, ay, uc > 0.5f, vc > 0.5f, ec, ncc);
           const float EXX = bil(N.f(V2C_NF_EXX), mc, yn, ec, ncc);
           const float SXX = bil(N.f(V2C_NF_SXX), mc, yn, ec, ncc);
           const float PR = bil(N.f(V2C_NF_PR), mc, yn, ec, ncc);
-          float EXXE = 0.f, SXXE = 0.f, SPPE = 0.f;
-          if (owned && P.antidiffinter != 1) {
-            EXXE = bil(N.f(V2C_NF_EXXE), mc, yn, ec, ncc);
-            SXXE = bil(N.f(V2C_NF_SXXE), mc, yn, ec, ncc);
-            SPPE = bil(N.f(V2C_NF_SPPE), mc, yn, ec, ncc);
-          }
           long m3 = stencil_vx(g, ax, ay, vc < 0.5f, g.xn - 2, e, n);
           const float VX = bil(N.f(V2C_NF_VX), m3, yn, e, n);
-          const float MVX = (owned && P.antidiffinter != 1) ? bil(N.f(V2C_NF_MVX), m3, yn, e, n) : 0.f;
           m3 = stencil_vy(g, ax, ay, uc < 0.5f, g.yn - 2, e, n);
           const float VY = bil(N.f(V2C_NF_VY), m3, yn, e, n);
-          const float MVY = (owned && P.antidiffinter != 1) ? bil(N.f(V2C_NF_MVY), m3, yn, e, n) : 0.f;
           if (backscatter) {
             sm.q[Q_U][k] = uc; sm.q[Q_V][k] = vc;
             sm.q[Q_PHIS][k] = PHIS; sm.q[Q_SXY][k] = SXY; sm.q[Q_EXY][k] = EXY;
@@ -304,12 +334,14 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
           bool changed = false, tk_set = false;
           if (a.do_n2m) {
             if (in_strict && t < 50 && tk <= 0.f) {
-              if (P.antidiffinter == 1) {
+              if (!PLAIN) {
                 msxx = SXX; msxy = SXY; mp = PR; mexx = EXX; mexy = EXY;
                 mvx = VX; mvy = VY; phi = PHIS; me = ES;
               } else {
-                msxx = SXXE; msxy = SXYE; mp = SPPE; mexx = EXXE; mexy = EXYE;
-                mvx = MVX; mvy = MVY; phi = PHISE; me = ESE;
+                Plain o;
+                plain_values(g, N, ax, ay, uc, vc, false, o);
+                msxx = o.sxx; msxy = o.sxy; mp = o.p; mexx = o.exx; mexy = o.exy;
+                mvx = o.vx; mvy = o.vy; phi = o.phi; me = o.e;
               }
               if (!P.tempmod) {
                 tk = a.S.eps2_f;
@@ -318,13 +350,15 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
               changed = true;
             }
             if (in_grid && t < 50 && tk > 0.f) {
-              if (P.antidiffinter == 1) {
+              if (!PLAIN) {
                 phi = PHIS; mexx = EXX; mexy = EXY; msxx = SXX; msxy = SXY;
                 mp = PR; mvx = VX; mvy = VY; me = ES;
               } else {
-                phi += (PHIS - PHISE); mexx += (EXX - EXXE); mexy += (EXY - EXYE);
-                msxx += (SXX - SXXE); msxy += (SXY - SXYE); mp += (PR - SPPE);
-                mvx += (VX - MVX); mvy += (VY - MVY); me += (ES - ESE);
+                Plain o;
+                plain_values(g, N, ax, ay, uc, vc, true, o);
+                phi += o.phi; mexx += o.exx; mexy += o.exy;
+                msxx += o.sxx; msxy += o.sxy; mp += o.p;
+                mvx += o.vx; mvy += o.vy; me += o.e;
               }
               changed = true;
             }
@@ -390,7 +424,7 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
         } else if (role == 1) {
           CLASS_RUN(qu.x, up_e) {  // the whole cell (ci, j) to its centre node
             const float u = sm.q[Q_U][q], v = sm.q[Q_V][q];
-            const float w = s1up * (1.f - 2.f * fabsf(u - 0.5f)) * (1.f - 2.f * fabsf(v - 0.5f));
+            const float w = s1up * tent(u) * tent(v);
             cur[0].add(sm.q[Q_PR][q] * w); cur[1].add(sm.q[Q_SXX][q] * w);
             cur[2].add(sm.q[Q_EXX][q] * w); cur[3].add(w);
           }
@@ -735,9 +769,11 @@ __global__ void __launch_bounds__(256) k_move(N2MArgs a) {
 void launch_n2m(const N2MArgs &a, cudaStream_t st) {
   dim3 grid((a.g.xn + a.TX - 1) / a.TX, (a.g.yn + TY - 1) / TY);
   if (!a.bs) {
-    k_n2m<false><<<grid, NTH, 0, st>>>(a);
+    // PLAIN: the markers take the node fields without antidiffusion
+    if (a.S.p.antidiffinter == 1) k_n2m<false, false><<<grid, NTH, 0, st>>>(a);
+    else k_n2m<false, true><<<grid, NTH, 0, st>>>(a);
   } else {
-    k_n2m<true><<<grid, NTH, 0, st>>>(a);
+    k_n2m<true, false><<<grid, NTH, 0, st>>>(a);
     const unsigned nb = (unsigned)((a.g.nn + 127) / 128);
     k_n2m_bs_mode1<0><<<nb, 128, 0, st>>>(a);
     k_n2m_bs_mode1<1><<<nb, 128, 0, st>>>(a);

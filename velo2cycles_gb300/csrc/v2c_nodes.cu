@@ -27,18 +27,6 @@ namespace {
 
 inline unsigned nblk(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
-// asinh(exp(w)) without forming exp(w)
-__device__ __forceinline__ float asinh_exp(float w) {
-  if (w > 20.f) return w + 0.693147180559945f + 0.25f * __expf(-2.f * w);
-  return asinhf(expf(w));
-}
-
-// log(sinh(s)), s > 0
-__device__ __forceinline__ float log_sinh(float s) {
-  if (s > 10.f) return s - 0.693147180559945f + log1pf(-expf(-2.f * s));
-  return logf(sinhf(s));
-}
-
 // Float-float forms of the exponents of the slip-rate law.  Its exponent
 // sums terms of a few hundred that cancel (ln V, (mu + b phi)/a, ln sinh of
 // tau/(a sigma)), and the slip rate is e^exponent: in FP32 the sum's
@@ -58,24 +46,59 @@ __device__ __forceinline__ ff ff_log_sinh(ff x) {
 // e^E for a float pair E (the low word as a first-order factor)
 __device__ __forceinline__ float exp_ff(ff E) { return expf(E.hi) * (1.f + E.lo); }
 
-// asinh(e^w) for a float-pair w (calc_RSF.c:128), to FP32 precision
-__device__ __forceinline__ float asinh_exp_ff(ff w) {
-  if (w.hi > 9.f) return (w.hi + 0.693147180559945f) + (w.lo + 0.25f * __expf(-2.f * w.hi));
-  return asinhf(exp_ff(w));
+// A node value formed in float-float and rounded once to FP32: the node
+// kernels of a Picard pass feed each other through FP32 node fields, and the
+// slip rate magnifies a one-ulp difference of its inputs a hundredfold
+// (tau/(a sigma) ~ 100 in the exponent), so each field is rounded from a
+// value ~2^-48 accurate rather than from a chain of FP32 roundings.
+__device__ __forceinline__ float rn(ff a) { return __fadd_rn(a.hi, a.lo); }
+__device__ __forceinline__ ff ff_quarter_sum(float a, float b, float c, float d) {
+  ff s = ff_add_f(ff_f(a), b);
+  s = ff_add_f(s, c);
+  return ff_scale(ff_add_f(s, d), 0.25f);
+}
+// a / b, the IEEE FP32 quotient where b is 0 or a non-finite (the reference's
+// inf and NaN), else the float-float quotient
+__device__ __forceinline__ ff ff_div_ieee(ff a, ff b) {
+  if (b.hi == 0.f || !isfinite(b.hi) || !isfinite(a.hi)) return ff_f(a.hi / b.hi);
+  return ff_div(a, b);
 }
 
-// ageing-law state after dt at slip rate V (calc_RSF.c:96-103)
-__device__ __forceinline__ float new_state(float ph, float V, float dt, float L, float V0) {
-  const float x = V * dt / L;
-  if (x <= 1e-6f) {
-    // log(e^ph (1 - x) + V0 dt / L)
-    return ph + log1pf(-x + V0 * dt / L * expf(-ph));
+// asinh(e^w) as a float pair (calc_RSF.c:128): w + ln 2 + e^-2w / 4 above
+// w = 9 (the next term is below 1e-16 of the result), the series
+// x - x^3/6 + 3 x^5/40 for x = e^w below 1e-3, else ln(x + sqrt(x^2 + 1))
+__device__ __forceinline__ ff ff_asinh_exp(ff w) {
+  if (w.hi > 9.f) return ff_add_f(ff_add(w, ff_ln2()), 0.25f * __expf(-2.f * w.hi));
+  const ff x = ff_exp(w);
+  if (x.hi < 1e-3f) {
+    const float x2 = x.hi * x.hi;
+    return ff_mul_f(x, 1.f - x2 * (1.f / 6.f - x2 * 0.075f));
   }
-  // log(V0/V + (e^ph - V0/V) e^-x) = log(A + B), A = V0/V (1 - e^-x), B = e^(ph-x)
-  const float la = logf(V0 / V) + logf(-expm1f(-x));
-  const float lb = ph - x;
-  const float hi = fmaxf(la, lb), lo = fminf(la, lb);
-  return hi + log1pf(expf(lo - hi));
+  return ff_log(ff_add(x, ff_sqrt(ff_add_f(ff_mul(x, x), 1.f))));
+}
+
+// ageing-law state after dt at slip rate V (calc_RSF.c:96-103), as a float
+// pair.  The state (~50 in the host rock) enters the slip rate as e^(b/a
+// phi) with b/a up to ~2, so its FP32 evaluation error (a few ulps from the
+// logarithms of V0/V and of 1 - e^-x, each of size ~20) would be several
+// 1e-6 of the slip rate: the logarithms and the sums run in float-float,
+// and only corrections far below an ulp of the state stay in FP32.
+// dt is a float pair (dt_hi, dt_lo).
+__device__ __forceinline__ ff new_state_ff(float ph, float V, ff dt, float L, float V0) {
+  const ff x = ff_div(ff_mul_f(dt, V), ff_f(L));  // V dt / L
+  // the reference's test V dt / L <= 1e-6, on the FP64 constant as a pair
+  const float c_hi = 9.99999997e-07f, c_lo = 2.52475725e-15f;
+  if (x.hi < c_hi || (x.hi == c_hi && x.lo <= c_lo)) {
+    // log(e^ph (1 - x) + V0 dt / L) = ph + log1p(-x + V0 dt / L e^-ph)
+    const float t = -x.hi + V0 * dt.hi / L * expf(-ph);
+    return ff_add_f(ff_f(ph), log1pf(t));
+  }
+  // log(A + B), A = V0/V (1 - e^-x), B = e^(ph - x)
+  const ff la = ff_add(ff_log(ff_div(ff_f(V0), ff_f(V))), ff_log(ff_f(-expm1f(-x.hi))));
+  const ff lb = ff_sub(ff_f(ph), x);
+  const bool a_big = la.hi > lb.hi || (la.hi == lb.hi && la.lo >= lb.lo);
+  const ff hi = a_big ? la : lb, lo = a_big ? lb : la;
+  return ff_add_f(hi, log1pf(expf(ff_sub(lo, hi).hi)));
 }
 
 // interpolate_center2basic (interpolation.c:1600-1637): means of the four
@@ -84,7 +107,7 @@ __device__ __forceinline__ float new_state(float ph, float V, float dt, float L,
 // marker reached has gd = 0 and gives inf as in the reference).  use_dsxx:
 // sxx - sxxe is taken from DSXX, which recompute_stress_strainrate wrote
 // for the current sxx and sxxe (the FP32 difference cancels at small dt)
-__global__ void k_c2b(Grid g, Nodes N, float dt, int use_dsxx) {
+__global__ void k_c2b(Grid g, Nodes N, float dt, float dt_lo, int use_dsxx) {
   long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (m3 >= g.nn) return;
   const long yn = g.yn;
@@ -93,21 +116,26 @@ __global__ void k_c2b(Grid g, Nodes N, float dt, int use_dsxx) {
   const float *exx = N.f(V2C_NF_EXX), *sxx = N.f(V2C_NF_SXX), *sxxe = N.f(V2C_NF_SXXE);
   const float *gd = N.f(V2C_NF_GD), *nd = N.f(V2C_NF_ND_M2C), *pr = N.f(V2C_NF_PR);
   const float *dsxx = N.f(V2C_NF_DSXX);
-  float se = 0.f, ss = 0.f, sp = 0.f, spl = 0.f, sel = 0.f;
+  const ff dt_ff{dt, dt_lo};
+  ff spl = ff_f(0.f), sel = ff_f(0.f);
   const long k[4] = {m3, m3 + 1, m3 + yn, m3 + yn + 1};
 #pragma unroll
   for (int q = 0; q < 4; q++) {
     const long i = k[q];
     const float e = exx[i], s = sxx[i], s0 = sxxe[i], G = gd[i];
-    se += e; ss += s; sp += pr[i];
-    spl += e - (use_dsxx ? dsxx[i] : s - s0) / (2.f * G * dt) - s / (2.f * nd[i]);
-    sel += 2.f * G * dt * e + s0;
+    ff ds;
+    if (use_dsxx) ds = ff_f(dsxx[i]);
+    else ds.hi = two_sum(s, -s0, ds.lo);
+    const ff gdt2 = ff_mul(ff_f(2.f * G), dt_ff);  // 2 G dt
+    spl = ff_add(spl, ff_sub(ff_sub(ff_f(e), ff_div_ieee(ds, gdt2)),
+                             ff_div_ieee(ff_f(s), ff_f(2.f * nd[i]))));
+    sel = ff_add(sel, ff_add_f(ff_mul_f(gdt2, e), s0));
   }
-  N.f(V2C_NF_EXXS)[m3] = 0.25f * se;
-  N.f(V2C_NF_EXXPL)[m3] = 0.25f * spl;
-  N.f(V2C_NF_SXXS)[m3] = 0.25f * ss;
-  N.f(V2C_NF_PRS)[m3] = 0.25f * sp;
-  N.f(V2C_NF_EXXEL)[m3] = 0.25f * sel;
+  N.f(V2C_NF_EXXS)[m3] = rn(ff_quarter_sum(exx[k[0]], exx[k[1]], exx[k[2]], exx[k[3]]));
+  N.f(V2C_NF_EXXPL)[m3] = rn(ff_scale(spl, 0.25f));
+  N.f(V2C_NF_SXXS)[m3] = rn(ff_quarter_sum(sxx[k[0]], sxx[k[1]], sxx[k[2]], sxx[k[3]]));
+  N.f(V2C_NF_PRS)[m3] = rn(ff_quarter_sum(pr[k[0]], pr[k[1]], pr[k[2]], pr[k[3]]));
+  N.f(V2C_NF_EXXEL)[m3] = rn(ff_scale(sel, 0.25f));
 }
 
 // bilinear weight of the centre between lines m1-1 and m1 against the
@@ -142,25 +170,38 @@ __global__ void k_b2c(Grid g, Nodes N, unsigned long long *stat) {
   const float dm0 = (1.f - e) * (1.f - n), dm1 = (1.f - e) * n, dm2 = e * (1.f - n), dm3 = e * n;
   const float *nu = N.f(V2C_NF_NU);
   const long m4 = (long)m10 * yn + m20;
-  const float nd = 1.f / (dm0 / nu[m4] + dm1 / nu[m4 + 1] + dm2 / nu[m4 + yn] + dm3 / nu[m4 + yn + 1]);
+  const float n0 = nu[m4], n1 = nu[m4 + 1], n2 = nu[m4 + yn], n3 = nu[m4 + yn + 1];
+  float nd;
+  if (n0 > 0.f && n1 > 0.f && n2 > 0.f && n3 > 0.f && isfinite(n0 + n1 + n2 + n3)) {
+    // the harmonic mean in float-float, rounded once
+    ff h = ff_div(ff_f(dm0), ff_f(n0));
+    h = ff_add(h, ff_div(ff_f(dm1), ff_f(n1)));
+    h = ff_add(h, ff_div(ff_f(dm2), ff_f(n2)));
+    h = ff_add(h, ff_div(ff_f(dm3), ff_f(n3)));
+    nd = rn(ff_div_ieee(ff_f(1.f), h));
+  } else {  // a zero or non-finite viscosity: the reference's IEEE result
+    nd = 1.f / (dm0 / n0 + dm1 / n1 + dm2 / n2 + dm3 / n3);
+  }
   N.f(V2C_NF_ND)[m3] = nd;
   if (!(nd > 0.f)) atomicAdd(stat + ST_NAN, 1ull);  // the reference prints these
 }
 
-// nueffcalc (momentum_continuity_addmatrix_checkerror.c:380-393)
-__device__ __forceinline__ float nueff_of(float nvp, float ggeff, float dt, float nubeg, float &Z) {
-  Z = ggeff * dt / (ggeff * dt + nvp);
-  const float nueff = Z * nvp;
-  return nueff < nubeg ? nubeg : nueff;
+// nueffcalc (momentum_continuity_addmatrix_checkerror.c:380-393) in
+// float-float: Z = G dt / (G dt + nvp), nueff = Z nvp (lower limit nubeg)
+__device__ __forceinline__ ff nueff_ff(float nvp, float ggeff, ff dt, float nubeg, ff &Z) {
+  const ff gdt = ff_mul_f(dt, ggeff);
+  Z = ff_div_ieee(gdt, ff_add_f(gdt, nvp));
+  const ff nueff = ff_mul_f(Z, nvp);
+  return rn(nueff) < nubeg ? ff_f(nubeg) : nueff;
 }
 
 // recompute_stress_strainrate (momentum_continuity_iterate.c:214-262) with
 // sxxcalc / sxycalc (momentum_continuity_addmatrix_checkerror.c:446-572):
 // strain rates from the node velocities, visco-elastic stresses from the
-// node viscosities and the previous elastic stresses.  Line spacings are
-// sums of the FP32 cell widths.
-__global__ void k_recompute(Grid g, Nodes N, float dt, float nubeg, const double *vx64,
-                            const double *vy64) {
+// node viscosities and the previous elastic stresses, in float-float from
+// the FP64 line spacings, each output rounded once.
+__global__ void k_recompute(Grid g, Nodes N, float dt, float dt_lo, float nubeg,
+                            const double *vx64, const double *vy64) {
   long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (m3 >= g.nn) return;
   const long yn = g.yn;
@@ -168,31 +209,43 @@ __global__ void k_recompute(Grid g, Nodes N, float dt, float nubeg, const double
   if (!(m1 >= 1 && m2 >= 1)) return;
   const long v0 = m3 - yn - 1, v1 = v0 + 1, v2 = v0 + yn;
   const float *vx = N.f(V2C_NF_VX), *vy = N.f(V2C_NF_VY);
-  float Z;
-  float nueff = nueff_of(N.f(V2C_NF_ND)[m3], N.f(V2C_NF_GD)[m3], dt, nubeg, Z);
+  const ff dt_ff{dt, dt_lo};
+  ff Z;
+  ff nueff = nueff_ff(N.f(V2C_NF_ND)[m3], N.f(V2C_NF_GD)[m3], dt_ff, nubeg, Z);
   // velocity differences from the FP64 copy where there is one: adjacent
   // velocities agree in their leading digits, which FP32 storage would keep
   // and the differences would lose
   auto dvx = [&](long a, long b) {
-    return vx64 ? (float)(__ldg(vx64 + a) - __ldg(vx64 + b)) : vx[a] - vx[b];
+    if (vx64) return ff_from_double(__ldg(vx64 + a) - __ldg(vx64 + b));
+    ff d;
+    d.hi = two_sum(vx[a], -vx[b], d.lo);
+    return d;
   };
   auto dvy = [&](long a, long b) {
-    return vy64 ? (float)(__ldg(vy64 + a) - __ldg(vy64 + b)) : vy[a] - vy[b];
+    if (vy64) return ff_from_double(__ldg(vy64 + a) - __ldg(vy64 + b));
+    ff d;
+    d.hi = two_sum(vy[a], -vy[b], d.lo);
+    return d;
   };
-  const float edotxx = 0.5f * (dvx(v2, v0) / __ldg(g.wx + m1 - 1) - dvy(v1, v0) / __ldg(g.wy + m2 - 1));
+  auto span = [](const double *gl, int i, int j) { return ff_from_double(gl[i] - gl[j]); };
+  const ff edotxx = ff_scale(ff_sub(ff_div(dvx(v2, v0), span(g.gx, m1, m1 - 1)),
+                                    ff_div(dvy(v1, v0), span(g.gy, m2, m2 - 1))), 0.5f);
   const float s0 = N.f(V2C_NF_SXXE)[m3];
-  N.f(V2C_NF_EXX)[m3] = edotxx;
-  N.f(V2C_NF_SXX)[m3] = 2.f * nueff * edotxx + s0 * (1.f - Z);
+  const ff two_nu_e = ff_scale(ff_mul(nueff, edotxx), 2.f);
+  N.f(V2C_NF_EXX)[m3] = rn(edotxx);
+  N.f(V2C_NF_SXX)[m3] = rn(ff_add(two_nu_e, ff_mul_f(ff_add_f(ff_neg(Z), 1.f), s0)));
   // the increment itself: at a coseismic dt sxx and sxxe agree to a few
   // FP32 ulps and their difference would be rounding
-  N.f(V2C_NF_DSXX)[m3] = 2.f * nueff * edotxx - Z * s0;
+  N.f(V2C_NF_DSXX)[m3] = rn(ff_sub(two_nu_e, ff_mul_f(Z, s0)));
   if (m1 < g.xn - 1 && m2 < g.yn - 1) {
-    nueff = nueff_of(N.f(V2C_NF_NU)[m3], N.f(V2C_NF_GG)[m3], dt, nubeg, Z);
-    const float exy1 = dvx(m3, v2) / (__ldg(g.wy + m2 - 1) + __ldg(g.wy + m2));
-    const float exy2 = dvy(m3, v1) / (__ldg(g.wx + m1 - 1) + __ldg(g.wx + m1));
-    N.f(V2C_NF_EXY)[m3] = exy1 + exy2;
-    N.f(V2C_NF_ESP)[m3] = exy1 - exy2;
-    N.f(V2C_NF_SXY)[m3] = 2.f * nueff * (exy1 + exy2) + N.f(V2C_NF_SXYE)[m3] * (1.f - Z);
+    nueff = nueff_ff(N.f(V2C_NF_NU)[m3], N.f(V2C_NF_GG)[m3], dt_ff, nubeg, Z);
+    const ff exy1 = ff_div(dvx(m3, v2), span(g.gy, m2 + 1, m2 - 1));
+    const ff exy2 = ff_div(dvy(m3, v1), span(g.gx, m1 + 1, m1 - 1));
+    const ff exy = ff_add(exy1, exy2);
+    N.f(V2C_NF_EXY)[m3] = rn(exy);
+    N.f(V2C_NF_ESP)[m3] = rn(ff_sub(exy1, exy2));
+    N.f(V2C_NF_SXY)[m3] = rn(ff_add(ff_scale(ff_mul(nueff, exy), 2.f),
+                                    ff_mul_f(ff_add_f(ff_neg(Z), 1.f), N.f(V2C_NF_SXYE)[m3])));
   }
 }
 
@@ -232,22 +285,23 @@ __global__ void k_c2b_old(Grid g, Nodes N) {
   long m2 = m3 % yn, m1 = m3 / yn;
   if (m1 >= 1 && m2 >= 1 && m1 < g.xn - 1 && m2 < g.yn - 1) {
     const float *exxe = N.f(V2C_NF_EXXE), *sxxe = N.f(V2C_NF_SXXE), *sppe = N.f(V2C_NF_SPPE);
-    N.f(V2C_NF_EXXES)[m3] = 0.25f * (exxe[m3] + exxe[m3 + 1] + exxe[m3 + yn] + exxe[m3 + yn + 1]);
-    N.f(V2C_NF_SXXES)[m3] = 0.25f * (sxxe[m3] + sxxe[m3 + 1] + sxxe[m3 + yn] + sxxe[m3 + yn + 1]);
-    N.f(V2C_NF_SPPES)[m3] = 0.25f * (sppe[m3] + sppe[m3 + 1] + sppe[m3 + yn] + sppe[m3 + yn + 1]);
+    N.f(V2C_NF_EXXES)[m3] = rn(ff_quarter_sum(exxe[m3], exxe[m3 + 1], exxe[m3 + yn], exxe[m3 + yn + 1]));
+    N.f(V2C_NF_SXXES)[m3] = rn(ff_quarter_sum(sxxe[m3], sxxe[m3 + 1], sxxe[m3 + yn], sxxe[m3 + yn + 1]));
+    N.f(V2C_NF_SPPES)[m3] = rn(ff_quarter_sum(sppe[m3], sppe[m3 + 1], sppe[m3 + yn], sppe[m3 + yn + 1]));
   }
 }
 
-__global__ void k_before(Grid g, Nodes N, Scal S, float dt, int rk, unsigned long long *stat) {
+__global__ void k_before(Grid g, Nodes N, Scal S, float dt, float dt_lo, int rk,
+                         unsigned long long *stat) {
   long m3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (m3 >= g.nn) return;
   const v2c_params &p = S.p;
   long m2 = m3 % g.yn, m1 = m3 / g.yn;
   if (!(m1 >= 1 && m2 >= 1 && m1 < g.xn - 1 && m2 < g.yn - 1)) return;
   const float W = (float)p.faultwidth;
+  const ff dt_ff{dt, dt_lo};
   const bool nP_const = p.pmode == 0 || p.timesum == 0;
   const ff nP_ff = nP_const ? ff{S.sn_hi, S.sn_lo} : ff_f(N.f(V2C_NF_SPPES)[m3]);
-  const float nP = nP_ff.hi;
   const float sxxs = N.f(V2C_NF_SXXS)[m3], sxy = N.f(V2C_NF_SXY)[m3];
   const float sigin = sqrtf(sxxs * sxxs + sxy * sxy);
   float nu;
@@ -260,28 +314,52 @@ __global__ void k_before(Grid g, Nodes N, Scal S, float dt, int rk, unsigned lon
     // rates and the rkmod 3 histories it also selects are never used)
     if ((p.rkmod == 0 && rk > 0) || (rk > 0 && rk < 3) || (rk == 3 && p.rkmod == 3))
       V = N.f(V2C_NF_RK_SLIPRS_SOLVED)[m3];
-    N.f(V2C_NF_PES)[m3] = N.f(V2C_NF_PE)[m3] + V / W * dt;
-    float newstate = 0.f, syield;
+    // V / W as a float pair (the plastic strain rate)
+    const ff VW = ff_div(ff_f(V), ff_f(W));
+    N.f(V2C_NF_PES)[m3] = rn(ff_add_f(ff_mul(VW, dt_ff), N.f(V2C_NF_PE)[m3]));
+    float newstate = 0.f;
+    ff sy;  // the yield strength, rounded once for storage
     if (p.RSFmode == 1) {
       const float L = N.f(V2C_NF_LS)[m3], V0 = N.f(V2C_NF_V0S)[m3], ph = N.f(V2C_NF_PHIS)[m3];
-      newstate = new_state(ph, V, dt, L, V0);
-      const float rad = (p.inertyn == 0) ? 4.3303e+06f * V : 0.f;
+      const ff ns = new_state_ff(ph, V, dt_ff, L, V0);
+      newstate = ns.hi;
+      // radiation damping 4.3303e6 V (an exact FP32 constant)
+      ff rad = ff_f(0.f);
+      if (p.inertyn == 0) rad.hi = two_prod(4.3303e+06f, V, rad.lo);
       const float a = N.f(V2C_NF_AS)[m3], b = N.f(V2C_NF_BS)[m3], mu = N.f(V2C_NF_MUS_S)[m3];
-      // exponents in float-float (see ff_log_sinh)
-      const ff lnVV0 = ff_log(ff_div(ff_f(V), ff_f(V0)));
-      if (p.power_law_RSF > 0)
-        syield = exp_ff(ff_add(ff_add(ff_log(ff_mul_f(nP_ff, mu)), ff_mul(ff_div(ff_f(a), ff_f(mu)), lnVV0)),
-                               ff_div(ff_mul_f(ff_f(newstate), b), ff_f(mu)))) + rad;
-      else
-        syield = nP * a * asinh_exp_ff(ff_add(ff_sub(lnVV0, ff_ln2()),
-                                              ff_div(ff_add_f(ff_mul_f(ff_f(newstate), b), mu), ff_f(a)))) + rad;
+      if (V == 0.f) {
+        // V/V0 e^... = 0: the yield strength is the damping term alone
+        sy = rad;
+      } else {
+        // exponents in float-float (see ff_log_sinh); asinh is odd, so a
+        // negative V (an error the flags below report) keeps its sign
+        const ff lnVV0 = ff_log(ff_div(ff_f(fabsf(V)), ff_f(V0)));
+        if (p.power_law_RSF > 0) {
+          sy = V > 0.f ? ff_add(ff_exp(ff_add(ff_add(ff_log(ff_mul_f(nP_ff, mu)),
+                                                     ff_mul(ff_div(ff_f(a), ff_f(mu)), lnVV0)),
+                                              ff_div(ff_mul_f(ns, b), ff_f(mu)))),
+                                rad)
+                       : ff_f(__int_as_float(0x7fc00000));
+        } else {
+          ff as = ff_mul(ff_mul_f(nP_ff, a),
+                         ff_asinh_exp(ff_add(ff_sub(lnVV0, ff_ln2()),
+                                             ff_div(ff_add_f(ff_mul_f(ns, b), mu), ff_f(a)))));
+          if (V < 0.f) as = ff_neg(as);
+          sy = ff_add(as, rad);
+        }
+      }
     } else {
-      syield = nP * N.f(V2C_NF_MUS_S)[m3] + N.f(V2C_NF_COHESION)[m3];
+      sy = ff_add_f(ff_mul_f(nP_ff, N.f(V2C_NF_MUS_S)[m3]), N.f(V2C_NF_COHESION)[m3]);
     }
+    const float syield = rn(sy);
     const float nm = N.f(V2C_NF_NU_M2C)[m3];
+    // nm syield / (2 nm V / W + syield)
+    auto vp_of = [&]() {
+      return rn(ff_div_ieee(ff_mul_f(sy, nm), ff_add(ff_mul_f(VW, 2.f * nm), sy)));
+    };
     float vp;
-    if (p.RSFmode == 1) vp = (syield > 0.f) ? nm * syield / (2.f * nm * V / W + syield) : nm;
-    else vp = nm * syield / (2.f * nm * V / W + syield);
+    if (p.RSFmode == 1) vp = (syield > 0.f) ? vp_of() : nm;
+    else vp = vp_of();
     N.f(V2C_NF_PHIS_IT)[m3] = newstate;
     N.f(V2C_NF_SYIELDS)[m3] = syield;
     N.f(V2C_NF_NUVP_IT)[m3] = vp;
@@ -312,9 +390,10 @@ __global__ void k_after(Grid g, Nodes N, Scal S, float dt, float *part) {
       const float W = (float)p.faultwidth;
       const bool nps_const = p.pmode == 0 || p.timesum == 0;
       const ff nps_ff = nps_const ? ff{S.sn_hi, S.sn_lo} : ff_f(N.f(V2C_NF_SPPES)[m3]);
-      const float nps = nps_ff.hi;
       const float sxxs = N.f(V2C_NF_SXXS)[m3], sxy = N.f(V2C_NF_SXY)[m3];
       const float sigin = sqrtf(sxxs * sxxs + sxy * sxy);
+      // the stress invariant as a float pair
+      const ff sig = ff_sqrt(ff_add(ff_mul(ff_f(sxxs), ff_f(sxxs)), ff_mul(ff_f(sxy), ff_f(sxy))));
       const float a = N.f(V2C_NF_AS)[m3], b = N.f(V2C_NF_BS)[m3], mu = N.f(V2C_NF_MUS_S)[m3];
       const float V0 = N.f(V2C_NF_V0S)[m3], L = N.f(V2C_NF_LS)[m3], ph = N.f(V2C_NF_PHIS_IT)[m3];
       float V;
@@ -322,17 +401,19 @@ __global__ void k_after(Grid g, Nodes N, Scal S, float dt, float *part) {
         if (sigin > 0.f) {
           // the slip rate's exponent in float-float from the FP32 node
           // values (see ff_log_sinh)
-          const ff sig = ff_sqrt(ff_add(ff_mul(ff_f(sxxs), ff_f(sxxs)), ff_mul(ff_f(sxy), ff_f(sxy))));
           const ff bpa = ff_div(ff_mul_f(ff_f(ph), b), ff_f(a));  // b phi / a
+          ff E;
           if (p.power_law_RSF > 0)
-            V = exp_ff(ff_sub(ff_add(ff_log(ff_f(V0)),
-                                     ff_mul(ff_div(ff_f(mu), ff_f(a)),
-                                            ff_log(ff_div(sig, ff_mul_f(nps_ff, mu))))),
-                              bpa));
+            E = ff_sub(ff_add(ff_log(ff_f(V0)),
+                              ff_mul(ff_div(ff_f(mu), ff_f(a)),
+                                     ff_log(ff_div(sig, ff_mul_f(nps_ff, mu))))),
+                       bpa);
           else
-            V = exp_ff(ff_sub(ff_add(ff_log(ff_f(2.f * V0)),
-                                     ff_log_sinh(ff_div(sig, ff_mul_f(nps_ff, a)))),
-                              ff_add(ff_div(ff_f(mu), ff_f(a)), bpa)));
+            E = ff_sub(ff_add(ff_log(ff_f(2.f * V0)), ff_log_sinh(ff_div(sig, ff_mul_f(nps_ff, a)))),
+                       ff_add(ff_div(ff_f(mu), ff_f(a)), bpa));
+          // e^E rounded once; below e^-80 (under the 1e-40 floor's FP32
+          // neighbourhood) the FP32 exponential and its subnormals
+          V = E.hi > -80.f ? rn(ff_exp(E)) : exp_ff(E);
           const float ex = N.f(V2C_NF_EXXPL)[m3], ey = N.f(V2C_NF_EXY)[m3];
           const float Vslip = sqrtf(ex * ex + ey * ey) * W;
           V = (V <= Vslip) ? V : Vslip;
@@ -354,7 +435,7 @@ __global__ void k_after(Grid g, Nodes N, Scal S, float dt, float *part) {
       }
       N.f(V2C_NF_RK_SLIPRS_SOLVED)[m3] = V;
       if (V > 0.f) {
-        const float d = N.f(V2C_NF_SYIELDS)[m3] - sigin;
+        const float d = rn(ff_sub(ff_f(N.f(V2C_NF_SYIELDS)[m3]), sig));
         N.f(V2C_NF_RK_DELTAS)[m3] = d;
         d2 = d * d;
         cnt = 1.f;
@@ -458,12 +539,14 @@ void launch_c2b_old(const Grid &g, const Nodes &N, cudaStream_t st) {
   k_c2b_old<<<nblk(g.nn, 256), 256, 0, st>>>(g, N);
 }
 
-void launch_c2b(const Grid &g, const Nodes &N, float dt, int use_dsxx, cudaStream_t st) {
-  k_c2b<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, dt, use_dsxx);
+void launch_c2b(const Grid &g, const Nodes &N, double dt, int use_dsxx, cudaStream_t st) {
+  const float hi = (float)dt, lo = (float)(dt - (double)hi);
+  k_c2b<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, hi, lo, use_dsxx);
 }
-void launch_recompute(const Grid &g, const Nodes &N, const Scal &S, float dt, const double *vx64,
+void launch_recompute(const Grid &g, const Nodes &N, const Scal &S, double dt, const double *vx64,
                       const double *vy64, cudaStream_t st) {
-  k_recompute<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, dt, S.nubeg_f, vx64, vy64);
+  const float hi = (float)dt, lo = (float)(dt - (double)hi);
+  k_recompute<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, hi, lo, S.nubeg_f, vx64, vy64);
 }
 void launch_copyarrays(const Grid &g, const Nodes &N, cudaStream_t st) {
   k_copyarrays<<<nblk(g.nn, 256), 256, 0, st>>>(g, N);
@@ -479,7 +562,8 @@ void launch_b2c(const Grid &g, const Nodes &N, unsigned long long *stat, cudaStr
 }
 void launch_before_solve(const Grid &g, const Nodes &N, const Scal &S, double dt, int rk,
                          unsigned long long *stat, cudaStream_t st) {
-  k_before<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, S, (float)dt, rk, stat);
+  const float hi = (float)dt, lo = (float)(dt - (double)hi);
+  k_before<<<nblk(g.nn, 256), 256, 0, st>>>(g, N, S, hi, lo, rk, stat);
 }
 
 void launch_after_solve(const Grid &g, const Nodes &N, const Scal &S, double dt, int rk,

@@ -140,14 +140,20 @@ __global__ void __launch_bounds__(PT, 5) k_phys(PhysArgs a) {
         const Axis ay = make_axis(g.wy, g.ncy, iy, v * __ldg(g.wy + iy));
         float e, nn;
         const long m3 = stencil_centre(g, ax, ay, u > 0.5f, v > 0.5f, e, nn);
-        const float mpb = 1e-5f * bil(a.N.f(V2C_NF_PR), m3, g.yn, e, nn);
+        // pressure in bar, 1e-5 P, as a float pair
+        const ff mpb_ff = ff_mul(bil_ff(a.N.f(V2C_NF_PR), m3, g.yn, e, nn),
+                                 ff{9.99999975e-06f, 2.52621247e-13f});
+        const float mpb = mpb_ff.hi;
         const float T = a.m.tk[i];
         float mro, mbb;
         density32(a.R, P.densimod, t, T, mpb, mro, mbb);
         const float mkt = conductivity32(a.R, t, T, mpb);
         const float sxx = a.m.sxx[i], sxy = a.m.sxy[i];
         sigin = sqrtf(sxx * sxx + sxy * sxy);
-        mnu = ductile_visc32(a.R, a.S, t, sigin, T, a.m.tk_lo[i], mpb);
+        float s2lo;
+        const float s2 = two_prod(sxx, sxx, s2lo);
+        const ff sig_ff = ff_sqrt(ff_add(ff{s2, s2lo}, ff_mul(ff_f(sxy), ff_f(sxy))));
+        mnu = ductile_visc32(a.R, a.S, t, sig_ff, T, a.m.tk_lo[i], mpb_ff);
         const float phi0 = a.m.phi[i];
         phi = marker_friction(a, ix, iy, u, v, ax.X, ay.X, t, phi0, fr);
         if (!collect) {

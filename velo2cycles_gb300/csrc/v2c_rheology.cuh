@@ -31,7 +31,11 @@ __device__ __forceinline__ float conductivity32(const Rock &R, int t, float T, f
 }
 
 // ductilevisc.  Returns NaN for a type that fits no branch (the reference
-// leaves its result undefined there).
+// leaves its result undefined there).  sigin (the stress invariant) and mpb
+// (pressure, bar) arrive as float pairs: the dislocation viscosity goes as
+// sigin^(1-n) and the Arrhenius factor as e^(V P/(R T)), with V P/(R T) up to
+// ~7 in the mantle, so their FP32 roundings alone would be a few 1e-7 of
+// the viscosity.
 //
 // Precision.  The viscosity is e^s0 times an O(1) ratio, with s0 = ln of
 // the diffusion-creep viscosity, up to ~60: an FP32 s0 alone (ulp 4e-6)
@@ -57,9 +61,10 @@ __device__ __forceinline__ float conductivity32(const Rock &R, int t, float T, f
 //        f2(d* + e) = R0 + e - (q B*)^em expm1(em log1p(e (1 + g)/B*)),
 //      every term of which FP32 holds to a few 1e-7 of e rather than of d,
 //      as it does the steps and the change that the stopping test reads.
-// The viscosity is e^s0 d/(1 + d) at the step the replay stops.
+// The viscosity is e^(s0 + ln(d/(1 + d))) at the step the replay stops, the
+// exponent and the exponential in float-float, rounded once to FP32.
 __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, int t,
-                                                float sigin, float T, float Tlo, float mpb) {
+                                                ff sig_ff, float T, float Tlo, ff mpb) {
   int kind = (int)R(RK_KIND, t);
   if (kind == VISC_STICKY) {
     float nu = R(RK_NU, t);
@@ -71,18 +76,17 @@ __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, in
 
   const float mm = R(RK_MM, t);
   // (E + PV)/(RT), density_ductilevisc_calc.c:116-120, capped at 150
-  const ff num = ff_add(ff{R(RK_DH, t), R(RK_DH_LO, t)},
-                        ff_mul_f(ff{R(RK_DV, t), R(RK_DV_LO, t)}, mpb));
+  const ff num = ff_add(ff{R(RK_DH, t), R(RK_DH_LO, t)}, ff_mul(ff{R(RK_DV, t), R(RK_DV_LO, t)}, mpb));
   const ff den = ff_mul(ff{T, Tlo}, ff{8.31400012969970703125f, -1.2969971407983394e-07f});
   ff le1 = den.hi != 0.f ? ff_div(num, den) : ff_f(num.hi / den.hi);
   if (le1.hi > 150.f || (le1.hi == 150.f && le1.lo > 0.f)) le1 = ff_f(150.f);
   // ln of the diffusion-creep viscosity 0.5 k1 e1, k1 = nu / ss^(mm-1)
   const ff s0 = ff_add(ff{R(RK_LNK, t), R(RK_LNK_LO, t)}, le1);
-  float lnr = 0.f;  // ln(eta / eta_diff); sigin == 0: eta = eta_diff
-  if (sigin > 0.f) {
+  ff lnr = ff_f(0.f);  // ln(eta / eta_diff); sigin == 0: eta = eta_diff
+  if (sig_ff.hi > 0.f) {
     const ff em_ff{R(RK_EM, t), R(RK_EM_LO, t)};
     const float em = em_ff.hi;
-    const ff q_ff = ff_div(ff{R(RK_SS, t), R(RK_SS_LO, t)}, ff_f(sigin));  // ss / sigin
+    const ff q_ff = ff_div(ff{R(RK_SS, t), R(RK_SS_LO, t)}, sig_ff);  // ss / sigin
     const float q = q_ff.hi;
     // G dt / eta_diff (0 without elasticity or time step)
     ff g_ff = ff_f(0.f);
@@ -156,18 +160,20 @@ __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, in
       e_prev = e_old;
       d_prev = d_old;
     }
-    // d/(1 + d) at the last step, d = d* + e as a float pair
-    float dlo;
-    const float dhi = two_sum(ds, e, dlo);
-    const float inv = __fdividef(1.f, dhi);
-    lnr = -log1pf(inv * (1.f - dlo * inv));
+    // ln(d/(1 + d)) at the last step, d = d* + e as a float pair
+    ff d_ff;
+    d_ff.hi = two_sum(ds, e, d_ff.lo);
+    lnr = ff_log(ff_div(d_ff, ff_add_f(d_ff, 1.f)));
   }
   // limits nubeg/nuend then the per-type limits, in that order
-  const ff lnv = ff_add_f(s0, lnr);
+  const ff lnv = ff_add(s0, lnr);
   float nu;
   if (lnv.hi < S.ln_nubeg) nu = S.nubeg_f;
   else if (lnv.hi > S.ln_nuend) nu = S.nuend_f;
-  else nu = expf(lnv.hi) * (1.f + lnv.lo);
+  else {
+    const ff v = ff_exp(lnv);
+    nu = __fadd_rn(v.hi, v.lo);
+  }
   if (nu < R(RK_N0, t)) nu = R(RK_N0, t);
   if (nu > R(RK_N1, t)) nu = R(RK_N1, t);
   return nu;
@@ -284,6 +290,31 @@ __device__ __forceinline__ float bil(const float *f, long m3, long yn, float e, 
   float d0 = (1.f - e) * (1.f - n), d1 = (1.f - e) * n, d2 = e * (1.f - n), d3 = e * n;
   return d0 * __ldg(f + m3) + d1 * __ldg(f + m3 + 1) + d2 * __ldg(f + m3 + yn) +
          d3 * __ldg(f + m3 + yn + 1);
+}
+
+// bilinear interpolation as a float pair: the first node's value plus the
+// FP32 change across the stencil (for a smooth field such as the pressure
+// the change is a small part of the value, so its rounding is too)
+__device__ __forceinline__ ff bil_ff(const float *f, long m3, long yn, float e, float n) {
+  const float f0 = __ldg(f + m3), f1 = __ldg(f + m3 + 1), f2 = __ldg(f + m3 + yn),
+              f3 = __ldg(f + m3 + yn + 1);
+  const float d10 = f1 - f0, d20 = f2 - f0, dd = (f3 - f2) - d10;
+  const float d = fmaf(e, fmaf(n, dd, d20), n * d10);
+  ff r;
+  r.hi = two_sum(f0, d, r.lo);
+  return r;
+}
+
+// bil(f) - bil(g) as one interpolation of the node differences (the same
+// bilinear form, so the same value in exact arithmetic): f and g are
+// consecutive states of one field that agree in their leading digits, and
+// their FP32 node differences are exact where they are within a factor 2
+__device__ __forceinline__ float bil_diff(const float *f, const float *g, long m3, long yn,
+                                          float e, float n) {
+  float d0 = (1.f - e) * (1.f - n), d1 = (1.f - e) * n, d2 = e * (1.f - n), d3 = e * n;
+  return d0 * (__ldg(f + m3) - __ldg(g + m3)) + d1 * (__ldg(f + m3 + 1) - __ldg(g + m3 + 1)) +
+         d2 * (__ldg(f + m3 + yn) - __ldg(g + m3 + yn)) +
+         d3 * (__ldg(f + m3 + yn + 1) - __ldg(g + m3 + yn + 1));
 }
 
 }  // namespace v2c

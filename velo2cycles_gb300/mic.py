@@ -123,6 +123,14 @@ class MarkerInCell:
         call("v2c_download_cells", self.h, c.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), self.n)
         return c
 
+    def download_marker_properties(self) -> tuple[np.ndarray, np.ndarray]:
+        """(viscosity, conductivity) of every marker as the last
+        marker2nodes evaluated them, in reference numbering (0 for markers
+        outside the model)."""
+        nu, kt = np.zeros(self.n), np.zeros(self.n)
+        call("v2c_download_marker_properties", self.h, _ptr(nu), _ptr(kt), self.n)
+        return nu, kt
+
     # -------------------------------------------------------------- nodes
     def upload_node(self, field: int, values: np.ndarray):
         a = np.ascontiguousarray(values, dtype=np.float64)
