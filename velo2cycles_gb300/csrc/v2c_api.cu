@@ -438,6 +438,7 @@ extern "C" int v2c_set_rock_table(v2c_ctx *ctx, const double *rt) {
     pair(RK_SS, RK_SS_LO, ss);
     pair(RK_EM, RK_EM_LO, mm != 0 ? (mm - 1.0) / mm : 0.0);
     pair(RK_MM1, RK_MM1_LO, mm - 1.0);
+    pair(RK_LNSS, RK_LNSS_LO, ss > 0 ? log(ss) : 0.0);
     int kind;
     // branch selection of ductilevisc (density_ductilevisc_calc.c:44-66)
     if (t == 1) kind = VISC_STICKY;

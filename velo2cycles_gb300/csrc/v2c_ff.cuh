@@ -108,6 +108,20 @@ __device__ __forceinline__ ff ff_div(ff a, ff b) {
   const float h = fast_two_sum(q1, q2, l);
   return ff_add_f(ff{h, l}, q3);
 }
+// a / b from the approximate reciprocal of b.hi and one correction: the
+// first quotient carries ~2 ulps, the remainder a - b q1 is formed exactly,
+// and its quotient (a term ~1e-7 of the result) may carry the same relative
+// error, so the pair is good to ~2^-44 -- for quotients rounded to FP32 at
+// the end, or used to that accuracy.  b.hi a normal, finite nonzero float.
+__device__ __forceinline__ ff ff_div_fast(ff a, ff b) {
+  const float rb = __fdividef(1.f, b.hi);
+  const float q1 = __fmul_rn(a.hi, rb);
+  const ff r = ff_sub(a, ff_mul_f(b, q1));
+  const float q2 = __fmul_rn(r.hi, rb);
+  float l;
+  const float h = fast_two_sum(q1, q2, l);
+  return ff{h, l};
+}
 // a = m 4^e with m in [0.25, 1): sqrt a = sqrt(m) 2^e, one Newton step on
 // the FP32 square root, so the low words stay normal for any normal a.hi
 __device__ __forceinline__ ff ff_sqrt(ff a) {
@@ -180,7 +194,10 @@ __device__ const float2 k_ff_exp2_64[64] = {
 // |n| < 2^15), |r| <= ln2/128; expm1(r) by its Taylor series (r^2/2 and
 // r^3/6 in float-float, the r^4 and r^5 terms in float; the first omitted
 // term is below 4e-17), then e^a = 2^k 2^(j/64) (1 + expm1(r)).
-__device__ __forceinline__ ff ff_exp(ff a) {
+// Out of line (as ff_log): the per-marker viscosity calls them several
+// times, and inlined copies of their ~50 instructions each made the marker
+// physics kernel wait on instruction fetch.
+static __device__ __noinline__ ff ff_exp(ff a) {
   if (a.hi < -87.0f) return ff_f(0.f);
   if (a.hi > 88.0f) return ff_f(INFINITY);
   const float nf = rintf(__fmul_rn(a.hi, 0x1.715476p+6f));  // 64/ln 2
@@ -205,7 +222,7 @@ __device__ __forceinline__ ff ff_exp(ff a) {
 
 // a = m 2^e with m in [0.5, 1); log a = log m + e ln 2, so that e^-log m
 // stays in (1, 2] whatever the size of a (a.hi a positive normal float)
-__device__ __forceinline__ ff ff_log(ff a) {
+static __device__ __noinline__ ff ff_log(ff a) {
   int e;
   (void)frexpf(a.hi, &e);
   const int e1 = e >> 1, e2 = e - e1;

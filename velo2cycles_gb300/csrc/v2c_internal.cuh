@@ -40,6 +40,7 @@ enum {
   RK_SS, RK_SS_LO,         // ss
   RK_EM, RK_EM_LO,         // (mm-1)/mm
   RK_MM1, RK_MM1_LO,       // mm-1
+  RK_LNSS_LO,              // low word of ln ss
   RK_N
 };
 enum { VISC_NEWTON = 0, VISC_POWER = 1, VISC_STICKY = 2, VISC_UNDEF = 3 };

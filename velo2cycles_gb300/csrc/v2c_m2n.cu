@@ -165,7 +165,7 @@ __device__ __forceinline__ ff acc_ff(const Acc &a) {
 }
 // num / den of two compensated sums, rounded once
 __device__ __forceinline__ float ratio(const Acc &num, const ff &den) {
-  return ff_round(ff_div(acc_ff(num), den));
+  return ff_round(ff_div_fast(acc_ff(num), den));
 }
 // the antidiffusion form cur + (n - prev) (interpolation.c:730-736, 758-763,
 // 784-806) from the float-pair node average n: cur and prev are consecutive
@@ -195,8 +195,8 @@ __device__ __forceinline__ void node_tail(const M2NArgs &a, int role, int ci, in
     const float ss = ff_round(ssf);
     const bool interior = ci >= 1 && j >= 1 && ci < g.xn - 1 && j < g.yn - 1;
     if (ss != 0.f && interior) {
-      const ff phin = ff_div(acc_ff(cur[6]), ssf), sxyen = ff_div(acc_ff(cur[3]), ssf);
-      const ff exyen = ff_div(acc_ff(cur[4]), ssf), pen = ff_div(acc_ff(cur[2]), ssf);
+      const ff phin = ff_div_fast(acc_ff(cur[6]), ssf), sxyen = ff_div_fast(acc_ff(cur[3]), ssf);
+      const ff exyen = ff_div_fast(acc_ff(cur[4]), ssf), pen = ff_div_fast(acc_ff(cur[2]), ssf);
       float phis, sxye, exye, pe;
       if (antid) {
         phis = antid_rn(phin, N.f(V2C_NF_PHIS_IT)[m3], N.f(V2C_NF_PHIE)[m3]);
@@ -256,8 +256,8 @@ __device__ __forceinline__ void node_tail(const M2NArgs &a, int role, int ci, in
       const ff s1f = acc_ff(cur[5]);
       const float s1 = ff_round(s1f);
       if (s1 != 0.f) {
-        const ff sxxen = ff_div(acc_ff(cur[2]), s1f), sppen = ff_div(acc_ff(cur[4]), s1f);
-        const ff exxen = ff_div(acc_ff(cur[3]), s1f);
+        const ff sxxen = ff_div_fast(acc_ff(cur[2]), s1f), sppen = ff_div_fast(acc_ff(cur[4]), s1f);
+        const ff exxen = ff_div_fast(acc_ff(cur[3]), s1f);
         float sxxe, sppe, exxe;
         if (antid) {
           sxxe = antid_rn(sxxen, N.f(V2C_NF_SXX)[mc], N.f(V2C_NF_SXXEE)[mc]);
@@ -292,26 +292,26 @@ __device__ __forceinline__ void node_tail(const M2NArgs &a, int role, int ci, in
     const ff wxf = acc_ff(cur[2]);
     if (ff_round(wxf) != 0.f) {
       const ff mrx0 = acc_ff(cur[1]);
-      const ff mvxn = ff_div(acc_ff(cur[0]), mrx0);
+      const ff mvxn = ff_div_fast(acc_ff(cur[0]), mrx0);
       N.f(V2C_NF_MVXN)[m3] = ff_round(mvxn);
       // the boundary correction (vxvy_boundarycorrection) leaves the vx
       // ghost row at zero; only the 13-node stencil gives it weight
       N.f(V2C_NF_MVX)[m3] = j == g.yn - 1 ? 0.f
                             : antid ? antid_rn(mvxn, N.f(V2C_NF_VX)[m3], N.f(V2C_NF_MVXE)[m3])
                                     : ff_round(mvxn);
-      N.f(V2C_NF_MRX)[m3] = ff_round(ff_div(mrx0, wxf));
+      N.f(V2C_NF_MRX)[m3] = ff_round(ff_div_fast(mrx0, wxf));
     } else {
       N.f(V2C_NF_MVX)[m3] = 0; N.f(V2C_NF_MRX)[m3] = 0;
     }
     const ff wyf = acc_ff(vy3[2]);
     if (ff_round(wyf) != 0.f) {
       const ff mry0 = acc_ff(vy3[1]);
-      const ff mvyn = ff_div(acc_ff(vy3[0]), mry0);
+      const ff mvyn = ff_div_fast(acc_ff(vy3[0]), mry0);
       N.f(V2C_NF_MVYN)[m3] = ff_round(mvyn);
       N.f(V2C_NF_MVY)[m3] = ci == g.xn - 1 ? 0.f  // the vy ghost column, likewise
                             : antid ? antid_rn(mvyn, N.f(V2C_NF_VY)[m3], N.f(V2C_NF_MVYE)[m3])
                                     : ff_round(mvyn);
-      N.f(V2C_NF_MRY)[m3] = ff_round(ff_div(mry0, wyf));
+      N.f(V2C_NF_MRY)[m3] = ff_round(ff_div_fast(mry0, wyf));
     } else {
       N.f(V2C_NF_MVY)[m3] = 0; N.f(V2C_NF_MRY)[m3] = 0;
     }

@@ -150,10 +150,8 @@ __global__ void __launch_bounds__(PT, 5) k_phys(PhysArgs a) {
         const float mkt = conductivity32(a.R, t, T, mpb);
         const float sxx = a.m.sxx[i], sxy = a.m.sxy[i];
         sigin = sqrtf(sxx * sxx + sxy * sxy);
-        float s2lo;
-        const float s2 = two_prod(sxx, sxx, s2lo);
-        const ff sig_ff = ff_sqrt(ff_add(ff{s2, s2lo}, ff_mul(ff_f(sxy), ff_f(sxy))));
-        mnu = ductile_visc32(a.R, a.S, t, sig_ff, T, a.m.tk_lo[i], mpb_ff);
+        const ff sig2 = ff_add(ff_mul(ff_f(sxx), ff_f(sxx)), ff_mul(ff_f(sxy), ff_f(sxy)));
+        mnu = ductile_visc32(a.R, a.S, t, sig2, T, a.m.tk_lo[i], mpb_ff);
         const float phi0 = a.m.phi[i];
         phi = marker_friction(a, ix, iy, u, v, ax.X, ay.X, t, phi0, fr);
         if (!collect) {

@@ -31,11 +31,11 @@ __device__ __forceinline__ float conductivity32(const Rock &R, int t, float T, f
 }
 
 // ductilevisc.  Returns NaN for a type that fits no branch (the reference
-// leaves its result undefined there).  sigin (the stress invariant) and mpb
-// (pressure, bar) arrive as float pairs: the dislocation viscosity goes as
-// sigin^(1-n) and the Arrhenius factor as e^(V P/(R T)), with V P/(R T) up to
-// ~7 in the mantle, so their FP32 roundings alone would be a few 1e-7 of
-// the viscosity.
+// leaves its result undefined there).  sig2 = sxx^2 + sxy^2 (the squared
+// stress invariant) and mpb (pressure, bar) arrive as float pairs: the
+// dislocation viscosity goes as sigin^(1-n) and the Arrhenius factor as
+// e^(V P/(R T)), with V P/(R T) up to ~7 in the mantle, so their FP32
+// roundings alone would be a few 1e-7 of the viscosity.
 //
 // Precision.  The viscosity is e^s0 times an O(1) ratio, with s0 = ln of
 // the diffusion-creep viscosity, up to ~60: an FP32 s0 alone (ulp 4e-6)
@@ -61,10 +61,11 @@ __device__ __forceinline__ float conductivity32(const Rock &R, int t, float T, f
 //        f2(d* + e) = R0 + e - (q B*)^em expm1(em log1p(e (1 + g)/B*)),
 //      every term of which FP32 holds to a few 1e-7 of e rather than of d,
 //      as it does the steps and the change that the stopping test reads.
-// The viscosity is e^(s0 + ln(d/(1 + d))) at the step the replay stops, the
-// exponent and the exponential in float-float, rounded once to FP32.
+// The viscosity is e^s0 d/(1 + d) at the step the replay stops, in
+// float-float, rounded once to FP32 (through the exponent s0 + ln(d/(1+d))
+// where it is near a limit or e^s0 is beyond the FP32 range).
 __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, int t,
-                                                ff sig_ff, float T, float Tlo, ff mpb) {
+                                                ff sig2, float T, float Tlo, ff mpb) {
   int kind = (int)R(RK_KIND, t);
   if (kind == VISC_STICKY) {
     float nu = R(RK_NU, t);
@@ -78,25 +79,28 @@ __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, in
   // (E + PV)/(RT), density_ductilevisc_calc.c:116-120, capped at 150
   const ff num = ff_add(ff{R(RK_DH, t), R(RK_DH_LO, t)}, ff_mul(ff{R(RK_DV, t), R(RK_DV_LO, t)}, mpb));
   const ff den = ff_mul(ff{T, Tlo}, ff{8.31400012969970703125f, -1.2969971407983394e-07f});
-  ff le1 = den.hi != 0.f ? ff_div(num, den) : ff_f(num.hi / den.hi);
+  ff le1 = den.hi != 0.f ? ff_div_fast(num, den) : ff_f(num.hi / den.hi);
   if (le1.hi > 150.f || (le1.hi == 150.f && le1.lo > 0.f)) le1 = ff_f(150.f);
   // ln of the diffusion-creep viscosity 0.5 k1 e1, k1 = nu / ss^(mm-1)
   const ff s0 = ff_add(ff{R(RK_LNK, t), R(RK_LNK_LO, t)}, le1);
-  ff lnr = ff_f(0.f);  // ln(eta / eta_diff); sigin == 0: eta = eta_diff
-  if (sig_ff.hi > 0.f) {
+  ff rat = ff_f(1.f);  // eta / eta_diff = d/(1 + d); sigin == 0: eta = eta_diff
+  if (sig2.hi > 0.f) {
     const ff em_ff{R(RK_EM, t), R(RK_EM_LO, t)};
     const float em = em_ff.hi;
-    const ff q_ff = ff_div(ff{R(RK_SS, t), R(RK_SS_LO, t)}, sig_ff);  // ss / sigin
-    const float q = q_ff.hi;
-    // G dt / eta_diff (0 without elasticity or time step)
+    // ln q = ln ss - ln sigin, q = ss / sigin
+    const ff lnq = ff_sub(ff{R(RK_LNSS, t), R(RK_LNSS_LO, t)}, ff_scale(ff_log(sig2), 0.5f));
+    const float q = __expf(lnq.hi);
+    // G dt / eta_diff (0 without elasticity or time step); below 6e-6 its
+    // FP32 value is within 1e-11 of itself, far inside what R0 needs
     ff g_ff = ff_f(0.f);
-    if (R(RK_LNG, t) > -INFINITY && S.lndt_hi > -INFINITY)
-      g_ff = ff_exp(ff_sub(ff_add(ff{R(RK_LNG, t), R(RK_LNG_LO, t)}, ff{S.lndt_hi, S.lndt_lo}), s0));
+    if (R(RK_LNG, t) > -INFINITY && S.lndt_hi > -INFINITY) {
+      const ff lng = ff_sub(ff_add(ff{R(RK_LNG, t), R(RK_LNG_LO, t)}, ff{S.lndt_hi, S.lndt_lo}), s0);
+      g_ff = lng.hi < -12.f ? ff_f(expf(lng.hi) * (1.f + lng.lo)) : ff_exp(lng);
+    }
     const float g = g_ff.hi, g1p = 1.f + g;
     // the reference's start, eta_disl / eta_diff = q^(mm-1) at the marker's
     // stress, in float-float: an FP32 start would change where the replay
     // stops in ~0.1 % of the markers
-    const ff lnq = ff_log(q_ff);
     const ff d0_ff = ff_exp(ff_mul(ff{R(RK_MM1, t), R(RK_MM1_LO, t)}, lnq));
     const float d0 = d0_ff.hi;
     // 1. d*: Newton on f2 with its exact derivative (fast intrinsics: only
@@ -160,19 +164,24 @@ __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, in
       e_prev = e_old;
       d_prev = d_old;
     }
-    // ln(d/(1 + d)) at the last step, d = d* + e as a float pair
+    // d/(1 + d) at the last step, d = d* + e as a float pair
     ff d_ff;
     d_ff.hi = two_sum(ds, e, d_ff.lo);
-    lnr = ff_log(ff_div(d_ff, ff_add_f(d_ff, 1.f)));
+    rat = ff_div_fast(d_ff, ff_add_f(d_ff, 1.f));
   }
-  // limits nubeg/nuend then the per-type limits, in that order
-  const ff lnv = ff_add(s0, lnr);
+  // limits nubeg/nuend then the per-type limits, in that order; an FP32
+  // estimate of ln nu (within 1e-5) decides all but the values near a limit
+  const float lest = s0.hi + __logf(rat.hi);
   float nu;
-  if (lnv.hi < S.ln_nubeg) nu = S.nubeg_f;
-  else if (lnv.hi > S.ln_nuend) nu = S.nuend_f;
-  else {
-    const ff v = ff_exp(lnv);
-    nu = __fadd_rn(v.hi, v.lo);
+  if (lest < S.ln_nubeg - 1e-3f) nu = S.nubeg_f;
+  else if (lest > S.ln_nuend + 1e-3f) nu = S.nuend_f;
+  else if (s0.hi < 80.f && lest > S.ln_nubeg + 1e-3f && lest < S.ln_nuend - 1e-3f) {
+    nu = ff_round(ff_mul(ff_exp(s0), rat));
+  } else {
+    const ff lnv = ff_add(s0, ff_log(rat));
+    if (lnv.hi < S.ln_nubeg) nu = S.nubeg_f;
+    else if (lnv.hi > S.ln_nuend) nu = S.nuend_f;
+    else nu = ff_round(ff_exp(lnv));
   }
   if (nu < R(RK_N0, t)) nu = R(RK_N0, t);
   if (nu > R(RK_N1, t)) nu = R(RK_N1, t);
