@@ -46,18 +46,26 @@ enum {
   P_CP, P_KT, P_TK, P_SXX, P_EXX, P_P, P_VX, P_VY, P_N
 };
 
+// A chunk's markers are staged at their sorted position plus the local row
+// of their cell (one free slot after each cell): the threads of consecutive
+// node rows read consecutive cells in lockstep, and with the cells' runs
+// at a spacing of count + 1 rather than count (16 or 20 markers per cell
+// in a fresh uniform seeding) their shared-memory reads fall in different
+// banks instead of a few.
+constexpr int SKEW = TY + 1;
 struct Smem {
-  float p[P_N][CHUNK];
-  uint8_t act[CHUNK];
+  float p[P_N][CHUNK + SKEW];
+  uint8_t act[CHUNK + SKEW];
 };
 
 // stage one marker's scatter payload; the per-marker physics (viscosity,
 // conductivity, density, state update) was done by the marker physics kernel
-__device__ __forceinline__ void stage(const M2NArgs &a, Smem &sm, int s, int k) {
+__device__ __forceinline__ void stage(const M2NArgs &a, Smem &sm, int s, int k, int jlo) {
   const Grid &g = a.g;
   const int idx = __ldg(a.perm + s);
   const int c = a.m.cell_in[idx];
   const int ix = c / g.ncy, iy = c - ix * g.ncy;
+  k += iy - jlo;  // the skew of the cell's run (Smem)
   const float u = a.m.u_in[idx], v = a.m.v_in[idx];
   const int t = a.m.type[idx];
   // strictly inside the model (interpolation.c:219)
@@ -369,38 +377,39 @@ __global__ void __launch_bounds__(NTH, MINB) k_m2n(M2NArgs a) {
         up_e = __ldg(a.start + cb + j + 1);
         s1up = iwx / __ldg(g.wy + j);
       }
+      const int rlo = j - 1 - jlo, rup = j - jlo;  // skews of cells (ci, j-1), (ci, j)
       for (int cs = seg_b; cs < seg_e; cs += CHUNK) {
         const int ce = min(cs + CHUNK, seg_e);
         __syncthreads();
-        for (int k = tid; k < ce - cs; k += NTH) stage(a, sm, cs + k, k);
+        for (int k = tid; k < ce - cs; k += NTH) stage(a, sm, cs + k, k, jlo);
         __syncthreads();
 // the staged markers of sorted positions [b, e) (one quarter class run)
-#define CLASS_RUN(b, e) \
-  for (int s = max((b), cs), s_e = min((e), ce), q = s - cs; s < s_e; ++s, q = s - cs) \
+#define CLASS_RUN(b, e, r) \
+  for (int s = max((b), cs), s_e = min((e), ce), q = s - cs + (r); s < s_e; ++s, ++q) \
     if (sm.act[q])
         if (role <= 1) {
           // cell (ci, j-1), bottom halves (v > 1/2): class 2 left, class 3 right
-          CLASS_RUN(ql.z, ql.w) {
+          CLASS_RUN(ql.z, ql.w, rlo) {
             const float u = sm.p[P_U][q], v = sm.p[P_V][q];
             if (u < 0.5f) {
               const float w = s1lo * (1.f - 2.f * u) * (2.f * v - 1.f);
               if (role == 0) ADD_BASIC_A(cur, q, w); else ADD_BASIC_B(cur, q, w);
             }
           }
-          CLASS_RUN(ql.w, lo_e) {
+          CLASS_RUN(ql.w, lo_e, rlo) {
             const float u = sm.p[P_U][q], v = sm.p[P_V][q];
             const float w = s1lo * (2.f * u - 1.f) * (2.f * v - 1.f);
             if (role == 0) ADD_BASIC_A(car, q, w); else ADD_BASIC_B(car, q, w);
           }
           // cell (ci, j), top halves (v < 1/2): class 0 left, class 1 right
-          CLASS_RUN(qu.x, qu.y) {
+          CLASS_RUN(qu.x, qu.y, rup) {
             const float u = sm.p[P_U][q], v = sm.p[P_V][q];
             if (u < 0.5f && v < 0.5f) {
               const float w = s1up * (1.f - 2.f * u) * (1.f - 2.f * v);
               if (role == 0) ADD_BASIC_A(cur, q, w); else ADD_BASIC_B(cur, q, w);
             }
           }
-          CLASS_RUN(qu.y, qu.z) {
+          CLASS_RUN(qu.y, qu.z, rup) {
             const float u = sm.p[P_U][q], v = sm.p[P_V][q];
             if (v < 0.5f) {
               const float w = s1up * (2.f * u - 1.f) * (1.f - 2.f * v);
@@ -409,7 +418,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_m2n(M2NArgs a) {
           }
         } else if (role == 2) {
           // the whole cell (ci, j) to its centre node
-          CLASS_RUN(qu.x, up_e) {
+          CLASS_RUN(qu.x, up_e, rup) {
             const float u = sm.p[P_U][q], v = sm.p[P_V][q];
             const float w = s1up * tent(u) * tent(v);
             cur[0].add(sm.p[P_NU][q] * w); cur[1].add(sm.p[P_NUG][q] * w);
@@ -418,7 +427,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_m2n(M2NArgs a) {
           }
         } else {
           // vy node (ci, j) from the bottom halves of cell (ci, j-1)
-          CLASS_RUN(ql.z, lo_e) {
+          CLASS_RUN(ql.z, lo_e, rlo) {
             const float u = sm.p[P_U][q], v = sm.p[P_V][q];
             const float w = s1lo * (1.f - fabsf(u - 0.5f)) * v;
             const float ro = sm.p[P_RO][q];
@@ -427,7 +436,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_m2n(M2NArgs a) {
           // cell (ci, j): vx node (ci, j) from u < 1/2 (classes 0, 2), vx node
           // (ci+1, j) from u > 1/2 (classes 1, 3), vy node (ci, j) from v < 1/2
           // (classes 0, 1)
-          CLASS_RUN(qu.x, qu.y) {
+          CLASS_RUN(qu.x, qu.y, rup) {
             const float u = sm.p[P_U][q], v = sm.p[P_V][q];
             const float ro = sm.p[P_RO][q];
             if (u < 0.5f) {
@@ -439,7 +448,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_m2n(M2NArgs a) {
               vy3[0].add(sm.p[P_VY][q] * ro * w); vy3[1].add(ro * w); vy3[2].add(w);
             }
           }
-          CLASS_RUN(qu.y, qu.z) {
+          CLASS_RUN(qu.y, qu.z, rup) {
             const float u = sm.p[P_U][q], v = sm.p[P_V][q];
             const float ro = sm.p[P_RO][q];
             const float wx = s1up * u * (1.f - fabsf(v - 0.5f));
@@ -449,7 +458,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_m2n(M2NArgs a) {
               vy3[0].add(sm.p[P_VY][q] * ro * w); vy3[1].add(ro * w); vy3[2].add(w);
             }
           }
-          CLASS_RUN(qu.z, qu.w) {
+          CLASS_RUN(qu.z, qu.w, rup) {
             const float u = sm.p[P_U][q], v = sm.p[P_V][q];
             if (u < 0.5f) {
               const float ro = sm.p[P_RO][q];
@@ -457,7 +466,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_m2n(M2NArgs a) {
               cur[0].add(sm.p[P_VX][q] * ro * w); cur[1].add(ro * w); cur[2].add(w);
             }
           }
-          CLASS_RUN(qu.w, up_e) {
+          CLASS_RUN(qu.w, up_e, rup) {
             const float u = sm.p[P_U][q], v = sm.p[P_V][q];
             const float ro = sm.p[P_RO][q];
             const float w = s1up * u * (1.f - fabsf(v - 0.5f));
