@@ -135,9 +135,14 @@ __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, in
     // = (c0 B*^em / B*) (1 + g1)/(1 + x)
     const float inv_Bs = __fdividef(1.f, Bs);
     const float kx = g1p * inv_Bs, kc = c0f1s * inv_Bs;
-    // (1 + x)^em - 1 = em x (1 + c1 x (1 + c2 x (1 + c3 x))) + O(x^5), for
-    // |x| < 1/32 within 3e-8 of itself (the steps near the stop)
-    const float c1 = 0.5f * (em - 1.f), c2 = (em - 2.f) * (1.f / 3.f), c3 = 0.25f * (em - 3.f);
+    // Near the stop (|x| < 1/32) both powers come from the binomial series
+    // of (1 + x)^a - 1 = h = a x (1 + c1 x (1 + c2 x (1 + c3 x (1 + c4 x)))),
+    // a = em - 1, c_k = (a - k)/(k + 1), within 1.4e-8 of itself there:
+    // (1 + x)^em - 1 = x + h (1 + x) and c0 B^em / B = kc (1 + h), without a
+    // division.
+    const float a1 = em - 1.f;
+    const float c1 = 0.5f * (a1 - 1.f), c2 = (a1 - 2.f) * (1.f / 3.f);
+    const float c3 = 0.25f * (a1 - 3.f), c4 = 0.2f * (a1 - 4.f);
     for (int counter = 1; counter <= 50; counter++) {
       const float e_old = e;
       const float d_old = ds + e_old;
@@ -146,11 +151,17 @@ __device__ __forceinline__ float ductile_visc32(const Rock &R, const Scal &S, in
       // B(d)/B* - 1: below -1 the reference's iteration has gone to a
       // negative prefactor, whose power is NaN there and is NaN here (log1pf)
       const float x = e_old * kx;
-      const float g1 = fabsf(x) < 0.03125f
-                           ? em * x * fmaf(c1 * x, fmaf(c2 * x, fmaf(c3, x, 1.f), 1.f), 1.f)
-                           : expm1f(em * log1pf(x));  // (B(d)/B*)^em - 1
+      float g1, cfB;  // (B(d)/B*)^em - 1 and c0 B^em / B
+      if (fabsf(x) < 0.03125f) {
+        const float h =
+            a1 * x * fmaf(c1 * x, fmaf(c2 * x, fmaf(c3 * x, fmaf(c4, x, 1.f), 1.f), 1.f), 1.f);
+        g1 = fmaf(h, 1.f + x, x);
+        cfB = fmaf(kc, h, kc);
+      } else {
+        g1 = expm1f(em * log1pf(x));
+        cfB = __fdividef(kc * (1.f + g1), 1.f + x);
+      }
       const float f2 = (e_old - c0f1s * g1) + r0;       // f2(d* + e)
-      const float cfB = __fdividef(kc * (1.f + g1), 1.f + x);  // c0 B^em / B
       // pow(eta_diff, 2/(eta_diff+eta_disl_old)) / eta_diff, the reference's
       // extra term of the derivative (density_ductilevisc_calc.c:190-191)
       const float p2 = (invS > 1e-30f && !(p2max < gm * 0x1p-25f))
