@@ -326,9 +326,10 @@ __device__ __forceinline__ void node_tail(const M2NArgs &a, int role, int ci, in
   }
 }
 
-// MINB resident CTAs per SM: 7 (72 registers) hides more latency at 20
-// markers per cell; at 16 or fewer the lanes' shared-memory bank conflicts
-// dominate and 6 (80 registers, no spills) is faster (measured at 20 and 16)
+// MINB resident CTAs per SM: 6 (80 registers, no spills); the skewed
+// staging area (33.8 KB) leaves room for 6 CTAs, and at 7 (72 registers)
+// the spills cost more than the extra CTA gave before the skew (C4 window:
+// 0.73 against 0.65 ms)
 template <int MINB>
 __global__ void __launch_bounds__(NTH, MINB) k_m2n(M2NArgs a) {
   __shared__ Smem sm;
@@ -665,9 +666,7 @@ void launch_m2n(const M2NArgs &a, cudaStream_t st) {
     return;
   }
   dim3 grid((a.g.xn + a.TX - 1) / a.TX, (a.g.yn + TY - 1) / TY);
-  const long ncell = (long)a.g.ncx * a.g.ncy;
-  if (a.n > 16 * ncell + ncell / 2) k_m2n<7><<<grid, NTH, 0, st>>>(a);
-  else k_m2n<6><<<grid, NTH, 0, st>>>(a);
+  k_m2n<6><<<grid, NTH, 0, st>>>(a);
 }
 
 void launch_sticky(const Nodes &N, const uint32_t *key, long nn, cudaStream_t st) {
