@@ -266,6 +266,20 @@ int v2c_download_node_field(v2c_ctx *ctx, int field, double *dst);
 int v2c_upload_node_fields(v2c_ctx *ctx, int count, const int *fields,
                            const double *const *src);
 int v2c_download_node_fields(v2c_ctx *ctx, int count, const int *fields, double *const *dst);
+/* The download above without waiting for it: the fields are converted on
+ * the context stream after the work enqueued so far (a snapshot: later
+ * calls may change them) and copied to dst on a transfer stream of the
+ * context, so that the copies run under the kernels the caller enqueues
+ * next.  dst (count arrays of nodenum doubles) must be pinned host memory
+ * for the copies to overlap, and must not be read before
+ * v2c_wait_downloads (or v2c_synchronize) returns.  A second asynchronous
+ * download reuses the staging area (count x nodenum doubles, allocated at
+ * the first call or when count grows, synchronising both streams) after
+ * the first one's copies.  No counterpart in the reference, whose node
+ * arrays are host memory. */
+int v2c_download_node_fields_async(v2c_ctx *ctx, int count, const int *fields,
+                                   double *const *dst);
+int v2c_wait_downloads(v2c_ctx *ctx);
 
 /* ======================================================= the MIC step calls
  * Reference equivalents in brackets.  All are asynchronous on the context

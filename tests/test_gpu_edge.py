@@ -145,3 +145,32 @@ def test_batched_node_fields(built_lib):
         m.download_nodes([abi.NF_N])
     assert e.value.code == abi.ERR_ARG
     m.close()
+
+
+def test_async_node_download(built_lib):
+    """v2c_download_node_fields_async: a snapshot of the fields as the calls
+    before it leave them, copied while the node kernels after it run (they
+    write other fields), equal to the synchronous download; a second
+    asynchronous download reuses the staging area after the first."""
+    c = synth.make_case("small", seed=8)
+    m = mic.from_case(c)
+    dt = c.params["timestep"]
+    m.marker2nodes()
+    fields = [abi.NF_NU_M2C, abi.NF_ND_M2C, abi.NF_GG, abi.NF_SXXE, abi.NF_SPPE, abi.NF_TK]
+    want = m.download_nodes(fields)
+    got = {f: np.full(c.nodenum, np.nan) for f in fields}
+    m.download_nodes_async(got)
+    m.interpolate_center2basic_old()
+    m.compute_before_solve(dt, 0)
+    # a second download of fields the node kernels just wrote
+    f2 = [abi.NF_NU, abi.NF_SYIELDS]
+    got2 = {f: np.full(c.nodenum, np.nan) for f in f2}
+    m.download_nodes_async(got2)
+    m.compute_after_solve(dt, 0)
+    m.wait_downloads()
+    for f in fields:
+        assert np.array_equal(got[f], want[f]), f
+    want2 = m.download_nodes(f2)
+    for f in f2:
+        assert np.array_equal(got2[f], want2[f]), f
+    m.close()

@@ -58,6 +58,8 @@ _SIGS = {
     "v2c_cycle_marker_slip": [c_ctx, c_dp, ctypes.c_long],
     "v2c_upload_node_fields": [c_ctx, ctypes.c_int, P(ctypes.c_int), P(c_dp)],
     "v2c_download_node_fields": [c_ctx, ctypes.c_int, P(ctypes.c_int), P(c_dp)],
+    "v2c_download_node_fields_async": [c_ctx, ctypes.c_int, P(ctypes.c_int), P(c_dp)],
+    "v2c_wait_downloads": [c_ctx],
     "v2c_marker2nodes": [c_ctx],
     "v2c_center2basic_old": [c_ctx],
     "v2c_compute_before_solve": [c_ctx, ctypes.c_double, ctypes.c_int],

@@ -60,6 +60,13 @@ struct v2c_ctx {
   // m.mnu / m.mkt hold the properties of the current marker slots (set by
   // marker2nodes, cleared when markers are uploaded or moved)
   bool props_valid = false;
+  // asynchronous node-field downloads: their own staging area, copied on a
+  // transfer stream after the conversion on the context stream
+  cudaStream_t xfer = nullptr;
+  cudaEvent_t ev_conv = nullptr, ev_copy = nullptr;
+  double *d_astage = nullptr;
+  int astage_fields = 0;
+  bool dl_pending = false;
   // sort
   SortBufs sb{};
   bool sorted = false;
@@ -333,6 +340,13 @@ extern "C" int v2c_create(const v2c_params *p, long max_markers, void *cuda_stre
 extern "C" int v2c_destroy(v2c_ctx *ctx) {
   if (!ctx) return V2C_ERR_ARG;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->xfer) {
+    cudaStreamSynchronize(ctx->xfer);
+    cudaStreamDestroy(ctx->xfer);
+  }
+  if (ctx->ev_conv) cudaEventDestroy(ctx->ev_conv);
+  if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
+  if (ctx->d_astage) cudaFree(ctx->d_astage);
   for (auto &gr : ctx->graphs) cudaGraphExecDestroy(gr.exec);
   ctx->graphs.clear();
   for (float *v : ctx->d_cyc_v)
@@ -854,6 +868,51 @@ extern "C" int v2c_upload_node_fields(v2c_ctx *ctx, int count, const int *fields
   return V2C_OK;
 }
 
+extern "C" int v2c_download_node_fields_async(v2c_ctx *ctx, int count, const int *fields,
+                                              double *const *dst) {
+  if (!ctx) return V2C_ERR_ARG;
+  if (!node_field_list_ok(count, fields, (const void *const *)dst)) return fail(ctx, V2C_ERR_ARG);
+  if (count == 0) return V2C_OK;
+  cudaStream_t st = ctx->stream;
+  if (!ctx->xfer) {
+    CK(cudaStreamCreateWithFlags(&ctx->xfer, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ctx->ev_conv, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming));
+  }
+  if (count > ctx->astage_fields) {
+    // a larger staging area: the earlier copies out of the old one first
+    CK(cudaStreamSynchronize(ctx->xfer));
+    CK(cudaStreamSynchronize(st));
+    if (ctx->d_astage) CK(cudaFree(ctx->d_astage));
+    ctx->d_astage = nullptr;
+    CK(cudaMalloc(&ctx->d_astage, sizeof(double) * ctx->nn * count));
+    ctx->astage_fields = count;
+  }
+  // the staging area is reused: the conversion waits for the copies of the
+  // previous asynchronous download
+  if (ctx->dl_pending) CK(cudaStreamWaitEvent(st, ctx->ev_copy, 0));
+  launch_fields_to_f64(ctx->d_node, ctx->nn, fields, count, ctx->d_astage, st);
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ctx->ev_conv, st));
+  CK(cudaStreamWaitEvent(ctx->xfer, ctx->ev_conv, 0));
+  for (int k = 0; k < count; k++)
+    CK(cudaMemcpyAsync(dst[k], ctx->d_astage + (long)k * ctx->nn, sizeof(double) * ctx->nn,
+                       cudaMemcpyDeviceToHost, ctx->xfer));
+  CK(cudaEventRecord(ctx->ev_copy, ctx->xfer));
+  ctx->dl_pending = true;
+  return V2C_OK;
+}
+
+extern "C" int v2c_wait_downloads(v2c_ctx *ctx) {
+  if (!ctx) return V2C_ERR_ARG;
+  if (ctx->dl_pending) {
+    CK(cudaEventSynchronize(ctx->ev_copy));
+    ctx->dl_pending = false;
+  }
+  return V2C_OK;
+}
+
 extern "C" int v2c_download_node_fields(v2c_ctx *ctx, int count, const int *fields,
                                         double *const *dst) {
   if (!ctx) return V2C_ERR_ARG;
@@ -1153,6 +1212,10 @@ extern "C" int v2c_calc_timestep(v2c_ctx *ctx, int oldornew, const v2c_timestep_
 extern "C" int v2c_synchronize(v2c_ctx *ctx) {
   if (!ctx) return V2C_ERR_ARG;
   CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->dl_pending) {
+    CK(cudaEventSynchronize(ctx->ev_copy));
+    ctx->dl_pending = false;
+  }
   CK(cudaGetLastError());
   return V2C_OK;
 }

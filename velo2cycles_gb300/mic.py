@@ -164,6 +164,24 @@ class MarkerInCell:
         call("v2c_download_node_fields", self.h, len(fields), fl, pp)
         return {f: out[f] for f in fields}
 
+    def download_nodes_async(self, arrays: dict):
+        """Start downloading node fields into arrays (field id -> nodenum
+        doubles, ideally pinned): a snapshot of the fields as the calls
+        enqueued so far leave them, copied while later calls run; read them
+        after wait_downloads()."""
+        fields = list(arrays)
+        for f in fields:
+            a = arrays[f]
+            assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.nn
+        fl = (ctypes.c_int * len(fields))(*fields)
+        pp = (ctypes.POINTER(ctypes.c_double) * len(fields))(*[_ptr(arrays[f]) for f in fields])
+        self._async_keep = (arrays, fl, pp)
+        call("v2c_download_node_fields_async", self.h, len(fields), fl, pp)
+
+    def wait_downloads(self):
+        call("v2c_wait_downloads", self.h)
+        self._async_keep = None
+
     # ----------------------------------------------------- the MIC calls
     def marker2nodes(self):
         call("v2c_marker2nodes", self.h)
