@@ -18,9 +18,12 @@ def restatement_path() -> str:
     return os.path.join(OUT, "liboracle.so")
 
 
-def reference_path(serial: bool = False) -> str:
-    """The reference routines built with OpenMP (v2c_ref), or with the
-    OpenMP pragmas ignored (v2c_ref_serial)."""
+def reference_path(serial: bool = False, fast: bool = False) -> str:
+    """The reference routines built with OpenMP (v2c_ref), with the OpenMP
+    pragmas ignored (v2c_ref_serial), or with OpenMP and floating-point
+    contraction allowed (v2c_ref_fast: the timed baseline)."""
+    if fast:
+        return os.path.join(OUT, "v2c_ref_fast")
     return os.path.join(OUT, "v2c_ref_serial" if serial else "v2c_ref")
 
 
@@ -437,10 +440,11 @@ def read_result(path: str, nodenum: int):
 
 def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeout=3600,
                   timestep=None, oldornew=0, dts=None, heatdif=None, stokes=None,
-                  serial=False):
+                  serial=False, fast=False):
     """Run the reference routines on `case`; returns the arrays after the
     stages plus per-stage seconds summed over the timed steps.  serial: the
-    build with the OpenMP pragmas ignored."""
+    build with the OpenMP pragmas ignored; fast: the build with
+    floating-point contraction (timing only)."""
     if not reference_available():
         build()
     if not reference_available():
@@ -450,7 +454,10 @@ def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeo
         write_case(cp, case, stages, nthreads, nsteps, warmup, timestep, oldornew, dts, heatdif,
                    stokes)
         env = dict(os.environ, OMP_NUM_THREADS=str(max(1, nthreads)))
-        r = subprocess.run([reference_path(serial), cp, rp], env=env, capture_output=True,
+        exe = reference_path(serial, fast)
+        if fast and not os.path.exists(exe):
+            exe = reference_path(serial)
+        r = subprocess.run([exe, cp, rp], env=env, capture_output=True,
                            timeout=timeout, cwd=d)
         if r.returncode != 0:
             raise RuntimeError(f"v2c_ref failed ({r.returncode}): {r.stderr.decode()[-2000:]}")

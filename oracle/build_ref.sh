@@ -33,14 +33,15 @@ temperature_iterate.c plastic.c recalc_marker_properties.c load_save.c"
 if [ -n "$REF" ] && [ -d "$REF/src" ]; then
   mkdir -p "$OUT/src"
   for f in $FILES; do cp "$REF/src/$f" "$OUT/src/$f"; done
-  # grid up to 1100 x 420 lines, 6.5 M markers; the Stokes matrix arrays
-  # (MAXVAL coefficients) hold the assembly of a 1001 x 401 grid.
+  # grid up to 1100 x 420 lines, 8.2 M markers (a 1001 x 401 window of the
+  # 20-markers-per-cell configuration); the Stokes matrix arrays (MAXVAL
+  # coefficients) hold the assembly of a 1001 x 401 grid.
   sed -i \
     -e 's/^#define MAXMAT .*/#define MAXMAT  8000000/' \
     -e 's/^#define MAXVAL .*/#define MAXVAL  24000000/' \
     -e 's/^#define MAXXLN .*/#define MAXXLN  1100/' \
     -e 's/^#define MAXYLN .*/#define MAXYLN  420/' \
-    -e 's/^#define MAXMRK .*/#define MAXMRK  6500001/' \
+    -e 's/^#define MAXMRK .*/#define MAXMRK  8200001/' \
     "$OUT/src/headevps.c"
 fi
 
@@ -49,6 +50,12 @@ if [ -f "$OUT/src/headevps.c" ]; then
   case "$(uname -m)" in x86_64) MODEL="-mcmodel=medium" ;; esac
   $CC -std=gnu99 -O3 -fopenmp -fcommon -w -ffp-contract=off $MODEL \
       -I"$OUT/src" -I"$HERE/../include" -o "$OUT/v2c_ref" "$HERE/ref_harness.c" -lm
+  # 2b. oracle/_ref/v2c_ref_fast -- the same build with floating-point
+  #     contraction allowed, as the reference's own icc build compiles by
+  #     default (compile_euler.sh): the timed CPU baseline; the build above
+  #     stays the bit-exact pin.
+  $CC -std=gnu99 -O3 -fopenmp -fcommon -w -ffp-contract=fast $MODEL \
+      -I"$OUT/src" -I"$HERE/../include" -o "$OUT/v2c_ref_fast" "$HERE/ref_harness.c" -lm
   # 3. oracle/_ref/v2c_ref_serial -- the same sources with the OpenMP
   #    pragmas ignored (libgomp linked only for omp_get_wtime): the routines
   #    as written for one thread.  moveandrotatemarkers appends spawned
