@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(NT, 4) k_solve_states(const double *S, long n,
                   : fp64     ? rsf_solve64(in, learned ? (double)u0 : u_plain64, rtol, maxit)
                              : rsf_solve_split(in, rsf32_of(in), u0, rtol, maxit);
       it = r.it32 + r.itff + r.it64;
-      if (!r.ok && learned) {
+      if (!r.ok && learned && u0 != u_plain) {
         RsfResult r2 = fp64 ? rsf_solve64(in, u_plain64, rtol, maxit)
                             : rsf_solve_split(in, rsf32_of(in), u_plain, rtol, maxit);
         it += r2.it32 + r2.itff + r2.it64;
@@ -138,6 +138,49 @@ __global__ void __launch_bounds__(NT, 4) k_solve_states(const double *S, long n,
     warp_add(stat + ST_NEWTON_ITERS, it);
     warp_add(stat + ST_NEWTON_FALLBACK, fb);
     warp_add(stat + ST_NEWTON_NONCONV, nc);
+  }
+}
+
+// The learned start of every state (the k_guess rule of the MIC step):
+// the plain start where its FP32 residual ratio is below RSF_NET_MIN_RES,
+// else the better of it and the network's proposal, the network evaluated
+// by a warp only when one of its states needs it.
+__global__ void __launch_bounds__(NT) k_learned_start(const double *S, long n, double W,
+                                                      const float *mlp, float *u0_out) {
+  __shared__ MlpSmem M;
+  mlp_load_smem(M, mlp);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  const long nwarps = (long)gridDim.x * (NT / 32);
+  for (long base = ((long)blockIdx.x * (NT / 32) + wl) * 32; base < n; base += nwarps * 32) {
+    const long i = base + lane;
+    RsfIn in;
+    double vold = 1e-9;
+    float rp = 0.f, up = 0.f, u_plain = 0.f;
+    bool need = false;
+    if (i < n) {
+      state_of(S, n, i, W, in, vold);
+      u_plain = (vold > 0) ? logf((float)vold) : -30.f;
+      float A_floor;
+      const Rsf32 q = rsf32_of(in);
+      if (!rsf_floor_certain(q, A_floor)) {
+        rp = rsf_start_residual(q, u_plain, up);
+        need = !(rp <= RSF_NET_MIN_RES);
+      }
+    }
+    float u0 = u_plain;
+    if (__any_sync(V2C_FULL, need)) {
+      float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      if (need) rsf_features(in, f);
+#pragma unroll
+      for (int k = 0; k < 8; k++) M.xin[wl][lane][k] = f[k];
+      __syncwarp();
+      mlp_warp_forward(M, wl);
+      float un;
+      if (need && rsf_start_residual(rsf32_of(in), M.yout[wl][lane][0], un) < rp) u0 = un;
+      __syncwarp();
+    }
+    if (i < n) u0_out[i] = u0;
   }
 }
 
@@ -516,7 +559,8 @@ extern "C" int v2c_rsf_newton(v2c_ctx *ctx, const double *states_dev, long n, in
       CKR(cudaMalloc((void **)&ns->d_guess, sizeof(float) * 2 * n));
       ns->guess_cap = n;
     }
-    k_infer<<<(unsigned)blocks, NT, 0, st>>>(states_dev, n, p->faultwidth, ns->d_mlp, ns->d_guess);
+    k_learned_start<<<(unsigned)blocks, NT, 0, st>>>(states_dev, n, p->faultwidth, ns->d_mlp,
+                                                     ns->d_guess);
     v2c_ctx_count_launches(ctx, 1);
   }
   auto kern = fp64 ? (learned ? k_solve_states<true, true> : k_solve_states<true, false>)

@@ -217,9 +217,12 @@ __global__ void __launch_bounds__(PT, 5) k_phys(PhysArgs a) {
   if (newton) warp_add(a.stat + ST_NEWTON_ITERS, it);
 }
 
-// The network's start for every listed problem, 32 per warp (BF16 tensor
-// cores), written to guess[e]; a kernel of its own so the Newton kernel
-// keeps the occupancy of the plain start.
+// The learned start of every listed problem, 32 per warp: the plain start
+// (the previous slip rate) where its FP32 residual ratio is already below
+// RSF_NET_MIN_RES, else the better of it and the network's proposal
+// (evaluated by the warp on the BF16 tensor cores only when one of its
+// problems needs it), written to guess[e]; a kernel of its own so the
+// Newton kernel keeps the occupancy of the plain start.
 __global__ void __launch_bounds__(PT, 4) k_guess(PhysArgs a, float *guess) {
   __shared__ MlpSmem S;
   mlp_load_smem(S, a.mlp);
@@ -227,24 +230,31 @@ __global__ void __launch_bounds__(PT, 4) k_guess(PhysArgs a, float *guess) {
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const long nwarps = (long)gridDim.x * (PT / 32);
   const long cnt = *a.list_n;
-  const v2c_params &P = a.S.p;
   const ff dt_ff{a.S.dt_hi, a.S.dt_lo}, W_ff{a.S.W_hi, a.S.W_lo}, sn_ff{a.S.sn_hi, a.S.sn_lo};
   for (long base = ((long)blockIdx.x * (PT / 32) + wl) * 32; base < cnt; base += nwarps * 32) {
     const long e = base + lane;
     const bool valid = e < cnt;
-    float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    RsfIn in;
+    float uplain = 0.f, rp = 0.f, up = 0.f;
+    bool need = false;
     if (valid) {
-      RsfIn in;
-      float uplain;
       marker_problem(a, a.list[e], dt_ff, W_ff, sn_ff, in, uplain);
-      rsf_features(in, f);
+      rp = rsf_start_residual(rsf32_of(in), uplain, up);
+      need = !(rp <= RSF_NET_MIN_RES);
     }
+    float u0 = uplain;
+    if (__any_sync(V2C_FULL, need)) {
+      float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      if (need) rsf_features(in, f);
 #pragma unroll
-    for (int k = 0; k < 8; k++) S.xin[wl][lane][k] = f[k];
-    __syncwarp();
-    mlp_warp_forward(S, wl);
-    if (valid) guess[e] = S.yout[wl][lane][0];
-    __syncwarp();
+      for (int k = 0; k < 8; k++) S.xin[wl][lane][k] = f[k];
+      __syncwarp();
+      mlp_warp_forward(S, wl);
+      float un;
+      if (need && rsf_start_residual(rsf32_of(in), S.yout[wl][lane][0], un) < rp) u0 = un;
+      __syncwarp();
+    }
+    if (valid) guess[e] = u0;
   }
 }
 
@@ -271,7 +281,7 @@ __global__ void __launch_bounds__(PT, 5) k_newton(PhysArgs a, const float *guess
     RsfResult r = FP64 ? rsf_solve64(in, (double)u0, P.newton_rtol, P.newton_maxit)
                        : rsf_solve_split(in, rsf32_of(in), u0, P.newton_rtol, P.newton_maxit);
     it += r.it32 + r.itff + r.it64;
-    if (!r.ok && LEARNED) {
+    if (!r.ok && LEARNED && u0 != uplain) {
       RsfResult r2 = FP64 ? rsf_solve64(in, (double)uplain, P.newton_rtol, P.newton_maxit)
                           : rsf_solve_split(in, rsf32_of(in), uplain, P.newton_rtol, P.newton_maxit);
       it += r2.it32 + r2.itff + r2.it64;

@@ -334,6 +334,26 @@ __device__ __forceinline__ bool rsf_floor_certain(const Rsf32 &q, float &A_floor
   return F >= 1e-3f * lhs;
 }
 
+// The start u0 clamped into the FP32 Newton's bracket, as rsf_newton32
+// does, and the FP32 residual ratio |F|/lhs there.
+__device__ __forceinline__ float rsf_start_residual(const Rsf32 &q, float u0, float &u) {
+  const float ulo = (float)RSF_LOG_FLOOR, uhi = q.uhi;
+  u = fminf(fmaxf(u0, ulo + 1e-3f * (uhi - ulo)), uhi - 1e-3f * (uhi - ulo));
+  float dF, lhs;
+  const float F = rsf_eval32(q, u, dF, lhs);
+  const float r = fabsf(F) / lhs;
+  return r == r ? r : INFINITY;
+}
+
+// The learned start, evaluated only where it can pay: the network's
+// proposal costs a few Newton iterations' worth of work, so a state whose
+// plain start (the previous slip rate) already has an FP32 residual ratio
+// below RSF_NET_MIN_RES -- a couple of Newton steps from the FP32 floor --
+// keeps it; elsewhere the proposal is taken if its residual is smaller
+// than the plain start's, so the chosen start is never the worse of the
+// two.
+constexpr float RSF_NET_MIN_RES = 1e-2f;
+
 // Split solve from the start u0 (FP32 phase, float-float phase, FP64
 // fallback).  q32 = rsf32_of(in).
 __device__ __forceinline__ RsfResult rsf_solve_split(const RsfIn &in, const Rsf32 &q32, float u0,
