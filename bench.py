@@ -163,8 +163,8 @@ def measured_peaks() -> dict:
 
 def ncu_traffic(kernel: str):
     """DRAM bytes per marker of `kernel` from the committed ncu summary
-    (profiles/traffic.json, a capture at C2); the caller scales it by the
-    markers of a launch."""
+    (profiles/traffic.json, one ncu pass at C4); the caller scales it by
+    the markers of a launch."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
         with open(p) as f:

@@ -328,9 +328,16 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
           const bool in_grid = (ix > 0 || u >= 0.f) && (ix < g.ncx - 1 || u <= 1.f) &&
                                (iy > 0 || v >= 0.f) && (iy < g.ncy - 1 || v <= 1.f);
           float tk = a.m.tk[idx];
-          float phi = a.m.phi[idx], mexx = a.m.exx[idx], mexy = a.m.exy[idx];
-          float msxx = a.m.sxx[idx], msxy = a.m.sxy[idx], mp = a.m.p[idx];
-          float mvx = a.m.vx[idx], mvy = a.m.vy[idx], me = a.m.e[idx];
+          // the marker's own values are read only without antidiffusion,
+          // where it keeps them plus the change of the node fields; with
+          // it, an updated marker takes all nine from the nodes
+          float phi = 0.f, mexx = 0.f, mexy = 0.f, msxx = 0.f, msxy = 0.f, mp = 0.f;
+          float mvx = 0.f, mvy = 0.f, me = 0.f;
+          if (PLAIN) {
+            phi = a.m.phi[idx]; mexx = a.m.exx[idx]; mexy = a.m.exy[idx];
+            msxx = a.m.sxx[idx]; msxy = a.m.sxy[idx]; mp = a.m.p[idx];
+            mvx = a.m.vx[idx]; mvy = a.m.vy[idx]; me = a.m.e[idx];
+          }
           bool changed = false, tk_set = false;
           if (a.do_n2m) {
             if (in_strict && t < 50 && tk <= 0.f) {
