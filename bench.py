@@ -212,17 +212,65 @@ def cpu_baseline(steps: int = 3, warmup: int = 1, threads: int | None = None) ->
             "seconds_per_step": secs}
 
 
+def reference_full(args, threads: int | None = None) -> dict:
+    """The reference's routines (oracle/_ref/v2c_ref_full: contraction
+    allowed, arrays sized for the full C4 configuration) on the GPU arm's
+    own workload -- the same configuration, seed and time step -- with all
+    host cores: W warm-up and K timed steps of the full MIC step, the
+    per-stage seconds only coming back."""
+    import oracle
+    from oracle import bindings as B
+    from velo2cycles_gb300 import synth
+
+    oracle.build()
+    if not os.path.exists(B.reference_path(full=True)):
+        raise RuntimeError("full-size reference build unavailable")
+    import gc
+    import subprocess
+    import tempfile
+
+    threads = threads or os.cpu_count() or 1
+    case = synth.make_case(args.config, seed=1, interpolationmod=args.interpolationmod)
+    n, xn, yn = case.n, case.params["xnumx"], case.params["ynumy"]
+    with tempfile.TemporaryDirectory(dir=B.scratch_dir(case)) as d:
+        cp, rp = os.path.join(d, "case.bin"), os.path.join(d, "res.bin")
+        B.write_case(cp, case, B.ALL_STAGES | B.TIMING_ONLY, threads, args.steps, args.warmup)
+        del case  # the reference process holds its own copy (~20 GB at C4)
+        gc.collect()
+        r = subprocess.run([B.reference_path(full=True), cp, rp], cwd=d, capture_output=True,
+                           env=dict(os.environ, OMP_NUM_THREADS=str(threads)),
+                           preexec_fn=B.big_stack, timeout=3600)
+        if r.returncode != 0:
+            raise RuntimeError(f"v2c_ref_full failed ({r.returncode}): "
+                               f"{r.stderr.decode()[-500:]}")
+        res = B.read_result(rp, 0)
+    secs = float(res["seconds"][:6].sum()) / args.steps
+    return {"value": n / secs, "unit": UNIT, "cores": threads, "kind": "reference",
+            "value_1thread": None,
+            "sample": f"the full {args.config} workload ({xn}x{yn} grid lines, {n} markers), "
+                      f"{args.warmup} warm-up + {args.steps} timed steps, full MIC step, "
+                      "FP contraction allowed",
+            "seconds_per_step": secs, "same_config": True}
+
+
 # ------------------------------------------------------- reference arm
 def run_reference_arm(args, rank: int) -> None:
     if rank != 0:
         return
-    base = cpu_baseline(steps=args.steps, warmup=args.warmup)
+    try:
+        base = reference_full(args)
+    except Exception as e:  # no full-size build or not enough host memory: the window
+        log(f"[bench] reference on the full workload unavailable ({e}); timing the window")
+        base = dict(cpu_baseline(steps=args.steps, warmup=args.warmup), same_config=False)
     line = {
         "impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": base["seconds_per_step"] * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "c4 marker-in-cell step (bounded window, see cpu_baseline.sample)"},
+        "config": {"workload": (f"{args.config} marker-in-cell step, full workload"
+                                if base["same_config"] else
+                                "c4 marker-in-cell step (bounded window, see cpu_baseline.sample)")},
+        "same_config": base["same_config"],
         "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample",
                                               "value_1thread")},
         "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0,

@@ -3,6 +3,8 @@ from __future__ import annotations
 
 import ctypes
 import os
+import resource
+import shutil
 import subprocess
 import tempfile
 
@@ -18,10 +20,13 @@ def restatement_path() -> str:
     return os.path.join(OUT, "liboracle.so")
 
 
-def reference_path(serial: bool = False, fast: bool = False) -> str:
+def reference_path(serial: bool = False, fast: bool = False, full: bool = False) -> str:
     """The reference routines built with OpenMP (v2c_ref), with the OpenMP
     pragmas ignored (v2c_ref_serial), or with OpenMP and floating-point
-    contraction allowed (v2c_ref_fast: the timed baseline)."""
+    contraction allowed (v2c_ref_fast: the timed baseline; v2c_ref_full: the
+    same with the arrays of the full C4 configuration)."""
+    if full:
+        return os.path.join(OUT, "v2c_ref_full")
     if fast:
         return os.path.join(OUT, "v2c_ref_fast")
     return os.path.join(OUT, "v2c_ref_serial" if serial else "v2c_ref")
@@ -361,6 +366,9 @@ SAVE_STAGE = 1 << 12
 # steps: the result holds the CSR arrays gausmat4_add built ("stokes": ia,
 # ja, a, b); needs the stokes= argument (v2c_stokes_ctl values)
 STOKES_STAGE = 1 << 13
+# timing only: the result holds the per-stage seconds and the deltas, no
+# arrays (a full C4 state is ~16 GB each way)
+TIMING_ONLY = 1 << 14
 STOKES_KEYS = ("mukoef", "dt", "gxkoef", "gykoef", "timebond", "drunkensailor")
 
 
@@ -425,7 +433,12 @@ def read_csr(path: str) -> dict:
 
 def read_result(path: str, nodenum: int):
     with open(path, "rb") as f:
-        assert f.read(8) == b"V2CRES01"
+        magic = f.read(8)
+        if magic == b"V2CSEC01":
+            secs = np.fromfile(f, dtype=np.float64, count=8)
+            deltas = float(np.fromfile(f, dtype=np.float64, count=1)[0])
+            return dict(seconds=secs, deltas=deltas)
+        assert magic == b"V2CRES01"
         n = int(np.fromfile(f, dtype=np.int64, count=1)[0])
         nodes = {k: np.fromfile(f, dtype=np.float64, count=nodenum) for k in range(abi.NF_N)}
         marks = {k: np.fromfile(f, dtype=np.float64, count=n) for k in range(abi.MF_N)}
@@ -438,27 +451,56 @@ def read_result(path: str, nodenum: int):
                 timestep_rc=ts_rc, timestep=info.to_dict())
 
 
+def big_stack():
+    """A 1 GB main-thread stack for the reference process: its boundary
+    corrections keep two node arrays on the stack (vxvy_boundarycorrection,
+    momentum_continuity_addmatrix_checkerror.c:1009), 64 MB at C4, beyond
+    the usual 8 MB limit."""
+    lim = 1 << 30
+    soft, hard = resource.getrlimit(resource.RLIMIT_STACK)
+    if hard != resource.RLIM_INFINITY:
+        lim = min(lim, hard)
+    if soft == resource.RLIM_INFINITY or soft < lim:
+        resource.setrlimit(resource.RLIMIT_STACK, (lim, hard))
+
+
+def scratch_dir(case):
+    """Where the case file goes: memory-backed /dev/shm when it holds the
+    case with room to spare, else the default temporary directory."""
+    need = 8 * (case.nodenum * abi.NF_N + case.n * (abi.MF_N + 1)) * 1.5
+    try:
+        if shutil.disk_usage("/dev/shm").free > need:
+            return "/dev/shm"
+    except OSError:
+        pass
+    return None
+
+
 def run_reference(case, stages=ALL_STAGES, nthreads=1, nsteps=1, warmup=0, timeout=3600,
                   timestep=None, oldornew=0, dts=None, heatdif=None, stokes=None,
-                  serial=False, fast=False):
+                  serial=False, fast=False, full=False):
     """Run the reference routines on `case`; returns the arrays after the
     stages plus per-stage seconds summed over the timed steps.  serial: the
     build with the OpenMP pragmas ignored; fast: the build with
-    floating-point contraction (timing only)."""
+    floating-point contraction (timing only); full: that build with the
+    arrays of the full C4 configuration (stages & TIMING_ONLY for a
+    seconds-only result)."""
     if not reference_available():
         build()
     if not reference_available():
         raise RuntimeError("reference oracle not built (reference sources unavailable)")
-    with tempfile.TemporaryDirectory() as d:
+    if full and not os.path.exists(reference_path(full=True)):
+        raise RuntimeError("full-size reference build unavailable")
+    with tempfile.TemporaryDirectory(dir=scratch_dir(case)) as d:
         cp, rp = os.path.join(d, "case.bin"), os.path.join(d, "res.bin")
         write_case(cp, case, stages, nthreads, nsteps, warmup, timestep, oldornew, dts, heatdif,
                    stokes)
         env = dict(os.environ, OMP_NUM_THREADS=str(max(1, nthreads)))
-        exe = reference_path(serial, fast)
+        exe = reference_path(serial, fast, full)
         if fast and not os.path.exists(exe):
             exe = reference_path(serial)
         r = subprocess.run([exe, cp, rp], env=env, capture_output=True,
-                           timeout=timeout, cwd=d)
+                           timeout=timeout, cwd=d, preexec_fn=big_stack)
         if r.returncode != 0:
             raise RuntimeError(f"v2c_ref failed ({r.returncode}): {r.stderr.decode()[-2000:]}")
         res = read_result(rp, case.nodenum)

@@ -67,3 +67,35 @@ if [ -f "$OUT/src/headevps.c" ]; then
 else
   echo "build_ref.sh: reference sources not found; built the restatement only" >&2
 fi
+
+# 4. oracle/_ref/v2c_ref_full -- the timed build (contraction allowed, as
+#    2b) with the arrays raised to the full C4 configuration: 4001 x 1001
+#    grid lines, 80.1 M markers, ~24 GB of static arrays.  That is beyond the
+#    default code model's reach on both architectures (x86-64: medium model;
+#    AArch64: the large model, which needs a non-PIE executable).  Optional:
+#    where it does not build, the reference arm times the window instead.
+if [ -n "$REF" ] && [ -d "$REF/src" ]; then
+  mkdir -p "$OUT/src_full"
+  for f in $FILES; do cp "$REF/src/$f" "$OUT/src_full/$f"; done
+  # MAXMAT: the boundary corrections of marker2nodes collect ~2 entries
+  # per node in val0[] (8.0 M at C4)
+  sed -i \
+    -e 's/^#define MAXMAT .*/#define MAXMAT  40000000/' \
+    -e 's/^#define MAXVAL .*/#define MAXVAL  24000000/' \
+    -e 's/^#define MAXXLN .*/#define MAXXLN  4001/' \
+    -e 's/^#define MAXYLN .*/#define MAXYLN  1001/' \
+    -e 's/^#define MAXMRK .*/#define MAXMRK  80100001/' \
+    "$OUT/src_full/headevps.c"
+fi
+if [ -f "$OUT/src_full/headevps.c" ]; then
+  case "$(uname -m)" in
+    x86_64) FULL="-mcmodel=medium" ;;
+    aarch64) FULL="-mcmodel=large -fno-pie -no-pie" ;;
+    *) FULL="" ;;
+  esac
+  if ! $CC -std=gnu99 -O3 -fopenmp -fcommon -w -ffp-contract=fast $FULL \
+      -I"$OUT/src_full" -I"$HERE/../include" -o "$OUT/v2c_ref_full" "$HERE/ref_harness.c" -lm; then
+    echo "build_ref.sh: the full-size reference build failed; the reference arm times a window" >&2
+    rm -f "$OUT/v2c_ref_full"
+  fi
+fi

@@ -174,3 +174,51 @@ def test_async_node_download(built_lib):
     for f in f2:
         assert np.array_equal(got2[f], want2[f]), f
     m.close()
+
+
+def test_pinned_node_transfers(built_lib):
+    """Node fields to and from pinned host buffers (direct asynchronous
+    copies, as the end-to-end bench uses) equal the same transfers through
+    pageable buffers (staged by the driver): upload, synchronous and
+    asynchronous download, with an odd node count and a single field."""
+    torch = pytest.importorskip("torch")
+    c = synth.make_case("small", seed=9)
+    m = mic.from_case(c)
+    m.marker2nodes()
+
+    def pinned(a=None):
+        t = torch.empty(c.nodenum, dtype=torch.float64, pin_memory=True)
+        if a is not None:
+            t.copy_(torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)))
+        return t.numpy()
+
+    fields = [abi.NF_NU_M2C, abi.NF_GG, abi.NF_SXXE, abi.NF_MVX, abi.NF_TK]
+    want = m.download_nodes(fields)  # pageable
+    got = {f: pinned() for f in fields}
+    m.download_nodes(fields, into=got)
+    for f in fields:
+        assert np.array_equal(got[f], want[f]), f
+    one = {abi.NF_RO: pinned()}
+    m.download_nodes([abi.NF_RO], into=one)
+    assert np.array_equal(one[abi.NF_RO], m.download_nodes([abi.NF_RO])[abi.NF_RO])
+    got_a = {f: pinned() for f in fields}
+    got_a[fields[0]][:] = np.nan
+    m.download_nodes_async(got_a)
+    m.interpolate_center2basic_old()
+    m.wait_downloads()
+    for f in fields:
+        assert np.array_equal(got_a[f], want[f]), f
+    # upload from pinned buffers, then read back through the pageable path
+    rng = np.random.default_rng(3)
+    up = {abi.NF_VX: rng.normal(size=c.nodenum), abi.NF_PR: rng.normal(size=c.nodenum) * 1e8,
+          abi.NF_SXY: rng.normal(size=c.nodenum) * 1e6}
+    m.upload_nodes(up)
+    m.synchronize()
+    ref = m.download_nodes(list(up))
+    m.upload_nodes({f: np.zeros(c.nodenum) for f in up})
+    m.upload_nodes({f: pinned(v) for f, v in up.items()})
+    m.synchronize()
+    back = m.download_nodes(list(up))
+    for f in up:
+        assert np.array_equal(back[f], ref[f]), f
+    m.close()
