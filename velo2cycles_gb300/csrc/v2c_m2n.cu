@@ -58,51 +58,89 @@ struct Smem {
   uint8_t act[CHUNK + SKEW];
 };
 
-// stage one marker's scatter payload; the per-marker physics (viscosity,
-// conductivity, density, state update) was done by the marker physics kernel
-__device__ __forceinline__ void stage(const M2NArgs &a, Smem &sm, int s, int k, int jlo) {
+// 4-byte asynchronous copy global -> shared (no register holds the value)
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Stage the chunk [cs, ce) of column ci's sorted markers, PER per thread,
+// all of a thread's markers at once: the sort indices, then the cells and
+// types, then every field by asynchronous copies straight into the
+// marker's slot (three rounds of memory latency per chunk rather than
+// three per marker, and no register holds a field).  Once a thread's own
+// copies have landed, the payload formed from them: strictly inside the
+// model (interpolation.c:219), the viscosity over the shear modulus, the
+// dencalcomp adiabatic term and the rock-table constants.  The per-marker
+// physics (viscosity, conductivity, density, state update) was done by the
+// marker physics kernel.
+constexpr int PER = CHUNK / NTH;
+static_assert(PER * NTH == CHUNK, "chunk = whole staging rounds");
+__device__ __forceinline__ void stage_chunk(const M2NArgs &a, Smem &sm, int cs, int ce, int ci,
+                                            int jlo, int tid) {
   const Grid &g = a.g;
-  const int idx = __ldg(a.perm + s);
-  const int c = a.m.cell_in[idx];
-  const int ix = c / g.ncy, iy = c - ix * g.ncy;
-  k += iy - jlo;  // the skew of the cell's run (Smem)
-  const float u = a.m.u_in[idx], v = a.m.v_in[idx];
-  const int t = a.m.type[idx];
-  // strictly inside the model (interpolation.c:219)
-  bool act = true;
-  if (ix == 0 || ix == g.ncx - 1) {
-    double x = g.gx[ix] + (double)u * (g.gx[ix + 1] - g.gx[ix]);
-    act = act && x > 0 && x < g.xsize;
+  int idx[PER], q[PER], t[PER];
+#pragma unroll
+  for (int j = 0; j < PER; j++) {
+    const int s = cs + tid + j * NTH;
+    idx[j] = s < ce ? __ldg(a.perm + s) : -1;
   }
-  if (iy == 0 || iy == g.ncy - 1) {
-    double y = g.gy[iy] + (double)v * (g.gy[iy + 1] - g.gy[iy]);
-    act = act && y > 0 && y < g.ysize;
+#pragma unroll
+  for (int j = 0; j < PER; j++) {
+    q[j] = -1;
+    if (idx[j] < 0) continue;
+    // slot: the position in the chunk plus the skew of the cell's run (Smem)
+    q[j] = tid + j * NTH + a.m.cell_in[idx[j]] - ci * g.ncy - jlo;
+    t[j] = a.m.type[idx[j]];
   }
-  sm.act[k] = act;
-  if (!act) return;
-  const float T = a.m.tk[idx];
-  const float mnu = a.m.mnu[idx];
-  const float bb = a.R(RK_BB, t);
-  sm.p[P_U][k] = u;
-  sm.p[P_V][k] = v;
-  sm.p[P_NU][k] = mnu;
-  sm.p[P_NUG][k] = mnu * a.R(RK_INV_GG, t);
-  sm.p[P_E][k] = a.m.e[idx];
-  sm.p[P_SXY][k] = a.m.sxy[idx];
-  sm.p[P_EXY][k] = a.m.exy[idx];
-  sm.p[P_COH][k] = a.m.coh[idx];
-  sm.p[P_PHI][k] = a.m.phi[idx];
-  sm.p[P_RO][k] = a.S.p.densimod ? a.m.mro[idx] : a.R(RK_RO, t);
-  sm.p[P_ET][k] = __fdividef(bb, 1.f - bb * (T - 298.15f));  // dencalcomp adiabatic term
-  sm.p[P_HT][k] = a.R(RK_HT, t);
-  sm.p[P_CP][k] = a.R(RK_CP, t);
-  sm.p[P_KT][k] = a.m.mkt[idx];
-  sm.p[P_TK][k] = T;
-  sm.p[P_SXX][k] = a.m.sxx[idx];
-  sm.p[P_EXX][k] = a.m.exx[idx];
-  sm.p[P_P][k] = a.m.p[idx];
-  sm.p[P_VX][k] = a.m.vx[idx];
-  sm.p[P_VY][k] = a.m.vy[idx];
+#pragma unroll
+  for (int j = 0; j < PER; j++) {
+    if (q[j] < 0) continue;
+    const int i = idx[j], kk = q[j];
+    cp_async4(&sm.p[P_U][kk], a.m.u_in + i);
+    cp_async4(&sm.p[P_V][kk], a.m.v_in + i);
+    cp_async4(&sm.p[P_NU][kk], a.m.mnu + i);
+    cp_async4(&sm.p[P_E][kk], a.m.e + i);
+    cp_async4(&sm.p[P_SXY][kk], a.m.sxy + i);
+    cp_async4(&sm.p[P_EXY][kk], a.m.exy + i);
+    cp_async4(&sm.p[P_COH][kk], a.m.coh + i);
+    cp_async4(&sm.p[P_PHI][kk], a.m.phi + i);
+    if (a.S.p.densimod) cp_async4(&sm.p[P_RO][kk], a.m.mro + i);
+    cp_async4(&sm.p[P_KT][kk], a.m.mkt + i);
+    cp_async4(&sm.p[P_TK][kk], a.m.tk + i);
+    cp_async4(&sm.p[P_SXX][kk], a.m.sxx + i);
+    cp_async4(&sm.p[P_EXX][kk], a.m.exx + i);
+    cp_async4(&sm.p[P_P][kk], a.m.p + i);
+    cp_async4(&sm.p[P_VX][kk], a.m.vx + i);
+    cp_async4(&sm.p[P_VY][kk], a.m.vy + i);
+  }
+  cp_async_wait_all();
+#pragma unroll
+  for (int j = 0; j < PER; j++) {
+    if (q[j] < 0) continue;
+    const int k = q[j], tt = t[j];
+    const int iy = jlo + k - (tid + j * NTH);
+    const float u = sm.p[P_U][k], v = sm.p[P_V][k];
+    bool act = true;
+    if (ci == 0 || ci == g.ncx - 1) {
+      double x = g.gx[ci] + (double)u * (g.gx[ci + 1] - g.gx[ci]);
+      act = act && x > 0 && x < g.xsize;
+    }
+    if (iy == 0 || iy == g.ncy - 1) {
+      double y = g.gy[iy] + (double)v * (g.gy[iy + 1] - g.gy[iy]);
+      act = act && y > 0 && y < g.ysize;
+    }
+    sm.act[k] = act;
+    const float bb = a.R(RK_BB, tt), T = sm.p[P_TK][k];
+    sm.p[P_NUG][k] = sm.p[P_NU][k] * a.R(RK_INV_GG, tt);
+    if (!a.S.p.densimod) sm.p[P_RO][k] = a.R(RK_RO, tt);
+    sm.p[P_ET][k] = __fdividef(bb, 1.f - bb * (T - 298.15f));  // dencalcomp adiabatic term
+    sm.p[P_HT][k] = a.R(RK_HT, tt);
+    sm.p[P_CP][k] = a.R(RK_CP, tt);
+  }
 }
 
 // calc_frictionpara_nodes (calc_RSF.c:298-350), FP64; out of line, taken
@@ -382,7 +420,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_m2n(M2NArgs a) {
       for (int cs = seg_b; cs < seg_e; cs += CHUNK) {
         const int ce = min(cs + CHUNK, seg_e);
         __syncthreads();
-        for (int k = tid; k < ce - cs; k += NTH) stage(a, sm, cs + k, k, jlo);
+        stage_chunk(a, sm, cs, ce, ci, jlo, tid);
         __syncthreads();
 // the staged markers of sorted positions [b, e) (one quarter class run)
 #define CLASS_RUN(b, e, r) \

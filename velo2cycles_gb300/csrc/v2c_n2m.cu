@@ -274,9 +274,19 @@ __global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
       for (int cs = seg_b; cs < seg_e; cs += CHUNK) {
         const int ce = min(cs + CHUNK, seg_e);
         if (backscatter) __syncthreads();
-        for (int k = tid; k < ce - cs; k += NTH) {
+        // the chunk's sort indices of this thread, read together (three
+        // markers per thread: one round of latency rather than three)
+        static_assert(CHUNK == 3 * NTH, "three staging rounds per chunk");
+        int pidx[3];
+#pragma unroll
+        for (int jj = 0; jj < 3; jj++)
+          pidx[jj] = tid + jj * NTH < ce - cs ? __ldg(a.perm + cs + tid + jj * NTH) : 0;
+#pragma unroll 1
+        for (int jj = 0; jj < 3; jj++) {
+          const int k = tid + jj * NTH;
+          if (k >= ce - cs) break;
           // ---------------------------------------------- stage marker
-          const int idx = __ldg(a.perm + cs + k);
+          const int idx = jj == 0 ? pidx[0] : (jj == 1 ? pidx[1] : pidx[2]);
           const int c = a.m.cell_in[idx];
           const int ix = c / ncy, iy = c - ix * ncy;
           const float u = a.m.u_in[idx], v = a.m.v_in[idx];
