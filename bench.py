@@ -366,7 +366,9 @@ def run_gpu(args, rank: int, world: int) -> None:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     t0 = time.time()
-    case = synth.make_case(args.config, seed=1 + rank, interpolationmod=args.interpolationmod)
+    window = tuple(int(v) for v in args.window.split(",")) if args.window else None
+    case = synth.make_case(args.config, seed=1 + rank, interpolationmod=args.interpolationmod,
+                           window=window)
     log(f"[bench] {args.config}: {case.n} markers, {case.nodenum} nodes, generated in "
         f"{time.time() - t0:.1f}s")
     stream = torch.cuda.Stream()
@@ -520,7 +522,8 @@ def run_gpu(args, rank: int, world: int) -> None:
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 fields, f64 node normalisation", "data": "synthetic",
-        "config": {"workload": f"{args.config}: {case.params['xnumx']}x{case.params['ynumy']} grid, "
+        "config": {"workload": f"{args.config}{' window ' + args.window if args.window else ''}: "
+                               f"{case.params['xnumx']}x{case.params['ynumy']} grid, "
                                f"{n} markers ({mpn:.1f}/node), RK4, "
                                f"interpolationmod={args.interpolationmod}, "
                                "antidiffinter=1, per-marker VEP+RSF Newton to 1e-10, learned "
@@ -884,6 +887,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c4")
+    ap.add_argument("--window", default="",
+                    help="i0,j0,nx,ny: a window of nx x ny grid lines of the configuration "
+                         "(a small case of the same spacing for profiler captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-c3", action="store_true", help="skip the Newton-only C3 block")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end loop")
