@@ -237,7 +237,7 @@ __device__ __forceinline__ void plain_values(const Grid &g, const Nodes &N, Axis
 }
 
 template <bool BS, bool PLAIN>
-__global__ void __launch_bounds__(NTH, 6) k_n2m(N2MArgs a) {
+__global__ void __launch_bounds__(NTH, 7) k_n2m(N2MArgs a) {
   __shared__ Smem sm;
   const Grid &g = a.g;
   const Nodes &N = a.N;
@@ -274,36 +274,23 @@ __global__ void __launch_bounds__(NTH, 6) k_n2m(N2MArgs a) {
       for (int cs = seg_b; cs < seg_e; cs += CHUNK) {
         const int ce = min(cs + CHUNK, seg_e);
         if (backscatter) __syncthreads();
-        // the chunk's sort indices of this thread, then their cells,
-        // offsets, types and temperatures, read together (three markers per
-        // thread: two rounds of latency rather than six; every marker of the
-        // strip is in column ci).  At 6 resident CTAs (80 registers) these
-        // fit; at 7 (72 registers) they spill and the gather is slower.
+        // the chunk's sort indices of this thread, read together (three
+        // markers per thread: one round of latency rather than three)
         static_assert(CHUNK == 3 * NTH, "three staging rounds per chunk");
-        int pidx[3], pc[3], pt[3];
-        float pu[3], pv[3], ptk[3];
+        int pidx[3];
 #pragma unroll
         for (int jj = 0; jj < 3; jj++)
           pidx[jj] = tid + jj * NTH < ce - cs ? __ldg(a.perm + cs + tid + jj * NTH) : 0;
-#pragma unroll
-        for (int jj = 0; jj < 3; jj++) {
-          pc[jj] = a.m.cell_in[pidx[jj]];
-          pu[jj] = a.m.u_in[pidx[jj]];
-          pv[jj] = a.m.v_in[pidx[jj]];
-          pt[jj] = a.m.type[pidx[jj]];
-          ptk[jj] = a.m.tk[pidx[jj]];
-        }
 #pragma unroll 1
         for (int jj = 0; jj < 3; jj++) {
           const int k = tid + jj * NTH;
           if (k >= ce - cs) break;
           // ---------------------------------------------- stage marker
           const int idx = jj == 0 ? pidx[0] : (jj == 1 ? pidx[1] : pidx[2]);
-          const int c = jj == 0 ? pc[0] : (jj == 1 ? pc[1] : pc[2]);
-          const int ix = ci, iy = c - ci * ncy;
-          const float u = jj == 0 ? pu[0] : (jj == 1 ? pu[1] : pu[2]);
-          const float v = jj == 0 ? pv[0] : (jj == 1 ? pv[1] : pv[2]);
-          const int t = jj == 0 ? pt[0] : (jj == 1 ? pt[1] : pt[2]);
+          const int c = a.m.cell_in[idx];
+          const int ix = c / ncy, iy = c - ix * ncy;
+          const float u = a.m.u_in[idx], v = a.m.v_in[idx];
+          const int t = a.m.type[idx];
           const bool owned = owned_col && iy >= j0 && iy < j0 + TY;
           if (!owned && !backscatter) continue;
           // interpolate_mechanical clamps the point into the model first
@@ -350,7 +337,7 @@ __global__ void __launch_bounds__(NTH, 6) k_n2m(N2MArgs a) {
                                  (iy > 0 || v > 0.f) && (iy < g.ncy - 1 || v < 1.f);
           const bool in_grid = (ix > 0 || u >= 0.f) && (ix < g.ncx - 1 || u <= 1.f) &&
                                (iy > 0 || v >= 0.f) && (iy < g.ncy - 1 || v <= 1.f);
-          float tk = jj == 0 ? ptk[0] : (jj == 1 ? ptk[1] : ptk[2]);
+          float tk = a.m.tk[idx];
           // the marker's own values are read only without antidiffusion,
           // where it keeps them plus the change of the node fields; with
           // it, an updated marker takes all nine from the nodes
