@@ -130,16 +130,23 @@ __device__ __forceinline__ int4 rank_segment(const uint32_t *tmp, int32_t *perm,
     int rank = 0;
     if (L <= 32) {
       // bitonic sort of the warp's keys (padding 0xffffffff sorts last:
-      // array indices stay below 2^30 - 1, so no key equals it)
+      // array indices stay below 2^30 - 1, so no key equals it), unless
+      // they are in order already: a cell whose markers one warp of the
+      // count pass met keeps their slots in array order, and array order
+      // is class order for markers that have kept their cell and class
+      // since the markers were last stored in sorted order
       uint32_t key = val;
+      const uint32_t next = __shfl_down_sync(V2C_FULL, val, 1);
+      if (!__all_sync(V2C_FULL, lane >= L - 1 || val < next)) {
 #pragma unroll
-      for (int k = 2; k <= 32; k <<= 1)
+        for (int k = 2; k <= 32; k <<= 1)
 #pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) {
-          const uint32_t other = __shfl_xor_sync(V2C_FULL, key, j);
-          const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
-          key = keep_min ? min(key, other) : max(key, other);
-        }
+          for (int j = k >> 1; j > 0; j >>= 1) {
+            const uint32_t other = __shfl_xor_sync(V2C_FULL, key, j);
+            const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+            key = keep_min ? min(key, other) : max(key, other);
+          }
+      }
       const bool in = lane < L;
       const uint32_t q = key >> 30;
       cnt.x += __popc(__ballot_sync(V2C_FULL, in && q == 0));
