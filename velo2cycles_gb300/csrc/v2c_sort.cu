@@ -119,47 +119,51 @@ __global__ void k_slots(const int32_t *cell, const float *u, const float *v, lon
 
 constexpr uint32_t KEY_INDEX = (1u << 30) - 1;
 
-// One warp ranks the L distinct keys of a cell's slots (any order), writes
-// their indices in ascending key order and returns the count of quarter
-// classes 0, 1, 2 (same value in every lane).
-__device__ __forceinline__ int4 rank_segment(const uint32_t *tmp, int32_t *perm, int L, int lane) {
+// One warp orders the L <= 32 distinct keys of a cell's slots, held one per
+// lane in val (lanes >= L hold 0xffffffff, which sorts last: array indices
+// stay below 2^30 - 1, so no key equals it), writes their indices in
+// ascending key order and returns the counts of quarter classes 0, 1, 2
+// (same value in every lane).  The bitonic network is skipped when the
+// keys are in order already: a cell whose markers one warp of the count
+// pass met keeps their slots in array order, and array order is class
+// order for markers that have kept their cell and class since the markers
+// were last stored in sorted order.
+__device__ __forceinline__ int4 rank_small(uint32_t val, int32_t *perm, int L, int lane) {
+  uint32_t key = val;
+  const uint32_t next = __shfl_down_sync(V2C_FULL, val, 1);
+  if (!__all_sync(V2C_FULL, lane >= L - 1 || val < next)) {
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        const uint32_t other = __shfl_xor_sync(V2C_FULL, key, j);
+        const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+        key = keep_min ? min(key, other) : max(key, other);
+      }
+  }
+  const bool in = lane < L;
+  const uint32_t q = key >> 30;
+  int4 cnt;
+  cnt.x = __popc(__ballot_sync(V2C_FULL, in && q == 0));
+  cnt.y = __popc(__ballot_sync(V2C_FULL, in && q == 1));
+  cnt.z = __popc(__ballot_sync(V2C_FULL, in && q == 2));
+  cnt.w = 0;
+  if (in) perm[lane] = (int32_t)(key & KEY_INDEX);
+  return cnt;
+}
+
+// The same for a cell of L > 32 keys (read from tmp): each key's rank is
+// the number of the cell's keys below it.
+__device__ __noinline__ int4 rank_large(const uint32_t *tmp, int32_t *perm, int L, int lane) {
   int4 cnt = make_int4(0, 0, 0, 0);
   for (int b = 0; b < L; b += 32) {
     const int jj = b + lane;
     const uint32_t val = (jj < L) ? tmp[jj] : 0xffffffffu;
     int rank = 0;
-    if (L <= 32) {
-      // bitonic sort of the warp's keys (padding 0xffffffff sorts last:
-      // array indices stay below 2^30 - 1, so no key equals it), unless
-      // they are in order already: a cell whose markers one warp of the
-      // count pass met keeps their slots in array order, and array order
-      // is class order for markers that have kept their cell and class
-      // since the markers were last stored in sorted order
-      uint32_t key = val;
-      const uint32_t next = __shfl_down_sync(V2C_FULL, val, 1);
-      if (!__all_sync(V2C_FULL, lane >= L - 1 || val < next)) {
-#pragma unroll
-        for (int k = 2; k <= 32; k <<= 1)
-#pragma unroll
-          for (int j = k >> 1; j > 0; j >>= 1) {
-            const uint32_t other = __shfl_xor_sync(V2C_FULL, key, j);
-            const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
-            key = keep_min ? min(key, other) : max(key, other);
-          }
-      }
-      const bool in = lane < L;
-      const uint32_t q = key >> 30;
-      cnt.x += __popc(__ballot_sync(V2C_FULL, in && q == 0));
-      cnt.y += __popc(__ballot_sync(V2C_FULL, in && q == 1));
-      cnt.z += __popc(__ballot_sync(V2C_FULL, in && q == 2));
-      if (in) perm[lane] = (int32_t)(key & KEY_INDEX);
-      continue;
-    } else {
-      for (int b2 = 0; b2 < L; b2 += 32) {
-        const uint32_t other = (b2 + lane < L) ? tmp[b2 + lane] : 0xffffffffu;
+    for (int b2 = 0; b2 < L; b2 += 32) {
+      const uint32_t other = (b2 + lane < L) ? tmp[b2 + lane] : 0xffffffffu;
 #pragma unroll 8
-        for (int k = 0; k < 32; k++) rank += (__shfl_sync(V2C_FULL, other, k) < val);
-      }
+      for (int k = 0; k < 32; k++) rank += (__shfl_sync(V2C_FULL, other, k) < val);
     }
     const bool in = jj < L;
     const uint32_t q = val >> 30;
@@ -171,31 +175,46 @@ __device__ __forceinline__ int4 rank_segment(const uint32_t *tmp, int32_t *perm,
   return cnt;
 }
 
-// one warp per cell: rank each key among the cell's keys (all distinct) and
-// write the quarter class starts; the largest cell count goes to the status
-// counter once per block
+// One warp per RG consecutive cells: their starts in one read, each cell's
+// keys read while the previous cell is ranked, their quarter class starts
+// written together; the largest cell count goes to the status counter once
+// per block.
+constexpr int RG = 8;
 __global__ void k_rank(const int32_t *start, long ncell, const uint32_t *tmp, int32_t *perm,
                        int4 *qstart, unsigned long long *stat) {
   __shared__ int bmax;
   if (threadIdx.x == 0) bmax = 0;
   __syncthreads();
-  const long c = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  const long c0 = ((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5) * RG;
   const int lane = threadIdx.x & 31;
-  if (c < ncell) {
-    const int s = start[c], L = start[c + 1] - s;
-    if (lane == 0 && L > 0) atomicMax(&bmax, L);
-    int4 cnt = make_int4(0, 0, 0, 0);
-    if (L == 1) {
-      const uint32_t key = tmp[s];
-      if (lane == 0) perm[s] = (int32_t)(key & KEY_INDEX);
-      const int q = (int)(key >> 30);
-      cnt = make_int4(q == 0, q == 1, q == 2, 0);
-    } else if (L > 1) {
-      cnt = rank_segment(tmp + s, perm + s, L, lane);
+  if (c0 < ncell) {
+    const int sv = (lane <= RG && c0 + lane <= ncell) ? start[c0 + lane] : 0;
+    const int ng = (int)min((long)RG, ncell - c0);
+    int s = __shfl_sync(V2C_FULL, sv, 0), L = __shfl_sync(V2C_FULL, sv, 1) - s;
+    uint32_t val = (lane < L && L <= 32) ? tmp[s + lane] : 0xffffffffu;
+    int4 myq = make_int4(0, 0, 0, 0);
+    int lmax = 0;
+    for (int g = 0; g < ng; g++) {
+      // the next cell's keys
+      int s1 = 0, L1 = 0;
+      uint32_t val1 = 0xffffffffu;
+      if (g + 1 < ng) {
+        s1 = __shfl_sync(V2C_FULL, sv, g + 1);
+        L1 = __shfl_sync(V2C_FULL, sv, g + 2) - s1;
+        if (lane < L1 && L1 <= 32) val1 = tmp[s1 + lane];
+      }
+      lmax = max(lmax, L);
+      int4 cnt = make_int4(0, 0, 0, 0);
+      if (L > 32) cnt = rank_large(tmp + s, perm + s, L, lane);
+      else if (L > 0) cnt = rank_small(val, perm + s, L, lane);
+      if (lane == g)
+        myq = make_int4(s, s + cnt.x, s + cnt.x + cnt.y, s + cnt.x + cnt.y + cnt.z);
+      s = s1; L = L1; val = val1;
     }
+    if (lane < ng) qstart[c0 + lane] = myq;
     if (lane == 0) {
-      qstart[c] = make_int4(s, s + cnt.x, s + cnt.x + cnt.y, s + cnt.x + cnt.y + cnt.z);
-      if (c == ncell - 1) {
+      if (lmax > 0) atomicMax(&bmax, lmax);
+      if (c0 + ng == ncell) {
         const int e = start[ncell];
         qstart[ncell] = make_int4(e, e, e, e);
       }
@@ -278,7 +297,8 @@ void launch_sort(const int32_t *cell, const float *u, const float *v, long n, lo
   k_scan_add<<<nblk(ncell, 256), 256, 0, st>>>(b.start, ncell, b.blocksum);
   uint32_t *keys = reinterpret_cast<uint32_t *>(b.tmp);
   if (n > 0) k_slots<<<nblk(n, 256), 256, 0, st>>>(cell, u, v, n, b.start, b.slot, keys);
-  k_rank<<<nblk(ncell * 32, 256), 256, 0, st>>>(b.start, ncell, keys, b.perm, b.qstart, stat);
+  k_rank<<<nblk((ncell + RG - 1) / RG * 32, 256), 256, 0, st>>>(b.start, ncell, keys, b.perm,
+                                                                 b.qstart, stat);
 }
 
 void launch_f64_to_f32(const double *src, float *dst, long n, cudaStream_t st) {
