@@ -51,6 +51,14 @@ def _dev(a: np.ndarray, dtype=None):
     return t
 
 
+def _torch_done(t) -> None:
+    """Wait for the torch work queued on t's device (the fills of output
+    buffers, the kernels that made the inputs): the library runs on its
+    context's stream, which nothing orders after torch's."""
+    import torch
+    torch.cuda.current_stream(t.device).synchronize()
+
+
 def solve(mic, states, guess: int = abi.GUESS_PLAIN, on_device: bool = False):
     """Solve every state; returns (out[V2C_RO_N, n], iterations[n]) as numpy
     (or torch device tensors when on_device).  Negative iteration counts
@@ -60,6 +68,7 @@ def solve(mic, states, guess: int = abi.GUESS_PLAIN, on_device: bool = False):
     n = S.shape[1]
     out = torch.zeros((abi.RO_N, n), dtype=torch.float64, device=S.device)
     it = torch.zeros(n, dtype=torch.int32, device=S.device)
+    _torch_done(S)
     call("v2c_rsf_newton", mic.h, ctypes.c_void_p(S.data_ptr()), n, int(guess),
          ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(it.data_ptr()))
     mic.synchronize()
@@ -76,6 +85,7 @@ def collect_states(mic, stride: int = 1, cap: int | None = None):
     n = mic.n
     cap = cap if cap is not None else (n + stride - 1) // stride
     X = torch.empty((abi.RS_N, cap), dtype=torch.float64, device="cuda")
+    _torch_done(X)
     got = ctypes.c_long()
     call("v2c_collect_newton_states", mic.h, int(stride), ctypes.c_void_p(X.data_ptr()), int(cap),
          ctypes.byref(got))
@@ -93,6 +103,7 @@ def train(mic, states, targets, epochs: int = 4, batch: int = 4096, lr: float = 
     S = states if isinstance(states, torch.Tensor) else _dev(np.asarray(states), np.float64)
     T = targets if isinstance(targets, torch.Tensor) else _dev(np.asarray(targets), np.float64)
     loss = ctypes.c_float()
+    _torch_done(S)
     call("v2c_mlp_train", mic.h, ctypes.c_void_p(S.data_ptr()), ctypes.c_void_p(T.data_ptr()),
          S.shape[1], int(epochs), int(batch), float(lr), int(seed), ctypes.byref(loss))
     return loss.value
@@ -104,6 +115,7 @@ def grad(mic, states, targets):
     T = _dev(np.asarray(targets), np.float64)
     g = np.zeros(abi.MLP_NPARAM - 20, dtype=np.float32)
     loss = ctypes.c_float()
+    _torch_done(S)
     call("v2c_mlp_grad", mic.h, ctypes.c_void_p(S.data_ptr()), ctypes.c_void_p(T.data_ptr()),
          S.shape[1], g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(loss))
     return g, loss.value
@@ -114,6 +126,7 @@ def infer(mic, states) -> np.ndarray:
     import torch
     S = _dev(np.asarray(states), np.float64)
     out = torch.zeros((2, S.shape[1]), dtype=torch.float32, device=S.device)
+    _torch_done(S)
     call("v2c_mlp_infer", mic.h, ctypes.c_void_p(S.data_ptr()), S.shape[1],
          ctypes.c_void_p(out.data_ptr()))
     mic.synchronize()
