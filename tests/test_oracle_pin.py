@@ -339,3 +339,21 @@ def test_calc_timestep_resets_and_golden():
     after = inter & (m > m_reset) & (N[abi.NF_BS] > 0) & (N[abi.NF_RK_SLIPRS_FINAL] > 0)
     phisc = N[abi.NF_V0S][after] / N[abi.NF_LS][after] * np.exp(-N[abi.NF_PHIS][after])
     assert info["dtphi"] == min(1e12, (0.2 / phisc).min())
+
+
+@needs_ref
+def test_reference_arm_builds_time_only():
+    """The timed reference builds (FP contraction allowed; the full-size
+    one with the arrays of the whole C4 configuration, where it built):
+    a timing-only run returns the per-stage seconds and no arrays, and the
+    full-size build computes what the window build computes."""
+    c = synth.make_case("small", 4)
+    t = B.run_reference(c, stages=B.ALL_STAGES | B.TIMING_ONLY, nthreads=2, nsteps=1, fast=True)
+    assert set(t) == {"seconds", "deltas"} and t["seconds"].shape == (8,)
+    assert np.all(t["seconds"][:6] >= 0) and t["seconds"][:6].sum() > 0
+    if not os.path.exists(B.reference_path(full=True)):
+        pytest.skip("no full-size reference build here")
+    a = B.run_reference(c, nthreads=2, fast=True)
+    b = B.run_reference(c, nthreads=2, fast=True, full=True)
+    assert all(np.array_equal(a["nodes"][k], b["nodes"][k], equal_nan=True) for k in a["nodes"])
+    assert all(np.array_equal(a["marks"][k], b["marks"][k], equal_nan=True) for k in a["marks"])
