@@ -253,11 +253,16 @@ int check_params(const v2c_params *p) {
   return V2C_OK;
 }
 
-int pick_tx(const v2c_ctx *c) {
-  // widest column strip that still gives 1.5 waves of 7 resident CTAs on
-  // each of the 152 SMs; a strip of tx columns restages one halo column
+// Column strip of the sweeps: the widest up to max_tx that still gives 1.5
+// waves of 7 resident CTAs on each of the 152 SMs (a strip of tx columns
+// restages one halo column).  The scatter takes strips of at most 16
+// columns, the gather 32: at C4 (126 x 32 strips of 32 columns) the
+// scatter's 4.4 waves at 6 CTAs left SMs idle in the last one, and 16
+// columns (8.8 waves, 3 % more halo work) ran 5.17 -> 5.01 ms, while the
+// gather ran 4.80 -> 4.86 ms with them.
+int pick_tx(const v2c_ctx *c, int max_tx) {
   long rows = (c->yn + 31) / 32;
-  int tx = 32;
+  int tx = max_tx;
   while (tx > 4 && rows * ((c->xn + tx - 1) / tx) < 152 * 7 * 3 / 2) tx /= 2;
   return tx;
 }
@@ -971,7 +976,7 @@ extern "C" int v2c_marker2nodes(v2c_ctx *ctx) {
   a.stat = ctx->d_stat;
   a.gxf = ctx->d_gxf;
   a.gyf = ctx->d_gyf;
-  a.TX = pick_tx(ctx);
+  a.TX = pick_tx(ctx, 16);
   a.n = ctx->n;
   CK(cudaMemsetAsync(ctx->d_sticky, 0, sizeof(uint32_t) * ctx->nn, st));
   ctx->dsxx_valid = false;  // the scatter writes sxxe
@@ -1142,7 +1147,7 @@ static int n2m_move(v2c_ctx *ctx, int do_n2m, int do_move) {
   a.gyf = ctx->d_gyf;
   a.quad = ctx->d_quad;
   a.n = ctx->n;
-  a.TX = pick_tx(ctx);
+  a.TX = pick_tx(ctx, 32);
   a.do_n2m = 1;
   if (do_n2m && ctx->p.interpolationmod == 1 && ctx->p.antidiffinter == 1) {
     // the full-stencil back-scatter: one payload record per marker
